@@ -1,0 +1,168 @@
+"""ctypes binding of ``libck_gb300.so`` (the C ABI of ``include/commkit_gb300.h``).
+
+The library is built in-tree (``python -m commkit_gb300.build``).  There is
+no fallback: if it is missing, :func:`lib` raises ``ImportError`` and every
+device function of the package fails with it.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import threading
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_lib" / "libck_gb300.so"
+
+CK_OK = 0
+CK_ERR_INVALID_ARGUMENT = 1
+CK_ERR_UNSUPPORTED = 2
+CK_ERR_CUDA = 3
+CK_ERR_OUT_OF_MEMORY = 4
+CK_ERR_DEVICE_TIMEOUT = 5
+
+CK_LLR_MAX_K = 16
+CK_LDPC_MIN_SUM = 0
+CK_LDPC_SUM_PRODUCT = 1
+CK_LDPC_PLACE_AUTO = 0
+CK_LDPC_PLACE_SHARED = 1
+CK_LDPC_PLACE_GLOBAL = 2
+
+# Every symbol the header declares; tests check the library exports them.
+EXPORTS = (
+    "ck_last_error",
+    "ck_status_string",
+    "ck_version",
+    "ck_llr_separable_maxlog",
+    "ck_llr_separable",
+    "ck_llr_separable_maxlog_frames",
+    "ck_llr_separable_frames",
+    "ck_ldpc_schedule",
+    "ck_ldpc_plan_create",
+    "ck_ldpc_plan_destroy",
+    "ck_ldpc_plan_get_info",
+    "ck_ldpc_plan_set_launch",
+    "ck_ldpc_plan_get_launch",
+    "ck_ldpc_workspace_size",
+    "ck_ldpc_decode",
+    "ck_ldpc_workspace_status",
+)
+
+
+class AxisMaxlog(ctypes.Structure):
+    _fields_ = [
+        ("levels", ctypes.c_void_p),
+        ("labels", ctypes.c_void_p),
+        ("lo", ctypes.c_void_p),
+        ("hi", ctypes.c_void_p),
+        ("pos", ctypes.c_void_p),
+        ("L", ctypes.c_int32),
+        ("k", ctypes.c_int32),
+    ]
+
+
+class AxisLevels(ctypes.Structure):
+    _fields_ = [
+        ("levels", ctypes.c_void_p),
+        ("logp", ctypes.c_void_p),
+        ("labels", ctypes.c_void_p),
+        ("pos", ctypes.c_void_p),
+        ("L", ctypes.c_int32),
+        ("k", ctypes.c_int32),
+    ]
+
+
+class PlanInfo(ctypes.Structure):
+    _fields_ = [
+        (name, ctypes.c_int32)
+        for name in (
+            "quasi_cyclic", "lifting", "base_rows", "base_cols", "blocks", "num_checks",
+            "num_variables", "num_edges", "num_layers", "max_row_degree", "device",
+        )
+    ]  # fmt: skip
+
+
+class Launch(ctypes.Structure):
+    _fields_ = [
+        ("threads_per_frame", ctypes.c_int32),
+        ("frames_per_block", ctypes.c_int32),
+        ("placement", ctypes.c_int32),
+    ]
+
+
+_lib: ctypes.CDLL | None = None
+_lock = threading.Lock()
+
+
+def _declare(lib: ctypes.CDLL) -> None:
+    p, i32, i64, f32 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_float
+    size_p = ctypes.POINTER(ctypes.c_size_t)
+    sigs = {
+        "ck_last_error": ([], ctypes.c_char_p),
+        "ck_status_string": ([ctypes.c_int], ctypes.c_char_p),
+        "ck_version": ([], ctypes.c_char_p),
+        "ck_llr_separable_maxlog": (
+            [p, i64, ctypes.POINTER(AxisMaxlog), ctypes.POINTER(AxisMaxlog), f32, p, p], ctypes.c_int),
+        "ck_llr_separable": (
+            [p, i64, ctypes.POINTER(AxisLevels), ctypes.POINTER(AxisLevels), f32, i32, p, p],
+            ctypes.c_int),
+        "ck_llr_separable_maxlog_frames": (
+            [p, i64, i64, p, ctypes.POINTER(AxisMaxlog), ctypes.POINTER(AxisMaxlog), p, p],
+            ctypes.c_int),
+        "ck_llr_separable_frames": (
+            [p, i64, i64, p, ctypes.POINTER(AxisLevels), ctypes.POINTER(AxisLevels), i32, p, p],
+            ctypes.c_int),
+        "ck_ldpc_schedule": ([p, p, i64, i32, i32, p, p, p, ctypes.POINTER(i32)], ctypes.c_int),
+        "ck_ldpc_plan_create": ([p, p, p, i32, i32, i32, ctypes.POINTER(p)], ctypes.c_int),
+        "ck_ldpc_plan_destroy": ([p], ctypes.c_int),
+        "ck_ldpc_plan_get_info": ([p, ctypes.POINTER(PlanInfo)], ctypes.c_int),
+        "ck_ldpc_plan_set_launch": ([p, ctypes.POINTER(Launch)], ctypes.c_int),
+        "ck_ldpc_plan_get_launch": ([p, ctypes.POINTER(Launch)], ctypes.c_int),
+        "ck_ldpc_workspace_size": ([p, i64, i32, size_p], ctypes.c_int),
+        "ck_ldpc_decode": (
+            [p, p, p, i64, i32, i32, f32, f32, i32, i32, p, p, p, i32, p, ctypes.c_size_t, p],
+            ctypes.c_int),
+        "ck_ldpc_workspace_status": ([p, p], ctypes.c_int),
+    }  # fmt: skip
+    for name, (args, res) in sigs.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded library; ``ImportError`` if it has not been built."""
+    global _lib
+    if _lib is None:
+        with _lock:
+            if _lib is None:
+                if not LIB_PATH.exists():
+                    raise ImportError(
+                        f"{LIB_PATH} is missing: build it with `python -m commkit_gb300.build` "
+                        "(commkit_gb300 has no CPU fallback)"
+                    )
+                # torch first: the library then binds to the CUDA runtime torch
+                # already loaded (same soname), so both share the current device.
+                import torch  # noqa: F401
+
+                handle = ctypes.CDLL(str(LIB_PATH))
+                _declare(handle)
+                _lib = handle
+    return _lib
+
+
+def last_error() -> str:
+    msg = lib().ck_last_error()
+    return msg.decode() if msg else ""
+
+
+def check(status: int, what: str) -> None:
+    """Raise the Python exception of a non-zero status."""
+    if status == CK_OK:
+        return
+    msg = f"{what}: {last_error() or lib().ck_status_string(status).decode()}"
+    if status in (CK_ERR_INVALID_ARGUMENT, CK_ERR_UNSUPPORTED):
+        raise ValueError(msg)
+    if status == CK_ERR_OUT_OF_MEMORY:
+        raise MemoryError(msg)
+    raise RuntimeError(msg)

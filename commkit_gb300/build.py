@@ -1,0 +1,94 @@
+"""In-tree build of ``libck_gb300.so``, the CUDA library behind the package.
+
+``python -m commkit_gb300.build`` compiles every ``csrc/*.cu`` / ``*.cpp``
+for sm_103a only (``-gencode arch=compute_103a,code=sm_103a``), in parallel,
+and links them against the shared CUDA runtime into
+``commkit_gb300/_lib/libck_gb300.so``.  Objects go to ``commkit_gb300/_build``.
+Rebuilds only what changed (sources or headers newer than the object).
+"""
+
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+SRC = PKG / "csrc"
+INCLUDE = ROOT / "include"
+BUILD = PKG / "_build"
+LIB_DIR = PKG / "_lib"
+LIB = LIB_DIR / "libck_gb300.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+FLAGS = [
+    "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+    # Every float operation of the kernels rounds once, as the reference's
+    # (explicit _rn intrinsics too; this keeps stray expressions honest).
+    "-fmad=false", "--expt-relaxed-constexpr",
+]  # fmt: skip
+
+
+def nvcc() -> str:
+    found = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(found).exists():
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build commkit_gb300")
+    return found
+
+
+def _sources() -> list[Path]:
+    return sorted([*SRC.glob("*.cu"), *SRC.glob("*.cpp")])
+
+
+def _headers() -> list[Path]:
+    return [*SRC.glob("*.cuh"), *SRC.glob("*.h"), *INCLUDE.glob("*.h")]
+
+
+def _stale(target: Path, deps: list[Path]) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(d.stat().st_mtime > t for d in deps)
+
+
+def _compile(src: Path, verbose: bool) -> Path:
+    obj = BUILD / (src.name + ".o")
+    if not _stale(obj, [src, *_headers()]):
+        return obj
+    cmd = [nvcc(), *ARCH, *FLAGS, "-I", str(INCLUDE), "-I", str(SRC), "-c", str(src), "-o", str(obj)]
+    if verbose:
+        cmd.insert(1, "-Xptxas=-v")
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"nvcc failed on {src.name}:\n{res.stdout}\n{res.stderr}")
+    if verbose and (res.stdout or res.stderr):
+        print(res.stdout + res.stderr, file=sys.stderr)
+    return obj
+
+
+def build(verbose: bool = False) -> Path:
+    """Compile and link the library if anything changed; returns its path."""
+    BUILD.mkdir(exist_ok=True)
+    LIB_DIR.mkdir(exist_ok=True)
+    srcs = _sources()
+    with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as pool:
+        objs = list(pool.map(lambda s: _compile(s, verbose), srcs))
+    if _stale(LIB, objs):
+        tmp = LIB.with_suffix(f".{os.getpid()}.tmp")
+        # The shared CUDA runtime (soname libcudart.so.13): a process that has
+        # loaded torch's copy reuses it, so both see one current device.
+        cmd = [nvcc(), *ARCH, "-shared", "-cudart", "shared", "-Xlinker", "-rpath=/usr/local/cuda/lib64",
+               "-o", str(tmp), *map(str, objs)]  # fmt: skip
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+        os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

@@ -1,0 +1,373 @@
+"""LDPC codes and layered min-sum decoding: :class:`LDPCCode`, :class:`MinSum`, :func:`decode`.
+
+Mirrors the LDPC part of ``commkit.coding``: ``LDPCCode``
+(``commkit/coding/ldpc.py:53-300``; edges sorted by (row, column), the
+first-fit layer schedule), ``MinSum`` (``ldpc.py:317-348``), ``decode``
+(``commkit/coding/base.py:317-379``) and ``DecodeResult``
+(``base.py:46-106``).  Decoding runs on the sm_103a decoder of
+``csrc/ck_ldpc.cu`` behind a per-code, per-device plan; its results
+(a-posteriori LLRs, hard decisions, iteration counts, syndrome flags) are
+bit-identical to the reference's.  The device follows the data; host input
+raises ``TypeError``.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import warnings
+from dataclasses import dataclass
+from functools import cached_property
+from typing import Any
+
+import numpy as np
+
+from . import _device, _lib
+from .mapping import PrecisionWarning
+
+__all__ = ["DecodeResult", "LDPCCode", "MinSum", "SumProduct", "decode"]
+
+_HARD_LLR = 1.0
+
+
+@dataclass(frozen=True)
+class MinSum:
+    """Layered normalized / offset min-sum (``commkit/coding/ldpc.py:317-348``):
+    the check-to-bit message is ``sign * max(scale * min - offset, 0)``."""
+
+    scale: float = 0.875
+    offset: float = 0.0
+    max_iterations: int = 50
+    early_stop: bool = True
+
+    def __post_init__(self) -> None:
+        s = float(self.scale)
+        if not np.isfinite(s) or not 0.0 < s <= 1.0:
+            raise ValueError(f"scale must be in (0, 1], got {self.scale}.")
+        o = float(self.offset)
+        if not np.isfinite(o) or o < 0.0:
+            raise ValueError(f"offset must be finite and >= 0, got {self.offset}.")
+        _check_iterations(self.max_iterations)
+
+
+@dataclass(frozen=True)
+class SumProduct:
+    """Layered sum-product (``commkit/coding/ldpc.py:351-371``)."""
+
+    max_iterations: int = 50
+    early_stop: bool = True
+
+    def __post_init__(self) -> None:
+        _check_iterations(self.max_iterations)
+
+
+def _check_iterations(v: Any) -> None:
+    if isinstance(v, bool) or not isinstance(v, (int, np.integer)) or v < 1:
+        raise ValueError(f"max_iterations must be an integer >= 1, got {v!r}.")
+
+
+@dataclass(frozen=True, eq=False)
+class DecodeResult:
+    """Output of :func:`decode`, arrays on the input's device (``base.py:46-106``)."""
+
+    bits: Any
+    llrs: Any | None
+    valid: Any
+    iterations: Any
+    checked: bool
+
+
+class LDPCCode:
+    """LDPC code given by the edges of its sparse parity-check matrix.
+
+    ``checks``/``variables``: row and column of each nonzero of ``H``
+    (``(E,)`` integers without duplicates); ``num_checks`` m,
+    ``num_variables`` N, ``punctured`` trailing parity bits not sent.
+    Information bits are the first ``k = N - m`` codeword bits: the parity
+    part (last m columns) must be invertible, as for the reference's
+    "accumulate" and "inverse" encoders (``ldpc.py:445-481``).
+    """
+
+    def __init__(self, checks: Any, variables: Any, num_checks: int, num_variables: int,
+                 punctured: int = 0):  # fmt: skip
+        rows = np.asarray(checks)
+        cols = np.asarray(variables)
+        m, n = int(num_checks), int(num_variables)
+        if rows.ndim != 1 or rows.shape != cols.shape or rows.size == 0:
+            raise ValueError("checks and variables must be equal-length 1-D arrays.")
+        if rows.dtype.kind not in "iu" or cols.dtype.kind not in "iu":
+            raise TypeError(f"checks and variables must be integers, got {rows.dtype} and {cols.dtype}.")
+        if m < 1 or n <= m:
+            raise ValueError(f"need 1 <= num_checks < num_variables, got {m} and {n}.")
+        if rows.min() < 0 or rows.max() >= m or cols.min() < 0 or cols.max() >= n:
+            raise ValueError("checks or variables out of range.")
+        order = np.lexsort((cols, rows))
+        rows, cols = rows[order].astype(np.int32), cols[order].astype(np.int32)
+        flat = rows.astype(np.int64) * n + cols
+        if np.any(flat[1:] == flat[:-1]):
+            raise ValueError("H has duplicate entries.")
+        if np.bincount(rows, minlength=m).min() < 2:
+            raise ValueError("every parity check needs at least two bits.")
+        p = int(punctured)
+        if p < 0:
+            raise ValueError(f"punctured must be >= 0, got {punctured}.")
+        if p > m:
+            # The information bits are the first N - m.
+            raise ValueError("punctured bits must be parity bits.")
+        rows.setflags(write=False)
+        cols.setflags(write=False)
+        self.checks, self.variables = rows, cols
+        self.num_checks, self.num_variables, self.punctured = m, n, p
+        self._plans: dict[int, _Plan] = {}
+
+    @classmethod
+    def quasi_cyclic(cls, base: Any, *, lifting: int, punctured: int = 0) -> LDPCCode:
+        """Quasi-cyclic code of a base matrix of circulant shifts (``ldpc.py:183-214``):
+        ``s >= 0`` places the identity shifted right by ``s`` (row ``r`` has its
+        one at column ``(r + s) mod Z``), ``-1`` a zero block."""
+        b = np.asarray(base)
+        z = int(lifting)
+        if z < 1:
+            raise ValueError("lifting must be >= 1.")
+        if b.ndim != 2 or b.size == 0 or b.dtype.kind not in "iu":
+            raise ValueError("base must be a non-empty 2-D integer matrix.")
+        if b.min() < -1:
+            raise ValueError("base entries must be shifts >= 0 or -1.")
+        bi, bj = np.nonzero(b >= 0)
+        r = np.arange(z)
+        rows = (bi[:, None] * z + r).ravel()
+        cols = (bj[:, None] * z + (r + b[bi, bj][:, None]) % z).ravel()
+        return cls(rows, cols, b.shape[0] * z, b.shape[1] * z, punctured)
+
+    @classmethod
+    def from_parity_check(cls, h: Any, *, punctured: int = 0) -> LDPCCode:
+        """The code of a dense 0/1 parity-check matrix ``(m, N)``."""
+        h = np.asarray(h)
+        if h.ndim != 2:
+            raise ValueError(f"parity_check must be 2-D, got {h.ndim}-D.")
+        if np.any((h != 0) & (h != 1)):
+            raise ValueError("parity_check must contain only 0 and 1.")
+        rows, cols = np.nonzero(h)
+        return cls(rows, cols, h.shape[0], h.shape[1], punctured)
+
+    @property
+    def n(self) -> int:
+        """Transmitted bits per codeword."""
+        return self.num_variables - self.punctured
+
+    @cached_property
+    def k(self) -> int:
+        """Information bits per codeword: N - m (the parity part is invertible)."""
+        _require_invertible_parity(self)
+        return self.num_variables - self.num_checks
+
+    @property
+    def rate(self) -> float:
+        return float(self.k / self.n)
+
+    def __repr__(self) -> str:
+        return f"LDPCCode(n={self.n}, k={self.k})"
+
+    @cached_property
+    def _schedule(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """``(row_ptr, cols, layer_ptr)``: CSR of H with rows in first-fit
+        layer order (``ldpc.py:283-296``), computed natively
+        (``ck_ldpc_schedule``)."""
+        m, n, E = self.num_checks, self.num_variables, self.checks.size
+        row_ptr = np.empty(m + 1, np.int32)
+        cols = np.empty(E, np.int32)
+        layer_ptr = np.empty(m + 1, np.int32)
+        num = ctypes.c_int32(0)
+        st = _lib.lib().ck_ldpc_schedule(
+            self.checks.ctypes.data, self.variables.ctypes.data, E, m, n, row_ptr.ctypes.data,
+            cols.ctypes.data, layer_ptr.ctypes.data, ctypes.byref(num),
+        )  # fmt: skip
+        _lib.check(st, "LDPCCode schedule")
+        out = (row_ptr, cols, layer_ptr[: num.value + 1].copy())
+        for a in out:
+            a.setflags(write=False)
+        return out
+
+    def _plan(self, device: int) -> _Plan:
+        plan = self._plans.get(device)
+        if plan is None:
+            plan = self._plans[device] = _Plan(*self._schedule, self.num_checks, self.num_variables)
+        return plan
+
+
+def _require_invertible_parity(code: LDPCCode) -> None:
+    """Raise unless the parity part ``H_p`` (last m columns) is invertible over GF(2).
+
+    Lower triangular with a unit diagonal (dual-diagonal / accumulate parts)
+    is settled from the edges; otherwise by elimination on packed bits.
+    """
+    m, n = code.num_checks, code.num_variables
+    k = n - m
+    rows, cols = code.checks, code.variables
+    par = cols >= k
+    pr, pc = rows[par].astype(np.int64), cols[par].astype(np.int64) - k
+    diag = np.zeros(m, bool)
+    diag[pr[pr == pc]] = True
+    if diag.all() and not np.any(pc > pr):
+        return
+    if m > 16384:
+        raise NotImplementedError(f"parity part of {m} checks is not triangular; rank test too large")
+    words = (m + 63) // 64
+    mat = np.zeros((m, words), np.uint64)
+    np.bitwise_or.at(mat, (pr, pc // 64), np.left_shift(np.uint64(1), (pc % 64).astype(np.uint64)))
+    r = 0
+    for c in range(m):
+        w, bit = c // 64, np.uint64(1) << np.uint64(c % 64)
+        hits = np.flatnonzero(mat[r:, w] & bit)
+        if hits.size == 0:
+            raise NotImplementedError("the parity part of H is singular; such codes are not supported")
+        piv = r + hits[0]
+        if piv != r:
+            mat[[r, piv]] = mat[[piv, r]]
+        below = r + 1 + np.flatnonzero(mat[r + 1 :, w] & bit)
+        mat[below] ^= mat[r]
+        r += 1
+
+
+class _Plan:
+    """A ``ck_ldpc_plan`` on one device, destroyed with the object."""
+
+    def __init__(self, row_ptr, cols, layer_ptr, m: int, n: int):
+        handle = ctypes.c_void_p()
+        st = _lib.lib().ck_ldpc_plan_create(
+            row_ptr.ctypes.data, cols.ctypes.data, layer_ptr.ctypes.data, m, n,
+            layer_ptr.size - 1, ctypes.byref(handle),
+        )  # fmt: skip
+        _lib.check(st, "LDPC plan")
+        self.handle = handle
+        info = _lib.PlanInfo()
+        _lib.check(_lib.lib().ck_ldpc_plan_get_info(handle, ctypes.byref(info)), "plan info")
+        self.info = {name: getattr(info, name) for name, _ in _lib.PlanInfo._fields_}
+
+    def set_launch(self, threads_per_frame: int = 0, frames_per_block: int = 0,
+                   placement: int = 0) -> None:  # fmt: skip
+        cfg = _lib.Launch(threads_per_frame, frames_per_block, placement)
+        _lib.check(_lib.lib().ck_ldpc_plan_set_launch(self.handle, ctypes.byref(cfg)), "set_launch")
+
+    def get_launch(self) -> tuple[int, int, int]:
+        cfg = _lib.Launch()
+        _lib.check(_lib.lib().ck_ldpc_plan_get_launch(self.handle, ctypes.byref(cfg)), "get_launch")
+        return cfg.threads_per_frame, cfg.frames_per_block, cfg.placement
+
+    def workspace_size(self, frames: int) -> int:
+        size = ctypes.c_size_t(0)
+        st = _lib.lib().ck_ldpc_workspace_size(self.handle, int(frames), _lib.CK_LDPC_MIN_SUM,
+                                                ctypes.byref(size))  # fmt: skip
+        _lib.check(st, "workspace size")
+        return int(size.value)
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value and _lib._lib is not None:
+            _lib.lib().ck_ldpc_plan_destroy(h)
+            self.handle = None
+
+
+def _resolve_method(method: Any) -> MinSum:
+    if method is None:
+        return MinSum()
+    if isinstance(method, SumProduct):
+        raise NotImplementedError("decode(): SumProduct is not implemented on sm_103a yet; use MinSum")
+    if not isinstance(method, MinSum):
+        raise TypeError(f"decode(): method {type(method).__name__} does not decode LDPCCode; use MinSum.")
+    return method
+
+
+def _as_llrs(llrs: Any, x: _device.DeviceArray):
+    """float32 LLRs; integer or bool input read as hard decisions (``base.py:232-245``)."""
+    import torch
+
+    if x.kind != "torch":
+        import cupy
+
+        a = llrs
+        if x.dtype.kind == "c":
+            raise TypeError(f"decode(): llrs must be real, got {x.dtype}.")
+        if x.dtype.kind in "biu":
+            return (1.0 - 2.0 * _HARD_LLR * (a != 0)).astype(cupy.float32)
+        if x.dtype == np.float64:
+            warnings.warn("decode(): float64 llrs computed in float32", PrecisionWarning, stacklevel=3)
+        return cupy.ascontiguousarray(a.astype(cupy.float32, copy=False))
+    t = llrs
+    if t.is_complex():
+        raise TypeError(f"decode(): llrs must be real, got {x.dtype}.")
+    if x.dtype.kind in "biu":
+        return _HARD_LLR - 2.0 * _HARD_LLR * (t != 0).to(torch.float32)
+    if t.dtype == torch.float64:
+        warnings.warn("decode(): float64 llrs computed in float32", PrecisionWarning, stacklevel=3)
+    return t.to(torch.float32).contiguous()
+
+
+def decode(llrs: Any, *, code: LDPCCode, method: MinSum | None = None,
+           workspace: Any = None) -> DecodeResult:  # fmt: skip
+    """Decode LLRs of a code's transmitted bits (``commkit/coding/base.py:317-379``).
+
+    ``llrs`` ``(N,)`` or ``(C, N)`` on a CUDA device, ``N`` a multiple of
+    ``code.n``; positive means bit 0.  Returns bits int8 ``(..., B k)``,
+    a-posteriori llrs float32 ``(..., B n)``, valid bool ``(..., B)`` and
+    iterations int32 ``(..., B)``, all on the input's device.
+    ``workspace``: optional device scratch (uint8) reused across calls, at
+    least ``code._plan(dev).workspace_size(B)`` bytes.
+    """
+    if not isinstance(code, LDPCCode):
+        raise TypeError(f"decode(): code must be an LDPCCode, got {type(code).__name__}.")
+    method = _resolve_method(method)
+    x0 = _device.wrap(llrs, "llrs")
+    x = _as_llrs(llrs, x0)
+    was_1d = x0.ndim == 1
+    x2 = x.reshape(1, -1) if was_1d else x
+    if x2.ndim != 2:
+        raise ValueError(f"decode(): llrs must be 1-D or 2-D, got {x2.ndim}-D.")
+    if x2.shape[-1] % code.n:
+        raise ValueError(
+            f"decode(): the last axis of llrs ({x2.shape[-1]}) must be a multiple of the block "
+            f"length {code.n}."
+        )
+    C = x2.shape[0]
+    nb = x2.shape[-1] // code.n
+    rows = C * nb
+    blocks = x2.reshape(rows, code.n)
+    xd = _device.wrap(blocks, "llrs")
+    k = code.k
+    out_llrs = _device.empty(xd, (rows, code.n), np.float32)
+    bits = _device.empty(xd, (rows, k), np.int8)
+    iters = _device.empty(xd, (rows,), np.int32)
+    valid_u8 = _device.empty(xd, (rows,), np.uint8)
+    if rows:
+        with _device.on_device(xd):
+            plan = code._plan(xd.device)
+            stream = _device.stream_of(xd)
+            ws_ptr, ws_bytes = 0, 0
+            if workspace is None:
+                need = plan.workspace_size(rows)
+                workspace = _device.empty(xd, (need,), np.uint8)
+            wsd = _device.wrap(workspace, "workspace")
+            ws_ptr, ws_bytes = wsd.ptr, wsd.size
+            st = _lib.lib().ck_ldpc_decode(
+                plan.handle, xd.ptr, _device.wrap(out_llrs).ptr, rows, code.n,
+                _lib.CK_LDPC_MIN_SUM, np.float32(method.scale), np.float32(method.offset),
+                int(method.max_iterations), 1 if method.early_stop else 0,
+                _device.wrap(iters).ptr, _device.wrap(valid_u8).ptr, _device.wrap(bits).ptr, k,
+                ws_ptr, ws_bytes, stream,
+            )  # fmt: skip
+            _lib.check(st, "decode()")
+    valid = valid_u8.view(_bool_dtype(xd))
+
+    def shaped(a, size):
+        a = a.reshape(C, nb * size)
+        return a.reshape(-1) if was_1d else a
+
+    return DecodeResult(bits=shaped(bits, k), llrs=shaped(out_llrs, code.n),
+                        valid=shaped(valid, 1), iterations=shaped(iters, 1), checked=True)  # fmt: skip
+
+
+def _bool_dtype(xd: _device.DeviceArray):
+    if xd.kind == "torch":
+        import torch
+
+        return torch.bool
+    return np.bool_

@@ -1,0 +1,589 @@
+// Layered min-sum LDPC decoding on sm_103a.
+//
+// The GB300-first replacement of the reference's `ldpc_layered<false>`
+// kernel (commkit/_cuda/src/ldpc.cu:107-159) behind its launcher
+// (commkit/_cuda/coding.py:27-67).  Same recursion, same layer order, the
+// same float32 operations in the same rounding (explicit _rn intrinsics, no
+// FMA), so a-posteriori LLRs, hard decisions, iteration counts and the
+// syndrome flag are bit-identical; what changes is where the data lives and
+// how the work is spread:
+//
+//  * Persistent frame groups.  The grid is sized to fill the GPU once
+//    (SMs x resident blocks); each block holds G frame groups of T threads
+//    and each group pulls frame after frame from a device queue (one atomic
+//    per frame).  Frames that converge early free their group for the next
+//    frame, so uneven iteration counts do not leave SMs idle, and scratch
+//    memory is bounded by the grid, not by the batch.
+//  * The frame's posterior LLRs live in shared memory for the whole decode,
+//    staged in by one bulk (TMA) copy; a layer's updates are shared-memory
+//    gathers and scatters, conflict-free for circulants (lanes handle
+//    consecutive rows of a circulant, so they touch consecutive columns).
+//  * Check-to-variable messages are stored losslessly compressed: a min-sum
+//    message of row i edge e is sign_e * (e == argmin ? min2' : min1'), so
+//    a row keeps (min1', min2', one word of 27 sign bits + a 5-bit argmin),
+//    12 bytes instead of 4 per edge.  The state sits in shared memory beside
+//    the LLRs when both fit, else in device memory, where the working set of
+//    the resident frames stays in L2.
+//  * Quasi-cyclic codes use circulant tables (block column, shift) in shared
+//    memory, so a row's columns are computed, not loaded; other codes read
+//    the CSR schedule.
+//  * The syndrome test runs over chunks of rows with a barrier-OR per chunk
+//    and stops at the first unsatisfied chunk, so a failing iteration pays
+//    for one chunk, not for the whole matrix.
+//
+// Within a row the min1/min2/argmin/sign-parity reduction is a multiset
+// computation (min2 is the second smallest magnitude counting repeats, the
+// argmin the first edge holding min1), so splitting it differently does not
+// change a bit; rows of one layer share no variable, and layers run in the
+// schedule's order, as in the reference.
+#include <math_constants.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "ck_ldpc_internal.h"
+
+namespace {
+
+struct Params {
+    // frames
+    const float* llr_in;
+    float* llr_out;
+    uint32_t B;
+    int32_t n_in;
+    int32_t* iters;
+    uint8_t* valid;
+    int8_t* bits;
+    int32_t k_bits;
+    // code
+    int32_t N, m, L;
+    int32_t Z, mb, nnzb;
+    ck::FastDiv divZ;
+    const int32_t* layer;  // QC: base rows per layer; CSR: rows per layer (L + 1)
+    const int32_t* eptr;   // QC: circulants per base row (mb + 1); CSR: row_ptr (m + 1)
+    const int2* blk;       // QC: (j Z, shift) per circulant
+    const int32_t* cols;   // CSR: column per edge
+    // method
+    float scale, offset;
+    int32_t max_iterations;
+    int32_t early_stop;
+    // launch
+    int32_t T;  // threads per frame group
+    int32_t G;  // frame groups per block
+    uint32_t tables_bytes, group_bytes, app_off, r_off, r_stride;
+    int32_t bulk_load;  // 1: stage the LLRs with one bulk copy
+    // workspace
+    uint32_t* counter;
+    uint32_t* status;
+    float* g_r;    // R-state slots in device memory (3 r_stride words per slot)
+    float* g_app;  // posterior slots in device memory (N per slot)
+    int32_t app_stride;
+};
+
+__device__ __forceinline__ float flip_sign(float v, uint32_t bit) {
+    return __uint_as_float(__float_as_uint(v) ^ (bit << 31));
+}
+
+// One check row, min-sum: reads the row's compressed state (m1, m2, w),
+// updates the posterior `a` of its deg variables (columns from col_of) and
+// writes the new state back.  Two passes as the reference's min_sum_row
+// (commkit/_cuda/src/ldpc.cu:45-72), with Q kept in registers between them
+// (columns are recomputed in the second pass rather than held).
+template <int DMAX, class ColOf>
+__device__ __forceinline__ void min_sum_row(float* __restrict__ a, const int deg,
+                                            const ColOf& col_of, float& m1, float& m2,
+                                            uint32_t& w, const float scale,
+                                            const float offset) {
+    const uint32_t oidx = w >> 27;
+    const uint32_t osign = w;
+    const float om1 = m1, om2 = m2;
+    float q[DMAX];
+    float min1 = CUDART_INF_F, min2 = CUDART_INF_F;
+    uint32_t idx = 31u;  // no edge; matches the reference's -1 when every |Q| is inf
+    uint32_t negs = 0u;
+#pragma unroll
+    for (int e = 0; e < DMAX; ++e) {
+        if (e < deg) {
+            const float r_old =
+                flip_sign(static_cast<uint32_t>(e) == oidx ? om2 : om1, (osign >> e) & 1u);
+            const float qe = __fsub_rn(a[col_of(e)], r_old);
+            q[e] = qe;
+            negs |= (qe < 0.0f ? 1u : 0u) << e;
+            const float mag = fabsf(qe);
+            if (mag < min1) idx = static_cast<uint32_t>(e);
+            min2 = fminf(min2, fmaxf(min1, mag));
+            min1 = fminf(min1, mag);
+        }
+    }
+    const float n1 = fmaxf(__fsub_rn(__fmul_rn(scale, min1), offset), 0.0f);
+    const float n2 = fmaxf(__fsub_rn(__fmul_rn(scale, min2), offset), 0.0f);
+    // Sign of edge e's new message: the parity of all signs times its own.
+    const uint32_t signs = negs ^ ((__popc(negs) & 1u) ? 0xffffffffu : 0u);
+#pragma unroll
+    for (int e = 0; e < DMAX; ++e) {
+        if (e < deg) {
+            const float rn = flip_sign(static_cast<uint32_t>(e) == idx ? n2 : n1, (signs >> e) & 1u);
+            a[col_of(e)] = __fadd_rn(q[e], rn);
+        }
+    }
+    m1 = n1;
+    m2 = n2;
+    w = (signs & 0x07ffffffu) | (idx << 27);
+}
+
+// Columns of row r of a circulant base row: j Z + (r + shift) mod Z.
+struct QcCols {
+    const int2* blk;
+    int32_t r, Z;
+    __device__ __forceinline__ int operator()(int e) const {
+        const int2 b = blk[e];
+        int o = r + b.y;
+        o = o >= Z ? o - Z : o;
+        return b.x + o;
+    }
+};
+
+struct CsrCols {
+    const int32_t* cols;
+    __device__ __forceinline__ int operator()(int e) const { return __ldg(cols + e); }
+};
+
+// Row `row` (schedule order) of the code: its degree and column functor.
+template <bool QC>
+struct RowOf;
+template <>
+struct RowOf<true> {
+    __device__ __forceinline__ static QcCols get(const Params& p, const int32_t* s_eptr,
+                                                 const int2* s_blk, uint32_t row, int& deg) {
+        const uint32_t b = p.divZ.div(row);
+        const int32_t r = static_cast<int32_t>(row - b * static_cast<uint32_t>(p.Z));
+        const int32_t e0 = s_eptr[b];
+        deg = s_eptr[b + 1] - e0;
+        return QcCols{s_blk + e0, r, p.Z};
+    }
+};
+template <>
+struct RowOf<false> {
+    __device__ __forceinline__ static CsrCols get(const Params& p, const int32_t*, const int2*,
+                                                  uint32_t row, int& deg) {
+        const int32_t e0 = __ldg(p.eptr + row);
+        deg = __ldg(p.eptr + row + 1) - e0;
+        return CsrCols{p.cols + e0};
+    }
+};
+
+// True in every thread of the group when every check is satisfied by the
+// hard decisions of `a` (commkit/_cuda/src/ldpc.cu:94-105).  Rows go in
+// chunks of T; the first chunk with an unsatisfied row ends the test.
+template <bool QC>
+__device__ __forceinline__ bool syndrome_ok(const Params& p, const float* a, const int32_t* s_eptr,
+                                            const int2* s_blk, int tid, int bar) {
+    for (int32_t base = 0; base < p.m; base += p.T) {
+        const int32_t row = base + tid;
+        uint32_t parity = 0;
+        if (row < p.m) {
+            int deg;
+            const auto col_of = RowOf<QC>::get(p, s_eptr, s_blk, static_cast<uint32_t>(row), deg);
+            for (int e = 0; e < deg; ++e) parity ^= a[col_of(e)] < 0.0f ? 1u : 0u;
+        }
+        if (ck::group_any(static_cast<int>(parity), bar, p.T)) return false;
+    }
+    return true;
+}
+
+template <bool QC, int DMAX, bool APP_SMEM, bool R_SMEM>
+__global__ void __launch_bounds__(DMAX <= 16 ? 1024 : 512)
+    ldpc_decode_kernel(const __grid_constant__ Params p) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    using ck::group_any;
+    using ck::group_sync;
+
+    // Tables: layer pointers, then (QC) circulants per base row and the
+    // circulants themselves.
+    int32_t* s_layer = reinterpret_cast<int32_t*>(smem);
+    int32_t* s_eptr = s_layer + (p.L + 1);
+    int2* s_blk = reinterpret_cast<int2*>(smem + ((static_cast<uint32_t>(p.L + 1 + p.mb + 1) * 4 + 7) & ~7u));
+    for (int i = threadIdx.x; i <= p.L; i += blockDim.x) s_layer[i] = p.layer[i];
+    if (QC) {
+        for (int i = threadIdx.x; i <= p.mb; i += blockDim.x) s_eptr[i] = p.eptr[i];
+        for (int i = threadIdx.x; i < p.nnzb; i += blockDim.x) s_blk[i] = p.blk[i];
+    }
+
+    const int g = threadIdx.x / p.T;
+    const int tid = threadIdx.x - g * p.T;
+    const int bar = g + 1;
+    const uint32_t slot = blockIdx.x * static_cast<uint32_t>(p.G) + static_cast<uint32_t>(g);
+    unsigned char* gbase = smem + p.tables_bytes + static_cast<uint32_t>(g) * p.group_bytes;
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(gbase);
+    volatile uint32_t* s_frame = reinterpret_cast<volatile uint32_t*>(gbase + 8);
+    float* a = APP_SMEM ? reinterpret_cast<float*>(gbase + p.app_off)
+                        : p.g_app + static_cast<size_t>(slot) * p.app_stride;
+    float* r1;
+    float* r2;
+    uint32_t* rw;
+    if (R_SMEM) {
+        r1 = reinterpret_cast<float*>(gbase + p.r_off);
+    } else {
+        r1 = p.g_r + static_cast<size_t>(slot) * 3 * p.r_stride;
+    }
+    r2 = r1 + p.r_stride;
+    rw = reinterpret_cast<uint32_t*>(r2 + p.r_stride);
+
+    if (tid == 0) {
+        ck::mbar_init(mbar, 1);
+        ck::fence_mbar_init();
+    }
+    __syncthreads();
+
+    uint32_t phase = 0;
+    for (;;) {
+        if (tid == 0) *s_frame = atomicAdd(p.counter, 1u);
+        group_sync(bar, p.T);
+        const uint32_t f = *s_frame;
+        if (f >= p.B) break;
+        const float* src = p.llr_in + static_cast<size_t>(f) * p.n_in;
+
+        // Stage the frame's channel LLRs; punctured variables start at 0.
+        bool loaded = true;
+        if (APP_SMEM && p.bulk_load) {
+            if (tid == 0) {
+                ck::fence_proxy_async_smem();
+                ck::mbar_arrive_expect_tx(mbar, static_cast<uint32_t>(p.n_in) * 4u);
+                ck::bulk_g2s(a, src, static_cast<uint32_t>(p.n_in) * 4u, mbar);
+            }
+            for (int i = p.n_in + tid; i < p.N; i += p.T) a[i] = 0.0f;
+            loaded = ck::mbar_wait(mbar, phase);
+            phase ^= 1u;
+        } else {
+            for (int i = tid; i < p.n_in; i += p.T) a[i] = __ldcs(src + i);
+            for (int i = p.n_in + tid; i < p.N; i += p.T) a[i] = 0.0f;
+        }
+        if (group_any(loaded ? 0 : 1, bar, p.T)) {
+            // A bulk copy did not complete in time: report and stop this
+            // group after a last bounded wait for the copy in flight.
+            if (tid == 0) {
+                atomicOr(p.status, ck::kStatusTimeout);
+                p.iters[f] = -1;
+                p.valid[f] = 0;
+            }
+            (void)ck::mbar_wait(mbar, phase ^ 1u);
+            return;
+        }
+        for (int i = tid; i < p.m; i += p.T) {
+            r1[i] = 0.0f;
+            r2[i] = 0.0f;
+            rw[i] = 0u;
+        }
+        group_sync(bar, p.T);
+
+        int32_t it = 0;
+        bool ok = p.early_stop && syndrome_ok<QC>(p, a, s_eptr, s_blk, tid, bar);
+        while (!ok && it < p.max_iterations) {
+            for (int32_t l = 0; l < p.L; ++l) {
+                const uint32_t row0 = QC ? static_cast<uint32_t>(s_layer[l]) * p.Z : s_layer[l];
+                const uint32_t row1 = QC ? static_cast<uint32_t>(s_layer[l + 1]) * p.Z : s_layer[l + 1];
+                for (uint32_t row = row0 + tid; row < row1; row += p.T) {
+                    int deg;
+                    const auto col_of = RowOf<QC>::get(p, s_eptr, s_blk, row, deg);
+                    float m1, m2;
+                    uint32_t w;
+                    if (R_SMEM) {
+                        m1 = r1[row];
+                        m2 = r2[row];
+                        w = rw[row];
+                    } else {
+                        m1 = __ldcg(r1 + row);
+                        m2 = __ldcg(r2 + row);
+                        w = __ldcg(rw + row);
+                    }
+                    min_sum_row<DMAX>(a, deg, col_of, m1, m2, w, p.scale, p.offset);
+                    if (R_SMEM) {
+                        r1[row] = m1;
+                        r2[row] = m2;
+                        rw[row] = w;
+                    } else {
+                        __stcg(r1 + row, m1);
+                        __stcg(r2 + row, m2);
+                        __stcg(rw + row, w);
+                    }
+                }
+                group_sync(bar, p.T);
+            }
+            ++it;
+            if (p.early_stop) ok = syndrome_ok<QC>(p, a, s_eptr, s_blk, tid, bar);
+        }
+        if (!p.early_stop) ok = syndrome_ok<QC>(p, a, s_eptr, s_blk, tid, bar);
+
+        float* dst = p.llr_out + static_cast<size_t>(f) * p.n_in;
+        for (int i = tid; i < p.n_in; i += p.T) __stcs(dst + i, a[i]);
+        if (p.bits) {
+            int8_t* bdst = p.bits + static_cast<size_t>(f) * p.k_bits;
+            for (int i = tid; i < p.k_bits; i += p.T) bdst[i] = a[i] < 0.0f ? 1 : 0;
+        }
+        if (tid == 0) {
+            p.iters[f] = it;
+            p.valid[f] = ok ? 1 : 0;
+        }
+        // Everyone has read `a` before the next frame overwrites it.
+        group_sync(bar, p.T);
+    }
+}
+
+using KernelFn = void (*)(Params);
+
+template <bool QC, int DMAX>
+KernelFn pick_placement(bool app_smem, bool r_smem) {
+    if (app_smem && r_smem) return ldpc_decode_kernel<QC, DMAX, true, true>;
+    if (app_smem) return ldpc_decode_kernel<QC, DMAX, true, false>;
+    return ldpc_decode_kernel<QC, DMAX, false, false>;
+}
+
+template <bool QC>
+KernelFn pick_degree(int dmax, bool app_smem, bool r_smem) {
+    if (dmax <= 8) return pick_placement<QC, 8>(app_smem, r_smem);
+    if (dmax <= 16) return pick_placement<QC, 16>(app_smem, r_smem);
+    return pick_placement<QC, 27>(app_smem, r_smem);
+}
+
+uint32_t align_up(uint32_t v, uint32_t a) { return (v + a - 1) / a * a; }
+
+struct Resolved {
+    KernelFn kernel;
+    int32_t T, G;
+    bool app_smem, r_smem;
+    uint32_t tables_bytes, group_bytes, app_off, r_off, r_stride, smem;
+    int32_t app_stride;
+    int grid;
+    size_t ws_bytes, r_ws_off, app_ws_off;
+};
+
+constexpr size_t kHeaderBytes = 256;
+
+int device_limits(int dev, int* sms, int* smem_optin) {
+    CK_CUDA(cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev));
+    CK_CUDA(cudaDeviceGetAttribute(smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    return CK_OK;
+}
+
+// Launch shape, shared-memory layout, grid and workspace of a decode of B
+// frames; a pure function of the plan, its launch setting and B.
+int resolve(const ck_ldpc_plan* plan, int64_t B, Resolved* r) {
+    int sms = 0, optin = 0;
+    CK_TRY(device_limits(plan->device, &sms, &optin));
+    const uint32_t tables =
+        plan->qc ? align_up(align_up(static_cast<uint32_t>(plan->L + 1 + plan->mb + 1) * 4, 8) +
+                                static_cast<uint32_t>(plan->nnzb) * 8,
+                            128)
+                 : align_up(static_cast<uint32_t>(plan->L + 1) * 4, 128);
+    const uint32_t ctrl = 128;
+    const uint32_t app_bytes = align_up(static_cast<uint32_t>(plan->N) * 4, 128);
+    const uint32_t r_stride = align_up(static_cast<uint32_t>(plan->m), 32);
+    const uint32_t r_bytes = 3 * r_stride * 4;
+    const uint32_t budget = static_cast<uint32_t>(optin) > tables ? optin - tables : 0;
+
+    bool app_smem = ctrl + app_bytes <= budget;
+    bool r_smem;
+    const int32_t place = plan->launch.placement;
+    if (!app_smem || place == CK_LDPC_PLACE_GLOBAL) {
+        r_smem = false;
+    } else if (place == CK_LDPC_PLACE_SHARED) {
+        r_smem = ctrl + app_bytes + r_bytes <= budget;
+    } else {
+        // Auto: beside the LLRs when two frames still fit per block budget.
+        r_smem = 2 * (ctrl + app_bytes + r_bytes) <= budget;
+    }
+    uint32_t group = ctrl + (app_smem ? app_bytes : 0) + (r_smem ? r_bytes : 0);
+
+    int32_t T = plan->launch.threads_per_frame;
+    if (T == 0) {
+        const int32_t avg = std::max(1, plan->m / plan->L);
+        T = 32;
+        while (T < 512 && T < avg / 2) T *= 2;
+    }
+    const int32_t max_threads = plan->max_deg <= 16 ? 1024 : 512;
+    if (T > max_threads)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT,
+                        "threads_per_frame %d above %d for row degree %d", T, max_threads,
+                        plan->max_deg);
+    int32_t G = plan->launch.frames_per_block;
+    const int32_t gmax_threads = max_threads / T;
+    const int32_t gmax_smem = static_cast<int32_t>(budget / group);
+    const int32_t gmax_bar = T > 32 ? ck::kMaxNamedGroups : 32;
+    const int32_t gmax = std::min(gmax_threads, std::min(gmax_smem, gmax_bar));
+    if (gmax < 1)
+        return ck::fail(CK_ERR_UNSUPPORTED, "a frame needs %u bytes of shared memory, %u available",
+                        group, budget);
+    if (G == 0) G = std::max(1, std::min(gmax, 512 / T));
+    if (G > gmax)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT,
+                        "frames_per_block %d above the %d that fit (threads, shared memory, "
+                        "barriers)",
+                        G, gmax);
+
+    r->kernel = plan->qc ? pick_degree<true>(plan->max_deg, app_smem, r_smem)
+                         : pick_degree<false>(plan->max_deg, app_smem, r_smem);
+    r->T = T;
+    r->G = G;
+    r->app_smem = app_smem;
+    r->r_smem = r_smem;
+    r->tables_bytes = tables;
+    r->group_bytes = group;
+    r->app_off = ctrl;
+    r->r_off = ctrl + (app_smem ? app_bytes : 0);
+    r->r_stride = r_stride;
+    r->smem = tables + static_cast<uint32_t>(G) * group;
+    r->app_stride = static_cast<int32_t>(app_bytes / 4);
+
+    CK_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void*>(r->kernel),
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(r->smem)));
+    int per_sm = 0;
+    CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, reinterpret_cast<const void*>(r->kernel), T * G, r->smem));
+    if (per_sm < 1)
+        return ck::fail(CK_ERR_UNSUPPORTED,
+                        "decoder block of %d threads and %u bytes of shared memory does not fit "
+                        "an SM",
+                        T * G, r->smem);
+    const int64_t need = (B + G - 1) / G;
+    r->grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(need, int64_t(sms) * per_sm)));
+    const size_t slots = static_cast<size_t>(r->grid) * G;
+    r->r_ws_off = kHeaderBytes;
+    const size_t r_ws = r_smem ? 0 : slots * r_bytes;
+    r->app_ws_off = kHeaderBytes + ((r_ws + 255) / 256) * 256;
+    const size_t app_ws = app_smem ? 0 : slots * app_bytes;
+    r->ws_bytes = r->app_ws_off + app_ws;
+    return CK_OK;
+}
+
+int check_device(const ck_ldpc_plan* plan) {
+    int dev = -1;
+    CK_CUDA(cudaGetDevice(&dev));
+    if (dev != plan->device)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "plan is for device %d, current device is %d",
+                        plan->device, dev);
+    return CK_OK;
+}
+
+}  // namespace
+
+extern "C" int ck_ldpc_workspace_size(const ck_ldpc_plan* plan, int64_t B, int32_t rule,
+                                      size_t* bytes) {
+    ck::clear_error();
+    if (!plan || !bytes) return ck::fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (rule != CK_LDPC_MIN_SUM)
+        return ck::fail(CK_ERR_UNSUPPORTED, "only the min-sum rule is implemented");
+    if (B < 0) return ck::fail(CK_ERR_INVALID_ARGUMENT, "B must be >= 0");
+    CK_TRY(check_device(plan));
+    Resolved r;
+    CK_TRY(resolve(plan, std::max<int64_t>(B, 1), &r));
+    *bytes = r.ws_bytes;
+    return CK_OK;
+}
+
+extern "C" int ck_ldpc_decode(const ck_ldpc_plan* plan, const float* llr_in, float* llr_out,
+                              int64_t B, int32_t n_in, int32_t rule, float scale, float offset,
+                              int32_t max_iterations, int32_t early_stop, int32_t* iters,
+                              uint8_t* valid, int8_t* bits, int32_t k_bits, void* workspace,
+                              size_t workspace_bytes, void* stream) {
+    ck::clear_error();
+    if (!plan) return ck::fail(CK_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (rule != CK_LDPC_MIN_SUM)
+        return ck::fail(CK_ERR_UNSUPPORTED, "only the min-sum rule is implemented");
+    if (B < 0 || B >= (int64_t(1) << 31))
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "B must be in [0, 2**31), got %lld",
+                        static_cast<long long>(B));
+    if (n_in < 1 || n_in > plan->N)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "n_in must be in [1, N=%d], got %d", plan->N,
+                        n_in);
+    if (max_iterations < 0)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "max_iterations must be >= 0");
+    if (bits && (k_bits < 0 || k_bits > n_in))
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "k_bits must be in [0, n_in]");
+    if (B == 0) return CK_OK;
+    if (!llr_in || !llr_out || !iters || !valid)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "llr_in, llr_out, iters and valid are required");
+    if (reinterpret_cast<uintptr_t>(llr_in) % 4 || reinterpret_cast<uintptr_t>(llr_out) % 4)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "LLR buffers must be 4-byte aligned");
+    CK_TRY(check_device(plan));
+    Resolved r;
+    CK_TRY(resolve(plan, B, &r));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    void* ws = workspace;
+    bool owned = false;
+    if (ws == nullptr) {
+        CK_CUDA(cudaMallocAsync(&ws, r.ws_bytes, s));
+        owned = true;
+    } else {
+        if (workspace_bytes < r.ws_bytes)
+            return ck::fail(CK_ERR_INVALID_ARGUMENT, "workspace of %zu bytes, %zu needed",
+                            workspace_bytes, r.ws_bytes);
+        if (reinterpret_cast<uintptr_t>(ws) % 256)
+            return ck::fail(CK_ERR_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
+    }
+    unsigned char* wsb = static_cast<unsigned char*>(ws);
+    int status = ck::cuda_check(cudaMemsetAsync(wsb, 0, kHeaderBytes, s), "cudaMemsetAsync");
+
+    Params p;
+    p.llr_in = llr_in;
+    p.llr_out = llr_out;
+    p.B = static_cast<uint32_t>(B);
+    p.n_in = n_in;
+    p.iters = iters;
+    p.valid = valid;
+    p.bits = k_bits > 0 ? bits : nullptr;
+    p.k_bits = k_bits;
+    p.N = plan->N;
+    p.m = plan->m;
+    p.L = plan->L;
+    p.Z = plan->qc ? plan->Z : 1;
+    p.mb = plan->qc ? plan->mb : 0;
+    p.nnzb = plan->qc ? plan->nnzb : 0;
+    p.divZ = plan->divZ;
+    p.layer = plan->d_layer;
+    p.eptr = plan->d_eptr;
+    p.blk = reinterpret_cast<const int2*>(plan->d_blk);
+    p.cols = plan->d_cols;
+    p.scale = scale;
+    p.offset = offset;
+    p.max_iterations = max_iterations;
+    p.early_stop = early_stop ? 1 : 0;
+    p.T = r.T;
+    p.G = r.G;
+    p.tables_bytes = r.tables_bytes;
+    p.group_bytes = r.group_bytes;
+    p.app_off = r.app_off;
+    p.r_off = r.r_off;
+    p.r_stride = r.r_stride;
+    p.bulk_load = (r.app_smem && (static_cast<uint32_t>(n_in) * 4u) % 16u == 0 &&
+                   reinterpret_cast<uintptr_t>(llr_in) % 16 == 0)
+                      ? 1
+                      : 0;
+    p.counter = reinterpret_cast<uint32_t*>(wsb);
+    p.status = reinterpret_cast<uint32_t*>(wsb + 4);
+    p.g_r = reinterpret_cast<float*>(wsb + r.r_ws_off);
+    p.g_app = reinterpret_cast<float*>(wsb + r.app_ws_off);
+    p.app_stride = r.app_stride;
+    if (status == CK_OK) {
+        r.kernel<<<r.grid, r.T * r.G, r.smem, s>>>(p);
+        status = ck::cuda_check(cudaGetLastError(), "decoder launch");
+    }
+    if (owned) {
+        const int st = ck::cuda_check(cudaFreeAsync(ws, s), "cudaFreeAsync");
+        if (status == CK_OK) status = st;
+    }
+    return status;
+}
+
+extern "C" int ck_ldpc_workspace_status(const void* workspace, void* stream) {
+    ck::clear_error();
+    if (!workspace) return ck::fail(CK_ERR_INVALID_ARGUMENT, "workspace is NULL");
+    uint32_t status = 0;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    CK_CUDA(cudaMemcpyAsync(&status, static_cast<const unsigned char*>(workspace) + 4,
+                            sizeof(status), cudaMemcpyDeviceToHost, s));
+    CK_CUDA(cudaStreamSynchronize(s));
+    if (status & ck::kStatusTimeout)
+        return ck::fail(CK_ERR_DEVICE_TIMEOUT, "a bulk copy of the decoder did not complete");
+    return CK_OK;
+}

@@ -1,0 +1,41 @@
+// The LDPC decoding plan shared by the host-side plan code and the decoder.
+#pragma once
+
+#include <stdint.h>
+
+#include <vector>
+
+#include "ck_common.cuh"
+
+namespace ck {
+
+// Largest check-row degree: the compressed check-to-variable state of a row
+// keeps its sign bits and the argmin in one 32-bit word (27 + 5 bits).
+constexpr int32_t kMaxRowDegree = 27;
+// Circulant tables held in shared memory.
+constexpr int32_t kMaxBaseRows = 1024;
+constexpr int32_t kMaxBlocks = 2048;
+// Frame groups of more than one warp synchronize on named barriers 1..15.
+constexpr int32_t kMaxNamedGroups = 15;
+
+}  // namespace ck
+
+struct ck_ldpc_plan {
+    int device = 0;
+    int32_t m = 0, N = 0, E = 0, L = 0;
+    int32_t max_deg = 0;
+    int32_t max_layer_rows = 0;
+    // Quasi-cyclic form: layer l holds base rows [h_layer[l], h_layer[l+1]),
+    // base row b has the circulants h_blk[2 i] (j Z), h_blk[2 i + 1] (shift)
+    // for i in [h_eptr[b], h_eptr[b+1]); schedule row b Z + r is its row r.
+    // CSR form: h_layer is layer_ptr, d_eptr row_ptr, d_cols cols.
+    bool qc = false;
+    int32_t Z = 0, mb = 0, nb = 0, nnzb = 0;
+    std::vector<int32_t> h_layer, h_eptr, h_blk;
+    int32_t* d_layer = nullptr;
+    int32_t* d_eptr = nullptr;
+    int32_t* d_blk = nullptr;
+    int32_t* d_cols = nullptr;
+    ck::FastDiv divZ{1, 1, 0};
+    ck_ldpc_launch launch{0, 0, 0};
+};

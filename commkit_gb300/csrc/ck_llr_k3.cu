@@ -1,0 +1,16 @@
+// LLR kernels for 3 bits per axis (64-QAM).
+#include "ck_llr_kernels.cuh"
+
+namespace ck {
+namespace llr {
+template int launch_ka<3, 0, ck_axis_maxlog>(const void*, uint32_t, const ck_axis_maxlog&,
+                                                const ck_axis_maxlog&, const NoiseScale&, float*,
+                                                cudaStream_t);
+template int launch_ka<3, 1, ck_axis_levels>(const void*, uint32_t, const ck_axis_levels&,
+                                                const ck_axis_levels&, const NoiseScale&, float*,
+                                                cudaStream_t);
+template int launch_ka<3, 2, ck_axis_levels>(const void*, uint32_t, const ck_axis_levels&,
+                                                const ck_axis_levels&, const NoiseScale&, float*,
+                                                cudaStream_t);
+}  // namespace llr
+}  // namespace ck

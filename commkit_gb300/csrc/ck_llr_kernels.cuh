@@ -1,0 +1,384 @@
+// Soft LLR demapping of separable (Gray square) QAM on sm_103a: the kernels.
+// Each ck_llr_k<KA>.cu instantiates them for one number of bits per axis,
+// so the build compiles the orders in parallel.
+//
+// The GB300-first replacement of the reference's `llr_separable_maxlog`
+// and `llr_separable` kernels (commkit/_cuda/src/llr.cu:225-337) behind the
+// launchers of commkit/_cuda/llr.py:87-206.  The work is a pure HBM
+// stream: 8 bytes of complex64 in and 4k bytes of float32 out per symbol,
+// a few dozen flops in between.  So the kernels are shaped for bandwidth:
+//
+//  * each thread loads two symbols with one 16-byte streaming load and
+//    writes their 2k LLRs with 16-byte streaming stores: a warp moves
+//    512 B in and 32*2k*4 B out per step, contiguous, no shared-memory
+//    staging (the reference stages every tile through shared memory to
+//    coalesce k-strided stores);
+//  * two symbol pairs are in flight per thread per step, and the grid is a
+//    multiple of the SM count, so the memory system sees enough requests;
+//  * the per-axis tables (levels, labels, opposite levels, bit positions)
+//    live in shared memory, indexed by the data-dependent snapped level;
+//  * the bits-per-axis count is a template parameter, so every per-bit
+//    loop unrolls into registers.
+//
+// Arithmetic: float32 with explicit _rn intrinsics (and -fmad=false), so
+// every operation rounds once, in the reference's order: the closed-form
+// max-log and the level-metric max-log are bit-identical to the IEEE
+// evaluation of the reference's formulas (commkit/mapping/_numba_llr.py:
+// 179-235 and :84-92).  The exact method follows the CPU reference's
+// log-sum-exp (_numba_llr.py:35-81: one exponential per level relative to
+// the symbol's peak metric, the half-sums in ascending level order, a
+// half below 1e-26 redone relative to its own maximum) with expf/logf;
+// it agrees with the reference within float32 rounding of exp/log.
+#pragma once
+
+#include <stdint.h>
+
+#include "ck_common.cuh"
+
+namespace ck {
+namespace llr {
+
+int num_sms();
+
+
+constexpr int kThreads = 256;
+constexpr float kExactFloor = 1e-26f;
+
+__device__ __forceinline__ float4 ld_stream(const float4* p) { return __ldcs(p); }
+__device__ __forceinline__ float2 ld_stream(const float2* p) { return __ldcs(p); }
+__device__ __forceinline__ void st_stream(float4* p, float4 v) { __stcs(p, v); }
+
+// -(d*d)*inv_s2 with two roundings and no contraction.
+__device__ __forceinline__ float neg_sq_scaled(float d, float inv_s2) {
+    return __fmul_rn(-__fmul_rn(d, d), inv_s2);
+}
+
+// ---------------------------------------------------------------------------
+// Closed-form max-log (commkit/_cuda/src/llr.cu:262-302,
+// commkit/mapping/_numba_llr.py:179-210)
+// ---------------------------------------------------------------------------
+
+template <int KA>
+struct MaxlogAxis {
+    static constexpr int L = 1 << KA;
+    float lev[L];
+    int32_t lab[L];
+    int32_t lo[KA * L];
+    int32_t hi[KA * L];
+    int32_t pos[KA];
+};
+
+// LLRs of one axis's KA bits (axis bit order) of the coordinate `x`.
+template <int KA>
+__device__ __forceinline__ void axis_maxlog(float x, const MaxlogAxis<KA>& t, float inv_s2,
+                                            float* o) {
+    constexpr int L = 1 << KA;
+    const float q = __fdiv_rn(__fsub_rn(x, t.lev[0]), __fsub_rn(t.lev[1], t.lev[0]));
+    int s = __float2int_rn(q);  // round half to even, as np.rint
+    s = min(max(s, 0), L - 1);
+    float d = __fsub_rn(x, t.lev[s]);
+    // Near a midpoint the rounded quotient can land one level off: keep the
+    // nearer of s and its neighbour towards x.
+    const int s2 = d > 0.0f ? s + 1 : s - 1;
+    if (s2 >= 0 && s2 < L) {
+        const float d2 = __fsub_rn(x, t.lev[s2]);
+        if (__fmul_rn(d2, d2) < __fmul_rn(d, d)) {
+            s = s2;
+            d = d2;
+        }
+    }
+    const float m_own = neg_sq_scaled(d, inv_s2);
+    const int32_t label = t.lab[s];
+#pragma unroll
+    for (int b = 0; b < KA; ++b) {
+        float m_other = -3.0e38f;
+        int j = t.lo[b * L + s];
+        if (j >= 0) m_other = fmaxf(m_other, neg_sq_scaled(__fsub_rn(x, t.lev[j]), inv_s2));
+        j = t.hi[b * L + s];
+        if (j >= 0) m_other = fmaxf(m_other, neg_sq_scaled(__fsub_rn(x, t.lev[j]), inv_s2));
+        const bool one = (label >> (KA - 1 - b)) & 1;
+        o[b] = one ? __fsub_rn(m_other, m_own) : __fsub_rn(m_own, m_other);
+    }
+}
+
+template <int KA>
+__device__ __forceinline__ void load_maxlog_axis(MaxlogAxis<KA>& t, const ck_axis_maxlog& a) {
+    constexpr int L = 1 << KA;
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+        t.lev[i] = a.levels[i];
+        t.lab[i] = a.labels[i];
+    }
+    for (int i = threadIdx.x; i < KA * L; i += blockDim.x) {
+        t.lo[i] = a.lo[i];
+        t.hi[i] = a.hi[i];
+    }
+    for (int i = threadIdx.x; i < KA; i += blockDim.x) t.pos[i] = a.pos[i];
+}
+
+// ---------------------------------------------------------------------------
+// Level metrics, max-log or exact (commkit/mapping/_numba_llr.py:35-92)
+// ---------------------------------------------------------------------------
+
+template <int KA>
+struct LevelAxis {
+    static constexpr int L = 1 << KA;
+    float lev[L];
+    float logp[L];
+    int32_t lab[L];
+    int32_t pos[KA];
+};
+
+template <int KA>
+__device__ __forceinline__ float level_metric(const LevelAxis<KA>& t, int j, float x,
+                                              float inv_s2) {
+    return __fadd_rn(neg_sq_scaled(__fsub_rn(x, t.lev[j]), inv_s2), t.logp[j]);
+}
+
+// Level loops unroll fully up to 16 levels (256-QAM), by 4 beyond.
+template <int KA>
+struct Unroll {
+    static constexpr int value = KA <= 4 ? (1 << KA) : 4;
+};
+
+template <int KA, bool EXACT>
+__device__ __forceinline__ void axis_levels(float x, const LevelAxis<KA>& t, float inv_s2,
+                                            float* o) {
+    constexpr int L = 1 << KA;
+    // Pass 1: the peak metric and each bit's maximum over its two halves,
+    // each started at the half's first level (the reference's max order).
+    float peak = 0.0f;
+    float p0[KA], p1[KA];
+    bool seen0[KA], seen1[KA];
+#pragma unroll
+    for (int b = 0; b < KA; ++b) {
+        seen0[b] = seen1[b] = false;
+        p0[b] = p1[b] = 0.0f;
+    }
+#pragma unroll Unroll<KA>::value
+    for (int j = 0; j < L; ++j) {
+        const float mj = level_metric(t, j, x, inv_s2);
+        if (j == 0 || mj > peak) peak = mj;
+        const int32_t lab = t.lab[j];
+#pragma unroll
+        for (int b = 0; b < KA; ++b) {
+            if ((lab >> (KA - 1 - b)) & 1) {
+                if (!seen1[b] || mj > p1[b]) p1[b] = mj;
+                seen1[b] = true;
+            } else {
+                if (!seen0[b] || mj > p0[b]) p0[b] = mj;
+                seen0[b] = true;
+            }
+        }
+    }
+    if (!EXACT) {
+#pragma unroll
+        for (int b = 0; b < KA; ++b) o[b] = __fsub_rn(p0[b], p1[b]);
+        return;
+    }
+    // Pass 2: the half-sums of e_j = exp(m_j - peak), ascending j.
+    float s0[KA], s1[KA];
+#pragma unroll
+    for (int b = 0; b < KA; ++b) s0[b] = s1[b] = 0.0f;
+#pragma unroll Unroll<KA>::value
+    for (int j = 0; j < L; ++j) {
+        const float e = expf(__fsub_rn(level_metric(t, j, x, inv_s2), peak));
+        const int32_t lab = t.lab[j];
+#pragma unroll
+        for (int b = 0; b < KA; ++b) {
+            if ((lab >> (KA - 1 - b)) & 1)
+                s1[b] = __fadd_rn(s1[b], e);
+            else
+                s0[b] = __fadd_rn(s0[b], e);
+        }
+    }
+#pragma unroll
+    for (int b = 0; b < KA; ++b) {
+        float l[2];
+#pragma unroll
+        for (int v = 0; v < 2; ++v) {
+            const float s = v ? s1[b] : s0[b];
+            if (s >= kExactFloor) {
+                l[v] = logf(s);
+                continue;
+            }
+            // Underflowed half: redo relative to its own maximum (rare).
+            const float p = v ? p1[b] : p0[b];
+            float r = 0.0f;
+            for (int j = 0; j < L; ++j) {
+                if (((t.lab[j] >> (KA - 1 - b)) & 1) != v) continue;
+                r = __fadd_rn(r, expf(__fsub_rn(level_metric(t, j, x, inv_s2), p)));
+            }
+            l[v] = __fadd_rn(logf(r), __fsub_rn(p, peak));
+        }
+        o[b] = __fsub_rn(l[0], l[1]);
+    }
+}
+
+template <int KA>
+__device__ __forceinline__ void load_level_axis(LevelAxis<KA>& t, const ck_axis_levels& a) {
+    constexpr int L = 1 << KA;
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+        t.lev[i] = a.levels[i];
+        t.logp[i] = a.logp[i];
+        t.lab[i] = a.labels[i];
+    }
+    for (int i = threadIdx.x; i < KA; i += blockDim.x) t.pos[i] = a.pos[i];
+}
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
+
+// Noise scaling of symbol i: one value per call, or one per frame.
+struct NoiseScale {
+    const float* frames;  // nullptr: use `value`
+    float value;
+    ck::FastDiv frame_len;
+
+    __device__ __forceinline__ float at(uint32_t i) const {
+        return frames ? __ldg(frames + frame_len.div(i)) : value;
+    }
+};
+
+// Both axes' tables of one method, in shared memory.
+template <int KA, int METHOD>
+struct Tables;
+template <int KA>
+struct Tables<KA, 0> {  // closed-form max-log
+    MaxlogAxis<KA> re, im;
+    __device__ __forceinline__ void load(const ck_axis_maxlog& r, const ck_axis_maxlog& i) {
+        load_maxlog_axis(re, r);
+        load_maxlog_axis(im, i);
+    }
+    __device__ __forceinline__ void symbol(float2 x, float s2, float* o) const {
+        axis_maxlog<KA>(x.x, re, s2, o);
+        axis_maxlog<KA>(x.y, im, s2, o + KA);
+    }
+};
+template <int KA>
+struct Tables<KA, 1> {  // level metrics, max-log
+    LevelAxis<KA> re, im;
+    __device__ __forceinline__ void load(const ck_axis_levels& r, const ck_axis_levels& i) {
+        load_level_axis(re, r);
+        load_level_axis(im, i);
+    }
+    __device__ __forceinline__ void symbol(float2 x, float s2, float* o) const {
+        axis_levels<KA, false>(x.x, re, s2, o);
+        axis_levels<KA, false>(x.y, im, s2, o + KA);
+    }
+};
+template <int KA>
+struct Tables<KA, 2> : Tables<KA, 1> {  // level metrics, exact
+    __device__ __forceinline__ void symbol(float2 x, float s2, float* o) const {
+        axis_levels<KA, true>(x.x, this->re, s2, o);
+        axis_levels<KA, true>(x.y, this->im, s2, o + KA);
+    }
+};
+
+template <int METHOD>
+struct AxisArg {
+    using type = ck_axis_levels;
+};
+template <>
+struct AxisArg<0> {
+    using type = ck_axis_maxlog;
+};
+
+// Writes the K = 2 KA LLRs `o` (axis bit order) of symbol i to their
+// label positions when those are not the standard ones.
+template <int KA, class T>
+__device__ __forceinline__ void store_scattered(const T& tab, float* out, uint32_t i,
+                                                const float* o) {
+    constexpr int K = 2 * KA;
+    float* row = out + static_cast<uint64_t>(i) * K;
+#pragma unroll
+    for (int b = 0; b < KA; ++b) {
+        row[tab.re.pos[b]] = o[b];
+        row[tab.im.pos[b]] = o[KA + b];
+    }
+}
+
+// Main kernel: two symbols per 16-byte load, two loads in flight per thread.
+// PAIRS = false is the fallback for buffers that are not 16-byte aligned:
+// one symbol per thread and scalar stores.
+template <int KA, int METHOD, bool PAIRS>
+__global__ void __launch_bounds__(kThreads) llr_kernel(const float2* __restrict__ x, uint32_t n,
+                                                       const typename AxisArg<METHOD>::type re,
+                                                       const typename AxisArg<METHOD>::type im,
+                                                       const NoiseScale noise,
+                                                       float* __restrict__ out) {
+    constexpr int K = 2 * KA;
+    __shared__ Tables<KA, METHOD> tab;
+    tab.load(re, im);
+    __syncthreads();
+    bool standard = true;
+#pragma unroll
+    for (int b = 0; b < KA; ++b)
+        standard = standard && tab.re.pos[b] == b && tab.im.pos[b] == KA + b;
+
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (PAIRS) {
+        const uint32_t npairs = n >> 1;
+        const float4* x4 = reinterpret_cast<const float4*>(x);
+        for (uint32_t p = t0; p < npairs; p += 2 * stride) {
+            const uint32_t pb = p + stride;
+            const bool two = pb < npairs;
+            const float4 va = ld_stream(x4 + p);
+            float4 vb = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (two) vb = ld_stream(x4 + pb);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                if (h == 1 && !two) break;
+                const uint32_t pp = h ? pb : p;
+                const float4 v = h ? vb : va;
+                float o[2 * K];
+                tab.symbol(make_float2(v.x, v.y), noise.at(2 * pp), o);
+                tab.symbol(make_float2(v.z, v.w), noise.at(2 * pp + 1), o + K);
+                if (standard) {
+                    float4* dst = reinterpret_cast<float4*>(out + static_cast<uint64_t>(pp) * 2 * K);
+#pragma unroll
+                    for (int q = 0; q < K / 2; ++q)
+                        st_stream(dst + q, make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2],
+                                                       o[4 * q + 3]));
+                } else {
+                    store_scattered<KA>(tab, out, 2 * pp, o);
+                    store_scattered<KA>(tab, out, 2 * pp + 1, o + K);
+                }
+            }
+        }
+        // Odd count: the last symbol.
+        if ((n & 1u) && t0 == 0) {
+            const uint32_t i = n - 1;
+            float o[K];
+            tab.symbol(x[i], noise.at(i), o);
+            store_scattered<KA>(tab, out, i, o);
+        }
+    } else {
+        for (uint32_t i = t0; i < n; i += stride) {
+            float o[K];
+            tab.symbol(ld_stream(x + i), noise.at(i), o);
+            store_scattered<KA>(tab, out, i, o);
+        }
+    }
+}
+
+template <int KA, int METHOD, class AX>
+int launch_ka(const void* x, uint32_t n, const AX& re, const AX& im, const NoiseScale& noise,
+              float* out, cudaStream_t stream) {
+    const bool aligned = (reinterpret_cast<uintptr_t>(x) % 16 == 0) &&
+                         (reinterpret_cast<uintptr_t>(out) % 16 == 0);
+    const uint32_t work = aligned ? (n / 2 + 1) : n;
+    const uint32_t want = (work + kThreads - 1) / kThreads;
+    const uint32_t cap = static_cast<uint32_t>(num_sms()) * 8u;  // 8 blocks of 256 per SM
+    const uint32_t blocks = want < cap ? (want > 0 ? want : 1) : cap;
+    const float2* xs = static_cast<const float2*>(x);
+    if (aligned)
+        llr_kernel<KA, METHOD, true><<<blocks, kThreads, 0, stream>>>(xs, n, re, im, noise, out);
+    else
+        llr_kernel<KA, METHOD, false><<<blocks, kThreads, 0, stream>>>(xs, n, re, im, noise, out);
+    return ck::cuda_check(cudaGetLastError(), "LLR kernel launch");
+}
+
+}  // namespace llr
+}  // namespace ck

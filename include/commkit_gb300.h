@@ -1,0 +1,234 @@
+/*
+ * commkit-gb300: C ABI of the GB300 (sm_103a) coded-modulation receiver
+ * back end, the soft LLR demapper and the layered QC-LDPC min-sum decoder
+ * of commkit, rebuilt as hand-written CUDA.
+ *
+ * Conventions
+ *  - Plain pointers and sizes only.  Array arguments are DEVICE pointers
+ *    unless a comment says "host"; they must stay valid until the work
+ *    queued on `stream` has run.
+ *  - `stream` is a cudaStream_t passed as void* (NULL: the legacy default
+ *    stream).  Work is queued asynchronously; nothing here synchronizes
+ *    the stream unless its comment says so.
+ *  - Every function returns a ck_status.  On error, ck_last_error() gives
+ *    a message for the calling host thread.  No function traps or aborts.
+ *  - Bit labels are MSB first; a positive LLR means bit 0 is more likely.
+ */
+#ifndef COMMKIT_GB300_H
+#define COMMKIT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum ck_status {
+    CK_OK = 0,
+    CK_ERR_INVALID_ARGUMENT = 1, /* bad size, shape or table: Python ValueError */
+    CK_ERR_UNSUPPORTED = 2,      /* valid input outside what the kernels handle */
+    CK_ERR_CUDA = 3,             /* a CUDA runtime call failed */
+    CK_ERR_OUT_OF_MEMORY = 4,    /* a device allocation failed */
+    CK_ERR_DEVICE_TIMEOUT = 5    /* a bounded device-side wait gave up */
+} ck_status;
+
+/* Message of the last error on this host thread ("" if none). */
+const char* ck_last_error(void);
+/* Static description of a status code. */
+const char* ck_status_string(int status);
+/* Library version, e.g. "0.1.0". */
+const char* ck_version(void);
+
+/* ---------------------------------------------------------------------- */
+/* LLR demapping of separable (Gray square) QAM                            */
+/* ---------------------------------------------------------------------- */
+
+/* Largest number of bits per symbol (commkit/_cuda/llr.py:12, LLR_MAX_K). */
+#define CK_LLR_MAX_K 16
+
+/*
+ * One axis of a separable constellation for the closed-form max-log
+ * (commkit/_cuda/llr.py:163-204, the `re`/`im` tuples
+ * (levels, labels, lo, hi, positions)).  Device arrays:
+ *   levels (L,) float32, ascending and equally spaced, L >= 2
+ *   labels (L,) int32, the axis's k bits of each level, MSB first
+ *   lo, hi (k, L) int32, per bit and level the nearest level below /
+ *          above with the other bit value, -1 for none
+ *   pos    (k,) int32, position of each of the axis's bits in the label
+ */
+typedef struct ck_axis_maxlog {
+    const float* levels;
+    const int32_t* labels;
+    const int32_t* lo;
+    const int32_t* hi;
+    const int32_t* pos;
+    int32_t L;
+    int32_t k;
+} ck_axis_maxlog;
+
+/*
+ * One axis for the level-metric demapper (commkit/_cuda/llr.py:100-145,
+ * the tuples (levels, log_prior, labels, positions)).  Device arrays:
+ *   levels (L,) float32; logp (L,) float32 log marginal prior (zeros for
+ *   uniform); labels (L,) int32; pos (k,) int32.  L <= 256.
+ */
+typedef struct ck_axis_levels {
+    const float* levels;
+    const float* logp;
+    const int32_t* labels;
+    const int32_t* pos;
+    int32_t L;
+    int32_t k;
+} ck_axis_levels;
+
+/*
+ * Closed-form max-log LLRs of a uniform separable constellation.
+ * Replaces the launcher `llr_separable_maxlog(x, re, im, *, inv_s2)`
+ * (commkit/_cuda/llr.py:150-206) and its kernel (commkit/_cuda/src/llr.cu:262-337).
+ *   x   (n,) complex64 symbols (interleaved float pairs), 8-byte aligned
+ *   out (n, re->k + im->k) float32 LLRs, the bits of a symbol adjacent
+ *   inv_s2 = float32(1 / max(noise_var, 1e-20))
+ * n < 2^31; 1 <= k <= CK_LLR_MAX_K.  Results are bit-identical to the
+ * reference's float32 formula evaluated in IEEE arithmetic.
+ */
+int ck_llr_separable_maxlog(const void* x, int64_t n, const ck_axis_maxlog* re,
+                            const ck_axis_maxlog* im, float inv_s2, float* out,
+                            void* stream);
+
+/*
+ * Max-log (exact = 0) or log-sum-exp (exact = 1) LLRs from the metrics of
+ * each axis's levels.  Replaces `llr_separable(x, re, im, *, inv_s2, exact)`
+ * (commkit/_cuda/llr.py:87-147; kernel commkit/_cuda/src/llr.cu:225-259),
+ * with the exact sums of commkit/mapping/_numba_llr.py:35-92.
+ */
+int ck_llr_separable(const void* x, int64_t n, const ck_axis_levels* re,
+                     const ck_axis_levels* im, float inv_s2, int32_t exact, float* out,
+                     void* stream);
+
+/*
+ * Batched forms: `inv_s2` is a DEVICE array with one value per frame of
+ * `frame_len` symbols (symbol i uses inv_s2[i / frame_len]), so frames of
+ * different noise variance demap in one launch.  Each frame's LLRs equal
+ * those of the single-variance call on that frame.  No counterpart in the
+ * reference, whose API takes one noise variance per call.
+ */
+int ck_llr_separable_maxlog_frames(const void* x, int64_t n, int64_t frame_len,
+                                   const float* inv_s2, const ck_axis_maxlog* re,
+                                   const ck_axis_maxlog* im, float* out, void* stream);
+int ck_llr_separable_frames(const void* x, int64_t n, int64_t frame_len, const float* inv_s2,
+                            const ck_axis_levels* re, const ck_axis_levels* im,
+                            int32_t exact, float* out, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* Layered LDPC decoding                                                   */
+/* ---------------------------------------------------------------------- */
+
+/*
+ * First-fit layer schedule of a parity-check matrix, on the host.
+ * Restates LDPCCode._schedule / _first_fit (commkit/coding/ldpc.py:283-296,
+ * 422-442): rows in natural order take the lowest layer none of whose rows
+ * shares a bit; rows are then stably grouped by layer.
+ *   checks, variables (E,) host int32: the edges sorted by (row, column)
+ *   row_ptr (m + 1,), cols (E,), layer_ptr (m + 1,) host int32 outputs
+ *   *num_layers: layers written to layer_ptr (layer_ptr has L + 1 entries)
+ */
+int ck_ldpc_schedule(const int32_t* checks, const int32_t* variables, int64_t E, int32_t m,
+                     int32_t N, int32_t* row_ptr, int32_t* cols, int32_t* layer_ptr,
+                     int32_t* num_layers);
+
+typedef struct ck_ldpc_plan ck_ldpc_plan;
+
+/*
+ * A decoding plan for one code on the current device: validates the
+ * schedule (host arrays row_ptr (m+1), cols (E), layer_ptr (L+1), the
+ * output of LDPCCode._schedule, commkit/coding/ldpc.py:283-296), recovers
+ * the circulant structure when the code is quasi-cyclic, and uploads the
+ * tables.  Synchronous (it copies the tables to the device).  The rows of
+ * a layer must share no variable and every row needs >= 2 edges.
+ */
+int ck_ldpc_plan_create(const int32_t* row_ptr, const int32_t* cols, const int32_t* layer_ptr,
+                        int32_t m, int32_t N, int32_t num_layers, ck_ldpc_plan** plan);
+int ck_ldpc_plan_destroy(ck_ldpc_plan* plan);
+
+/* What the plan found. */
+typedef struct ck_ldpc_plan_info {
+    int32_t quasi_cyclic;   /* 1: circulant tables, 0: CSR tables */
+    int32_t lifting;        /* Z (QC only) */
+    int32_t base_rows;      /* mb (QC only) */
+    int32_t base_cols;      /* nb (QC only) */
+    int32_t blocks;         /* nonzero circulants (QC only) */
+    int32_t num_checks;     /* m */
+    int32_t num_variables;  /* N */
+    int32_t num_edges;      /* E */
+    int32_t num_layers;     /* L */
+    int32_t max_row_degree;
+    int32_t device;
+} ck_ldpc_plan_info;
+int ck_ldpc_plan_get_info(const ck_ldpc_plan* plan, ck_ldpc_plan_info* info);
+
+/*
+ * Launch shape of the decoder: threads per frame (a multiple of 32, at
+ * most 1024), frames per thread block and where the compressed
+ * check-to-variable messages live; 0 lets the plan choose.  Every shape
+ * gives the same results bit for bit; it only changes speed.  The
+ * autotuner sets it per code.
+ */
+typedef struct ck_ldpc_launch {
+    int32_t threads_per_frame;
+    int32_t frames_per_block;
+    int32_t placement; /* CK_LDPC_PLACE_*: where the check-message state lives */
+} ck_ldpc_launch;
+
+#define CK_LDPC_PLACE_AUTO 0   /* the plan chooses */
+#define CK_LDPC_PLACE_SHARED 1 /* shared memory, beside the frame's LLRs */
+#define CK_LDPC_PLACE_GLOBAL 2 /* device memory (L2-resident working set) */
+int ck_ldpc_plan_set_launch(ck_ldpc_plan* plan, const ck_ldpc_launch* launch);
+int ck_ldpc_plan_get_launch(const ck_ldpc_plan* plan, ck_ldpc_launch* launch);
+
+#define CK_LDPC_MIN_SUM 0
+#define CK_LDPC_SUM_PRODUCT 1
+
+/* Device scratch bytes ck_ldpc_decode needs for B frames with `rule`. */
+int ck_ldpc_workspace_size(const ck_ldpc_plan* plan, int64_t B, int32_t rule, size_t* bytes);
+
+/*
+ * Layered belief-propagation decoding of B frames.  Replaces the launcher
+ * `ldpc_layered(app, row_ptr, cols, layer_ptr, *, scale, offset,
+ * max_iterations, early_stop) -> (iters, valid)` (commkit/_cuda/coding.py:
+ * 27-67; kernel commkit/_cuda/src/ldpc.cu:107-159) and fuses the steps
+ * around it in LDPCCode's _decode (commkit/coding/ldpc.py:544-588): the
+ * zero-padding of punctured bits and the hard decisions of the info bits.
+ *   llr_in  (B, n_in) float32 channel LLRs, n_in <= N (the last N - n_in
+ *           variables, punctured, start at LLR 0)
+ *   llr_out (B, n_in) float32 a-posteriori LLRs; may equal llr_in (in place,
+ *           the reference's `app` with n_in = N)
+ *   rule    CK_LDPC_MIN_SUM (`scale`, `offset` as MinSum) or
+ *           CK_LDPC_SUM_PRODUCT (`scale`, `offset` ignored)
+ *   iters   (B,) int32 iterations run (-1 if a device wait gave up)
+ *   valid   (B,) uint8 1 when every check is satisfied
+ *   bits    (B, k_bits) int8 hard decisions of the first k_bits variables,
+ *           or NULL
+ *   workspace: device scratch of at least ck_ldpc_workspace_size() bytes,
+ *           256-byte aligned; NULL makes the call allocate and free it
+ *           stream-ordered (cudaMallocAsync / cudaFreeAsync).
+ * Min-sum results (LLRs, bits, iterations, valid) are bit-identical to
+ * the reference's kernel and its Numba twin.  B < 2^31.
+ */
+int ck_ldpc_decode(const ck_ldpc_plan* plan, const float* llr_in, float* llr_out, int64_t B,
+                   int32_t n_in, int32_t rule, float scale, float offset,
+                   int32_t max_iterations, int32_t early_stop, int32_t* iters, uint8_t* valid,
+                   int8_t* bits, int32_t k_bits, void* workspace, size_t workspace_bytes,
+                   void* stream);
+
+/*
+ * Reads the device status word a decode left in `workspace` (synchronizes
+ * `stream`): CK_OK, or CK_ERR_DEVICE_TIMEOUT if a bounded wait gave up.
+ */
+int ck_ldpc_workspace_status(const void* workspace, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COMMKIT_GB300_H */

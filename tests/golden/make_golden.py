@@ -1,0 +1,281 @@
+"""Generate the golden fixtures of ``tests/golden/`` by running the reference.
+
+Run once, where the reference source tree is available::
+
+    python tests/golden/make_golden.py /path/to/commkit-reference
+
+It imports ``commkit`` from that tree with a no-op ``numba`` stand-in
+(``njit`` -> identity, ``prange`` -> ``range``), so the reference's Numba
+kernels run as plain Python on numpy float32 scalars, as its own CI runs
+them with ``NUMBA_DISABLE_JIT=1`` (``.github/workflows/ci.yml:91-116``).
+Every output here is the reference's own result on seeded inputs:
+
+* ``qam_tables.npz``: Gray QAM points, labels and the per-axis demapper
+  tables (``commkit/mapping/_lattice.py:100-124``, ``_demap.py:82-106,355``)
+  for 4/16/64/256-QAM;
+* ``llr_golden.npz``: LLRs of seeded symbols (plus ties at level midpoints
+  and far-out points) from the closed-form max-log kernel and the
+  level-metric max-log and exact kernels (``commkit/mapping/_numba_llr.py``);
+* ``ldpc_golden.npz``: the first-fit schedules and min-sum decodes of the
+  seeded codes A, B and C (``commkit_gb300.workloads``) and of the
+  reference's own known-answer cases, DVB-S2 short 1/2 and PON with
+  ``MinSum(0.75, 0.05, 12)`` on ``1.8 + 1.5 N(0,1)`` LLRs of seed 1
+  (``tests/coding/test_ldpc_kernel.py:16-34``).
+
+Large outputs are stored as SHA-256 digests of their bytes (negative zeros
+folded to +0) plus their first frame; inputs drawn from ``default_rng``
+are stored as a digest and regenerated by the tests.
+"""
+
+from __future__ import annotations
+
+import hashlib
+import sys
+import time
+import types
+from concurrent.futures import ProcessPoolExecutor
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parents[1]
+
+
+def digest(a: np.ndarray) -> str:
+    a = np.ascontiguousarray(a)
+    if a.dtype.kind == "f":
+        a = np.where(a == 0, np.zeros_like(a), a)
+    return hashlib.sha256(a.tobytes()).hexdigest()
+
+
+def _numba_stand_in() -> None:
+    if "numba" in sys.modules:
+        return
+    mod = types.ModuleType("numba")
+
+    def njit(*args, **kwargs):
+        if len(args) == 1 and callable(args[0]) and not kwargs:
+            return args[0]
+        return lambda f: f
+
+    class _Any:
+        def __getattr__(self, name):
+            return self
+
+        def __call__(self, *a, **k):
+            return self
+
+        def __getitem__(self, k):
+            return self
+
+    mod.njit = mod.jit = njit
+    mod.vectorize = mod.guvectorize = lambda *a, **k: (lambda f: f)
+    mod.prange = range
+    mod.get_num_threads = lambda: 1
+    mod.set_num_threads = lambda n: None
+    mod.types = mod.config = _Any()
+    sys.modules["numba"] = mod
+
+
+def _import_reference(ref: str):
+    _numba_stand_in()
+    if ref not in sys.path:
+        sys.path.insert(0, ref)
+    if str(REPO) not in sys.path:
+        sys.path.insert(0, str(REPO))
+    import commkit
+
+    return commkit
+
+
+# ---------------------------------------------------------------------------
+
+
+def qam_tables(ref: str) -> dict:
+    _import_reference(ref)
+    from commkit.mapping import Constellation
+    from commkit.mapping._demap import _opposite_levels, _packed_labels
+
+    out = {}
+    for order in (4, 16, 64, 256):
+        c = Constellation.qam(order)
+        out[f"q{order}_points"] = np.asarray(c.points)
+        out[f"q{order}_bit_labels"] = np.asarray(c.bit_labels, np.int8)
+        out[f"q{order}_power"] = np.float64(c.power())
+        for name, ax in zip(("re", "im"), c._axes, strict=True):
+            lo, hi = _opposite_levels(ax.labels)
+            out[f"q{order}_{name}_levels"] = ax.levels.astype(np.float32)
+            out[f"q{order}_{name}_labels"] = _packed_labels(ax.labels).astype(np.int32)
+            out[f"q{order}_{name}_lo"] = lo
+            out[f"q{order}_{name}_hi"] = hi
+            out[f"q{order}_{name}_pos"] = ax.bits.astype(np.int32)
+    return out
+
+
+def llr_symbols(order: int, seed: int, n: int = 480) -> np.ndarray:
+    """Seeded symbols: noisy points, exact midpoints between levels, far-out
+    points and zeros."""
+    from commkit_gb300.workloads import gray_qam_points
+
+    rng = np.random.default_rng(seed)
+    pts = gray_qam_points(order).astype(np.complex64)
+    x = pts[rng.integers(0, order, n)] + (0.15 * rng.standard_normal(n)
+                                          + 0.15j * rng.standard_normal(n)).astype(np.complex64)  # fmt: skip
+    lev = np.unique(pts.real)
+    mids = ((lev[1:] + lev[:-1]) / 2).astype(np.float32)
+    special = [complex(a, b) for a in mids for b in mids[:2]]
+    special += [complex(3.0 * lev[-1], -4.0 * lev[-1]), complex(-50.0, 50.0), 0j, complex(lev[0], lev[-1])]
+    return np.concatenate([x.astype(np.complex64), np.asarray(special, np.complex64)])
+
+
+def llr_golden(ref: str) -> dict:
+    _import_reference(ref)
+    from commkit.mapping import Constellation
+    from commkit.mapping import _numba_llr as K
+    from commkit.mapping._demap import _half_indices, _log_prior, _opposite_levels, _packed_labels
+
+    out = {}
+    for order in (4, 16, 64, 256):
+        c = Constellation.qam(order)
+        re, im = c._axes
+        k = re.bits.size + im.bits.size
+        for ni, nv in enumerate((0.5, 0.05, 1e-3)):
+            x = llr_symbols(order, seed=100 + 10 * order + ni)
+            inv_s2 = np.float32(1.0 / max(nv, 1e-20))
+            xr, xi = x.real, x.imag
+            closed = np.empty((x.size, k), np.float32)
+            args = []
+            for a in (re, im):
+                lo, hi = _opposite_levels(a.labels)
+                args += [a.levels.astype(np.float32), _packed_labels(a.labels), lo, hi,
+                         a.bits.astype(np.int64)]  # fmt: skip
+            K.llr_separable_maxlog_kernel(xr, xi, *args, inv_s2, closed)
+            tabs = (re.levels.astype(np.float32), im.levels.astype(np.float32),
+                    _log_prior(re.pmf, re.levels.size), _log_prior(im.pmf, im.levels.size),
+                    _half_indices(re.labels), _half_indices(im.labels),
+                    re.bits.astype(np.int64), im.bits.astype(np.int64))  # fmt: skip
+            levels_max = np.empty((x.size, k), np.float32)
+            K.llr_separable_kernel(xr, xi, *tabs, inv_s2, False, levels_max)
+            exact = np.empty((x.size, k), np.float32)
+            K.llr_separable_kernel(xr, xi, *tabs, inv_s2, True, exact)
+            key = f"q{order}_n{ni}"
+            out[key + "_x"] = x
+            out[key + "_nv"] = np.float64(nv)
+            out[key + "_inv_s2"] = inv_s2
+            out[key + "_closed"] = closed
+            out[key + "_levels_maxlog"] = levels_max
+            out[key + "_exact"] = exact
+    return out
+
+
+def _decode_case(ref: str, code, llrs: np.ndarray, method) -> dict:
+    from commkit.coding import decode
+
+    res = decode(llrs.reshape(-1), code=code, method=method)
+    B = llrs.shape[0]
+    post = np.asarray(res.llrs, np.float32).reshape(B, -1)
+    return {
+        "post_digest": digest(post),
+        "post_first": post[0].copy(),
+        "bits_packed": np.packbits(np.asarray(res.bits, np.uint8).reshape(B, -1), axis=1),
+        "valid": np.asarray(res.valid, bool),
+        "iters": np.asarray(res.iterations, np.int32),
+    }
+
+
+def ldpc_qc_case(ref: str, name: str, frames: int, order: int, ebn0: float,
+                 max_iterations: int, method_name: str) -> dict:  # fmt: skip
+    """A seeded code of ``commkit_gb300.workloads`` through the reference:
+    schedule, encode (checked against the workload encoder), LLRs, decode."""
+    commkit = _import_reference(ref)
+    from commkit.coding import LDPCCode, MinSum, encode
+    from commkit.coding import ldpc as ldpc_module
+    from commkit.mapping import Constellation, compute_llr
+
+    from commkit_gb300 import workloads as W
+
+    spec = W.CODES[name]
+    base = spec.base()
+    ldpc_module._MAX_INVERSE = max(ldpc_module._MAX_INVERSE, base.shape[0] * spec.z)
+    code = LDPCCode.quasi_cyclic(base, lifting=spec.z)
+    row_ptr, cols, layer_ptr = code._schedule
+    batch = W.coded_batch(spec, frames, order, ebn0, seed=7)
+    ref_words = np.asarray(encode(batch.info.reshape(-1), code=code)).reshape(frames, -1)
+    ours = W.encode_qc(base, spec.z, batch.info)
+    assert np.array_equal(ref_words, ours), "workload encoder differs from the reference's"
+    c = Constellation.qam(order)
+    method = "exact" if method_name == "exact" else "maxlog"
+    llrs = np.stack([
+        np.asarray(compute_llr(batch.symbols[f], noise_var=float(batch.noise_var[f]),
+                               constellation=c, method=method), np.float32)
+        for f in range(frames)
+    ])  # fmt: skip
+    case = _decode_case(ref, code, llrs, MinSum(max_iterations=max_iterations))
+    out = {f"{name}_{k}": v for k, v in case.items()}
+    out.update({
+        f"{name}_base": base, f"{name}_z": np.int64(spec.z), f"{name}_order": np.int64(order),
+        f"{name}_ebn0": np.float64(ebn0), f"{name}_frames": np.int64(frames),
+        f"{name}_max_iterations": np.int64(max_iterations), f"{name}_llr_method": method,
+        f"{name}_layer_ptr": layer_ptr.astype(np.int32),
+        f"{name}_schedule_digest": digest(np.concatenate([row_ptr, cols]).astype(np.int32)),
+        f"{name}_symbols_digest": digest(batch.symbols),
+        f"{name}_llrs": llrs if llrs.size <= 40000 else np.zeros(0, np.float32),
+        f"{name}_llrs_digest": digest(llrs), f"{name}_k": np.int64(code.k),
+    })  # fmt: skip
+    del commkit
+    return out
+
+
+def kat_case(ref: str, which: str) -> dict:
+    """The reference's bit-exactness cases (``tests/coding/test_ldpc_kernel.py:16-34``)."""
+    _import_reference(ref)
+    from commkit.coding import LDPCCode, MinSum
+
+    code = LDPCCode.dvbs2("1/2", frame="short") if which == "dvbs2s" else LDPCCode.pon()
+    rng = np.random.default_rng(1)
+    llrs = (1.8 + 1.5 * rng.standard_normal((6, code.n))).astype(np.float32)
+    row_ptr, cols, layer_ptr = code._schedule
+    out = {
+        f"{which}_checks": code.checks.astype(np.int32),
+        f"{which}_variables": code.variables.astype(np.int32),
+        f"{which}_m": np.int64(code.num_checks), f"{which}_N": np.int64(code.num_variables),
+        f"{which}_n": np.int64(code.n), f"{which}_k": np.int64(code.k),
+        f"{which}_layer_ptr": layer_ptr.astype(np.int32),
+        f"{which}_schedule_digest": digest(np.concatenate([row_ptr, cols]).astype(np.int32)),
+        f"{which}_llrs_digest": digest(llrs),
+    }  # fmt: skip
+    for es in (False, True):
+        case = _decode_case(ref, code, llrs,
+                            MinSum(scale=0.75, offset=0.05, max_iterations=12, early_stop=es))  # fmt: skip
+        out.update({f"{which}_es{int(es)}_{k}": v for k, v in case.items()})
+    return out
+
+
+def main(ref: str) -> None:
+    t0 = time.time()
+    jobs = {
+        "qam": (qam_tables, (ref,)),
+        "llr": (llr_golden, (ref,)),
+        "A": (ldpc_qc_case, (ref, "A", 8, 4, 2.5, 20, "exact")),
+        "B": (ldpc_qc_case, (ref, "B", 6, 16, 3.5, 20, "maxlog")),
+        "C": (ldpc_qc_case, (ref, "C", 1, 16, 1.0, 50, "maxlog")),
+        "dvbs2s": (kat_case, (ref, "dvbs2s")),
+        "pon": (kat_case, (ref, "pon")),
+    }
+    import multiprocessing as mp
+
+    with ProcessPoolExecutor(max_workers=len(jobs), mp_context=mp.get_context("spawn")) as pool:
+        futs = {k: pool.submit(fn, *args) for k, (fn, args) in jobs.items()}
+        res = {k: f.result() for k, f in futs.items()}
+    np.savez_compressed(HERE / "qam_tables.npz", **res["qam"])
+    np.savez_compressed(HERE / "llr_golden.npz", **res["llr"])
+    ldpc = {}
+    for k in ("A", "B", "C", "dvbs2s", "pon"):
+        ldpc.update(res[k])
+    np.savez_compressed(HERE / "ldpc_golden.npz", **ldpc)
+    print(f"golden fixtures written in {time.time() - t0:.0f} s")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
