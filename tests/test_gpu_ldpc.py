@@ -1,0 +1,245 @@
+"""GPU decoder parity: the sm_103a layered min-sum decoder against the
+reference's golden decodes and the pinned CPU oracle, bit for bit
+(a-posteriori LLRs, hard decisions, iteration counts, syndrome flags)."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from commkit_gb300 import workloads as W
+from tests.conftest import digest, kat_llrs
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch_dev():
+    import torch
+
+    return torch, torch.device("cuda", 0)
+
+
+@pytest.fixture(scope="module")
+def ck():
+    import commkit_gb300
+
+    return commkit_gb300
+
+
+def _qc_code(ck, name):
+    spec = W.CODES[name]
+    return ck.LDPCCode.quasi_cyclic(spec.base(), lifting=spec.z)
+
+
+def _to_np(res, frames):
+    return (res.bits.cpu().numpy().reshape(frames, -1), res.llrs.cpu().numpy().reshape(frames, -1),
+            res.valid.cpu().numpy().reshape(-1), res.iterations.cpu().numpy().reshape(-1))  # fmt: skip
+
+
+def _assert_same(got, want):
+    for a, b, what in zip(got, want, ("bits", "llrs", "valid", "iterations"), strict=True):
+        np.testing.assert_array_equal(a, b, err_msg=what)
+
+
+def _oracle(code, llrs, **method):
+    row_ptr, cols, _ = code._schedule
+    return oracle.decode(llrs, (row_ptr, cols, code.num_variables), k=code.k, **method)
+
+
+@pytest.mark.parametrize("which", ["dvbs2s", "pon"])
+@pytest.mark.parametrize("early_stop", [False, True])
+def test_reference_kat(golden_ldpc, torch_dev, ck, which, early_stop):
+    """The reference's own bit-exactness cases (tests/coding/test_ldpc_kernel.py:24-34):
+    DVB-S2 short 1/2 (CSR path) and PON (circulant path, punctured)."""
+    torch, dev = torch_dev
+    g = golden_ldpc
+    m, N, n = (int(g[f"{which}_{s}"]) for s in ("m", "N", "n"))
+    code = ck.LDPCCode(g[f"{which}_checks"], g[f"{which}_variables"], m, N, N - n)
+    llrs = kat_llrs(n)
+    res = ck.decode(torch.from_numpy(llrs).to(dev), code=code,
+                    method=ck.MinSum(scale=0.75, offset=0.05, max_iterations=12, early_stop=early_stop))  # fmt: skip
+    bits, post, valid, iters = _to_np(res, 6)
+    p = f"{which}_es{int(early_stop)}"
+    np.testing.assert_array_equal(iters, g[p + "_iters"])
+    np.testing.assert_array_equal(valid, g[p + "_valid"])
+    np.testing.assert_array_equal(np.packbits(bits.astype(np.uint8), axis=1), g[p + "_bits_packed"])
+    np.testing.assert_array_equal(post[0], g[p + "_post_first"])
+    assert digest(post) == g[p + "_post_digest"]
+    info = code._plan(0).info
+    assert info["quasi_cyclic"] == (1 if which == "pon" else 0)
+
+
+@pytest.mark.parametrize("name", ["A", "B"])
+def test_golden_codes(golden_ldpc, torch_dev, ck, name):
+    torch, dev = torch_dev
+    g = golden_ldpc
+    code = _qc_code(ck, name)
+    llrs = g[f"{name}_llrs"]
+    frames = llrs.shape[0]
+    res = ck.decode(torch.from_numpy(llrs).to(dev), code=code,
+                    method=ck.MinSum(max_iterations=int(g[f"{name}_max_iterations"])))  # fmt: skip
+    bits, post, valid, iters = _to_np(res, frames)
+    np.testing.assert_array_equal(iters, g[f"{name}_iters"])
+    np.testing.assert_array_equal(valid, g[f"{name}_valid"])
+    np.testing.assert_array_equal(np.packbits(bits.astype(np.uint8), axis=1), g[f"{name}_bits_packed"])
+    assert digest(post) == g[f"{name}_post_digest"]
+    assert code._plan(0).info["lifting"] == W.CODES[name].z
+
+
+def test_config1_code_a_1024_frames(torch_dev, ck):
+    """Config 1: code A, QPSK at Eb/N0 2.5 dB, exact LLRs, MinSum(max_iterations=20),
+    1024 frames: the GPU demap + decode against the oracle, frame for frame."""
+    torch, dev = torch_dev
+    code = _qc_code(ck, "A")
+    batch = W.coded_batch(W.CODE_A, 1024, 4, 2.5, seed=1)
+    x = torch.from_numpy(batch.symbols).to(dev)
+    c = ck.Constellation.qam(4)
+    llr = ck.compute_llr(x, noise_var=float(batch.noise_var[0]), constellation=c, method="exact")
+    llr_np = llr.cpu().numpy()
+    want_llr = oracle.llr(batch.symbols.reshape(-1), 4, oracle.inv_s2(batch.noise_var[0]),
+                          method="exact").reshape(1024, -1)  # fmt: skip
+    np.testing.assert_allclose(llr_np, want_llr, rtol=1e-5, atol=1e-6)
+    method = ck.MinSum(max_iterations=20)
+    res = ck.decode(llr, code=code, method=method)
+    got = _to_np(res, 1024)
+    _assert_same(got, _oracle(code, llr_np, max_iterations=20))
+    # FER against the transmitted bits is then identical too; report it.
+    fer = np.mean(np.any(got[0] != batch.info, axis=1))
+    assert fer < 0.5
+
+
+@pytest.mark.parametrize("frames", [96])
+def test_config3_code_c(torch_dev, ck, frames):
+    """Config 3 (code C, 16-QAM max-log at Eb/N0 1.0 dB, 50 iterations) on a
+    slice of frames: max-log LLRs and the decode both bit-exact."""
+    torch, dev = torch_dev
+    code = _qc_code(ck, "C")
+    batch = W.coded_batch(W.CODE_C, frames, 16, 1.0, seed=1)
+    x = torch.from_numpy(batch.symbols).to(dev)
+    llr = ck.compute_llr(x, noise_var=float(batch.noise_var[0]), constellation=ck.Constellation.qam(16))
+    llr_np = llr.cpu().numpy()
+    want = oracle.llr(batch.symbols.reshape(-1), 16, oracle.inv_s2(batch.noise_var[0])).reshape(frames, -1)
+    np.testing.assert_array_equal(llr_np, want)
+    res = ck.decode(llr, code=code, method=ck.MinSum(max_iterations=50))
+    _assert_same(_to_np(res, frames), _oracle(code, llr_np, max_iterations=50))
+
+
+@pytest.mark.parametrize("name", ["A", "C"])
+def test_launch_shapes_do_not_change_results(torch_dev, ck, name):
+    """Every launch shape (threads per frame, frames per block, message
+    placement) gives the same bits: the autotuner only changes speed."""
+    torch, dev = torch_dev
+    code = _qc_code(ck, name)
+    spec = W.CODES[name]
+    order = 4 if name == "A" else 16
+    frames = 40
+    batch = W.coded_batch(spec, frames, order, 2.0 if name == "A" else 2.5, seed=4)
+    x = torch.from_numpy(batch.symbols).to(dev)
+    llr = ck.compute_llr(x, noise_var=float(batch.noise_var[0]), constellation=ck.Constellation.qam(order))
+    method = ck.MinSum(max_iterations=12)
+    plan = code._plan(0)
+    base = _to_np(ck.decode(llr, code=code, method=method), frames)
+    _assert_same(base, _oracle(code, llr.cpu().numpy(), max_iterations=12))
+    shapes = [(32, 1, 0), (32, 3, 0), (64, 2, 1), (128, 1, 2), (256, 2, 0), (512, 1, 2)]
+    try:
+        for T, G, place in shapes:
+            try:
+                plan.set_launch(T, G, place)
+                ws = plan.workspace_size(frames)
+            except ValueError:
+                continue  # shape does not fit this code
+            assert ws > 0
+            got = _to_np(ck.decode(llr, code=code, method=method), frames)
+            _assert_same(got, base)
+    finally:
+        plan.set_launch(0, 0, 0)
+
+
+def test_noiseless_codewords_stop_before_the_first_iteration(torch_dev, ck):
+    """``tests/coding/test_ldpc.py:157-165``: codewords decode with 0 iterations."""
+    torch, dev = torch_dev
+    code = _qc_code(ck, "A")
+    info = np.random.default_rng(2).integers(0, 2, (5, code.k), dtype=np.int8)
+    words = W.encode_qc(W.CODE_A.base(), 54, info)
+    res = ck.decode(torch.from_numpy(words).to(dev), code=code)  # int input: hard decisions
+    bits, _, valid, iters = _to_np(res, 5)
+    np.testing.assert_array_equal(bits, info)
+    assert valid.all() and (iters == 0).all()
+
+
+def test_random_llrs_fail_with_max_iterations(torch_dev, ck):
+    """``tests/coding/test_ldpc.py:254-262``: noise decodes to invalid after max_iterations."""
+    torch, dev = torch_dev
+    code = _qc_code(ck, "B")
+    llrs = np.random.default_rng(5).standard_normal((3, code.n)).astype(np.float32)
+    res = ck.decode(torch.from_numpy(llrs).to(dev), code=code, method=ck.MinSum(max_iterations=4))
+    _, _, valid, iters = _to_np(res, 3)
+    assert not valid.any() and (iters == 4).all()
+    res = ck.decode(torch.from_numpy(llrs).to(dev), code=code,
+                    method=ck.MinSum(max_iterations=3, early_stop=False))  # fmt: skip
+    assert (res.iterations.cpu().numpy() == 3).all()
+
+
+def test_inplace_launcher_and_contract(torch_dev, ck):
+    """The reference's launcher interface (commkit/_cuda/coding.py:27-67):
+    in-place ``app``, (iters, valid) back, dtype/shape errors, B = 0."""
+    torch, dev = torch_dev
+    from commkit_gb300 import _cuda
+
+    code = _qc_code(ck, "A")
+    row_ptr, cols, layer_ptr = (torch.from_numpy(a.copy()).to(dev) for a in code._schedule)
+    launch = _cuda.get_kernel("ldpc_layered")
+    llrs = (1.0 + 1.5 * np.random.default_rng(3).standard_normal((7, code.num_variables))).astype(np.float32)
+    app = torch.from_numpy(llrs).to(dev)
+    kw = dict(scale=0.875, offset=0.0, max_iterations=9, early_stop=True)
+    iters, valid = launch(app, row_ptr, cols, layer_ptr, **kw)
+    row, col, _ = code._schedule
+    post, want_it, want_ok = oracle.ldpc_layered(llrs.copy(), row, col, max_iterations=9)
+    np.testing.assert_array_equal(app.cpu().numpy(), post)
+    np.testing.assert_array_equal(iters.cpu().numpy(), want_it)
+    np.testing.assert_array_equal(valid.cpu().numpy(), want_ok)
+    with pytest.raises(TypeError, match="float32"):
+        launch(app.to(torch.float64), row_ptr, cols, layer_ptr, **kw)
+    with pytest.raises(TypeError, match="int32"):
+        launch(app, row_ptr.to(torch.int64), cols, layer_ptr, **kw)
+    it0, ok0 = launch(app[:0], row_ptr, cols, layer_ptr, **kw)
+    assert it0.shape == (0,) and ok0.shape == (0,)
+
+
+def test_decode_shapes_and_errors(torch_dev, ck):
+    torch, dev = torch_dev
+    code = _qc_code(ck, "A")
+    x = torch.zeros((2, 3 * code.n), dtype=torch.float32, device=dev)
+    res = ck.decode(x, code=code)
+    assert res.bits.shape == (2, 3 * code.k) and res.llrs.shape == (2, 3 * code.n)
+    assert res.valid.shape == (2, 3) and res.iterations.shape == (2, 3) and res.checked
+    assert res.valid.dtype == torch.bool
+    res1 = ck.decode(x[0], code=code)
+    assert res1.bits.shape == (3 * code.k,)
+    with pytest.raises(ValueError, match="multiple"):
+        ck.decode(x[:, :-1], code=code)
+    with pytest.raises(NotImplementedError):
+        ck.decode(x, code=code, method=ck.SumProduct())
+    with pytest.warns(ck.PrecisionWarning):
+        ck.decode(x.to(torch.float64), code=code)
+    empty = ck.decode(x[:0], code=code)
+    assert empty.bits.shape == (0, 3 * code.k)
+
+
+def test_workspace_is_reused_and_status_is_clean(torch_dev, ck):
+    torch, dev = torch_dev
+    from commkit_gb300 import _device, _lib
+
+    code = _qc_code(ck, "C")
+    batch = W.coded_batch(W.CODE_C, 6, 16, 3.0, seed=9)
+    llr = ck.compute_llr(torch.from_numpy(batch.symbols).to(dev), noise_var=float(batch.noise_var[0]),
+                         constellation=ck.Constellation.qam(16))  # fmt: skip
+    plan = code._plan(0)
+    ws = torch.empty(plan.workspace_size(6), dtype=torch.uint8, device=dev)
+    a = _to_np(ck.decode(llr, code=code, workspace=ws), 6)
+    b = _to_np(ck.decode(llr, code=code, workspace=ws), 6)
+    _assert_same(a, b)
+    st = _lib.lib().ck_ldpc_workspace_status(_device.wrap(ws).ptr, _device.stream_of(_device.wrap(ws)))
+    assert st == _lib.CK_OK
