@@ -46,6 +46,7 @@ EXPORTS = (
     "ck_ldpc_workspace_size",
     "ck_ldpc_decode",
     "ck_ldpc_workspace_status",
+    "ck_ldpc_decode_static",
 )
 
 
@@ -123,6 +124,8 @@ def _declare(lib: ctypes.CDLL) -> None:
             [p, p, p, i64, i32, i32, f32, f32, i32, i32, p, p, p, i32, p, ctypes.c_size_t, p],
             ctypes.c_int),
         "ck_ldpc_workspace_status": ([p, p], ctypes.c_int),
+        "ck_ldpc_decode_static": (
+            [p, p, p, i64, i32, i32, f32, f32, i32, i32, p, p, p, i32, p], ctypes.c_int),
     }  # fmt: skip
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)

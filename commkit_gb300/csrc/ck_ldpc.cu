@@ -587,3 +587,104 @@ extern "C" int ck_ldpc_workspace_status(const void* workspace, void* stream) {
         return ck::fail(CK_ERR_DEVICE_TIMEOUT, "a bulk copy of the decoder did not complete");
     return CK_OK;
 }
+
+// Decode into caller-provided scratch of a fixed capacity (the allocation-free
+// entry point of ck_ldpc_static.cu): the same kernel and launch shape as
+// ck_ldpc_decode, with the persistent grid cut down to the frame slots whose
+// device-memory state fits in `scratch_bytes`.  Frames beyond the slots wait
+// in the device queue, so any B fits; a code whose one slot does not fit is
+// rejected.
+int ck::ldpc_decode_in_scratch(const ck_ldpc_plan* plan, const float* llr_in, float* llr_out,
+                               int64_t B, int32_t n_in, float scale, float offset,
+                               int32_t max_iterations, int32_t early_stop, int32_t* iters,
+                               uint8_t* valid, int8_t* bits, int32_t k_bits, void* scratch,
+                               size_t scratch_bytes, cudaStream_t s) {
+    if (B < 0 || B >= (int64_t(1) << 31))
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "B must be in [0, 2**31), got %lld",
+                        static_cast<long long>(B));
+    if (n_in < 1 || n_in > plan->N)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "n_in must be in [1, N=%d], got %d", plan->N,
+                        n_in);
+    if (max_iterations < 0)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "max_iterations must be >= 0");
+    if (bits && (k_bits < 0 || k_bits > n_in))
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "k_bits must be in [0, n_in]");
+    if (B == 0) return CK_OK;
+    if (!llr_in || !llr_out || !iters || !valid)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "llr_in, llr_out, iters and valid are required");
+    if (reinterpret_cast<uintptr_t>(llr_in) % 4 || reinterpret_cast<uintptr_t>(llr_out) % 4)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "LLR buffers must be 4-byte aligned");
+    if (reinterpret_cast<uintptr_t>(scratch) % 256)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "scratch must be 256-byte aligned");
+    CK_TRY(check_device(plan));
+    Resolved r;
+    CK_TRY(resolve(plan, B, &r));
+    // Bytes of device-memory state per frame slot (the header is shared).
+    const size_t r_bytes = r.r_smem ? 0 : static_cast<size_t>(3) * r.r_stride * 4;
+    const size_t app_bytes = r.app_smem ? 0 : static_cast<size_t>(r.app_stride) * 4;
+    const size_t per_slot = r_bytes + app_bytes;
+    if (per_slot > 0) {
+        const size_t usable = scratch_bytes > kHeaderBytes + 256 ? scratch_bytes - kHeaderBytes - 256 : 0;
+        const size_t max_slots = usable / per_slot;
+        if (max_slots < static_cast<size_t>(r.G))
+            return ck::fail(CK_ERR_UNSUPPORTED,
+                            "one block of %d frames needs %zu bytes of scratch, the static "
+                            "scratch holds %zu",
+                            r.G, kHeaderBytes + 256 + per_slot * r.G, scratch_bytes);
+        const int grid_cap = static_cast<int>(max_slots / r.G);
+        if (r.grid > grid_cap) r.grid = grid_cap;
+    }
+    const size_t slots = static_cast<size_t>(r.grid) * r.G;
+    r.r_ws_off = kHeaderBytes;
+    r.app_ws_off = kHeaderBytes + ((slots * r_bytes + 255) / 256) * 256;
+    r.ws_bytes = r.app_ws_off + slots * app_bytes;
+    if (r.ws_bytes > scratch_bytes)
+        return ck::fail(CK_ERR_UNSUPPORTED, "decode needs %zu bytes of scratch, %zu available",
+                        r.ws_bytes, scratch_bytes);
+    unsigned char* wsb = static_cast<unsigned char*>(scratch);
+    // The queue counter and status word must start at zero on every call.
+    CK_CUDA(cudaMemsetAsync(wsb, 0, kHeaderBytes, s));
+
+    Params p;
+    p.llr_in = llr_in;
+    p.llr_out = llr_out;
+    p.B = static_cast<uint32_t>(B);
+    p.n_in = n_in;
+    p.iters = iters;
+    p.valid = valid;
+    p.bits = k_bits > 0 ? bits : nullptr;
+    p.k_bits = k_bits;
+    p.N = plan->N;
+    p.m = plan->m;
+    p.L = plan->L;
+    p.Z = plan->qc ? plan->Z : 1;
+    p.mb = plan->qc ? plan->mb : 0;
+    p.nnzb = plan->qc ? plan->nnzb : 0;
+    p.divZ = plan->divZ;
+    p.layer = plan->d_layer;
+    p.eptr = plan->d_eptr;
+    p.blk = reinterpret_cast<const int2*>(plan->d_blk);
+    p.cols = plan->d_cols;
+    p.scale = scale;
+    p.offset = offset;
+    p.max_iterations = max_iterations;
+    p.early_stop = early_stop ? 1 : 0;
+    p.T = r.T;
+    p.G = r.G;
+    p.tables_bytes = r.tables_bytes;
+    p.group_bytes = r.group_bytes;
+    p.app_off = r.app_off;
+    p.r_off = r.r_off;
+    p.r_stride = r.r_stride;
+    p.bulk_load = (r.app_smem && (static_cast<uint32_t>(n_in) * 4u) % 16u == 0 &&
+                   reinterpret_cast<uintptr_t>(llr_in) % 16 == 0)
+                      ? 1
+                      : 0;
+    p.counter = reinterpret_cast<uint32_t*>(wsb);
+    p.status = reinterpret_cast<uint32_t*>(wsb + 4);
+    p.g_r = reinterpret_cast<float*>(wsb + r.r_ws_off);
+    p.g_app = reinterpret_cast<float*>(wsb + r.app_ws_off);
+    p.app_stride = r.app_stride;
+    r.kernel<<<r.grid, r.T * r.G, r.smem, s>>>(p);
+    return ck::cuda_check(cudaGetLastError(), "decoder launch");
+}

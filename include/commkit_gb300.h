@@ -227,6 +227,32 @@ int ck_ldpc_decode(const ck_ldpc_plan* plan, const float* llr_in, float* llr_out
  */
 int ck_ldpc_workspace_status(const void* workspace, void* stream);
 
+/* Capacity of the decoder's static scratch array (64 MiB per GPU). */
+#define CK_LDPC_STATIC_SCRATCH_BYTES (64u * 1024u * 1024u)
+
+/*
+ * ck_ldpc_decode without any allocation, for callers that may not allocate
+ * device memory while they decode (a real-time receive loop that cannot take
+ * cudaMalloc's synchronisation and latency mid-burst, an application that
+ * fixed its memory budget at start-up, a host runtime that owns all device
+ * memory).  No counterpart in the reference, whose launcher allocates its
+ * message buffer on every call.
+ * Arguments as ck_ldpc_decode, minus the workspace: the scratch is a
+ * CK_LDPC_STATIC_SCRATCH_BYTES array in the library's device memory, held
+ * on every GPU that loads it until the process exits.  The first call on a
+ * device looks up that array's address (cudaGetSymbolAddress, with the
+ * device current), so make it before any stream capture.  All calls on a
+ * device share the array: calls whose work overlaps on the GPU race, so
+ * serialise them on one stream.  The grid is limited to the frames whose
+ * state fits (any B works); a code whose one block of frames needs more
+ * scratch than the array holds returns CK_ERR_UNSUPPORTED.  Results are
+ * identical to ck_ldpc_decode's.
+ */
+int ck_ldpc_decode_static(const ck_ldpc_plan* plan, const float* llr_in, float* llr_out,
+                          int64_t B, int32_t n_in, int32_t rule, float scale, float offset,
+                          int32_t max_iterations, int32_t early_stop, int32_t* iters,
+                          uint8_t* valid, int8_t* bits, int32_t k_bits, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
