@@ -59,6 +59,8 @@ struct Params {
     int32_t N, m, L;
     int32_t Z, mb, nnzb;
     ck::FastDiv divZ;
+    int32_t Zp;          // QC: row slots per base row, Z rounded up to a multiple of 32
+    ck::FastDiv divZp;
     const int32_t* layer;  // QC: base rows per layer; CSR: rows per layer (L + 1)
     const int32_t* eptr;   // QC: circulants per base row (mb + 1); CSR: row_ptr (m + 1)
     const int2* blk;       // QC: (j Z, shift) per circulant
@@ -131,6 +133,75 @@ __device__ __forceinline__ void min_sum_row(float* __restrict__ a, const int deg
     w = (signs & 0x07ffffffu) | (idx << 27);
 }
 
+// The same update for a circulant row of exactly D edges: fully unrolled,
+// no per-slot predicates, the columns computed once and kept in registers
+// for the second pass.  A warp's rows all belong to one base row, so the
+// degree dispatch that picks D is uniform across the warp.
+template <int D>
+__device__ __forceinline__ void qc_row_fixed(float* __restrict__ a, const int2* __restrict__ blk,
+                                             const int32_t r, const int32_t Z, float& m1,
+                                             float& m2, uint32_t& w, const float scale,
+                                             const float offset) {
+    const uint32_t oidx = w >> 27;
+    const uint32_t osign = w;
+    const float om1 = m1, om2 = m2;
+    float q[D];
+    int c[D];
+    float min1 = CUDART_INF_F, min2 = CUDART_INF_F;
+    uint32_t idx = 31u;
+    uint32_t negs = 0u;
+#pragma unroll
+    for (int e = 0; e < D; ++e) {
+        const int2 b = blk[e];
+        int o = r + b.y;
+        o = o >= Z ? o - Z : o;
+        c[e] = b.x + o;
+        const float r_old =
+            flip_sign(static_cast<uint32_t>(e) == oidx ? om2 : om1, (osign >> e) & 1u);
+        const float qe = __fsub_rn(a[c[e]], r_old);
+        q[e] = qe;
+        negs |= (qe < 0.0f ? 1u : 0u) << e;
+        const float mag = fabsf(qe);
+        if (mag < min1) idx = static_cast<uint32_t>(e);
+        min2 = fminf(min2, fmaxf(min1, mag));
+        min1 = fminf(min1, mag);
+    }
+    const float n1 = fmaxf(__fsub_rn(__fmul_rn(scale, min1), offset), 0.0f);
+    const float n2 = fmaxf(__fsub_rn(__fmul_rn(scale, min2), offset), 0.0f);
+    const uint32_t signs = negs ^ ((__popc(negs) & 1u) ? 0xffffffffu : 0u);
+#pragma unroll
+    for (int e = 0; e < D; ++e) {
+        const float rn = flip_sign(static_cast<uint32_t>(e) == idx ? n2 : n1, (signs >> e) & 1u);
+        a[c[e]] = __fadd_rn(q[e], rn);
+    }
+    m1 = n1;
+    m2 = n2;
+    w = (signs & 0x07ffffffu) | (idx << 27);
+}
+
+// Degree dispatch of a circulant row (warp-uniform): D = 2..DMAX unrolled.
+template <int DMAX>
+__device__ __forceinline__ void qc_row(float* __restrict__ a, const int2* __restrict__ blk,
+                                       const int deg, const int32_t r, const int32_t Z, float& m1,
+                                       float& m2, uint32_t& w, const float scale,
+                                       const float offset) {
+    switch (deg) {
+#define CK_ROW_CASE(D) \
+    case D:            \
+        if (D <= DMAX) qc_row_fixed<(D <= DMAX ? D : 2)>(a, blk, r, Z, m1, m2, w, scale, offset); \
+        break;
+        CK_ROW_CASE(2) CK_ROW_CASE(3) CK_ROW_CASE(4) CK_ROW_CASE(5) CK_ROW_CASE(6)
+        CK_ROW_CASE(7) CK_ROW_CASE(8) CK_ROW_CASE(9) CK_ROW_CASE(10) CK_ROW_CASE(11)
+        CK_ROW_CASE(12) CK_ROW_CASE(13) CK_ROW_CASE(14) CK_ROW_CASE(15) CK_ROW_CASE(16)
+        CK_ROW_CASE(17) CK_ROW_CASE(18) CK_ROW_CASE(19) CK_ROW_CASE(20) CK_ROW_CASE(21)
+        CK_ROW_CASE(22) CK_ROW_CASE(23) CK_ROW_CASE(24) CK_ROW_CASE(25) CK_ROW_CASE(26)
+        CK_ROW_CASE(27)
+#undef CK_ROW_CASE
+        default:
+            break;
+    }
+}
+
 // Columns of row r of a circulant base row: j Z + (r + shift) mod Z.
 struct QcCols {
     const int2* blk;
@@ -178,6 +249,26 @@ struct RowOf<false> {
 template <bool QC>
 __device__ __forceinline__ bool syndrome_ok(const Params& p, const float* a, const int32_t* s_eptr,
                                             const int2* s_blk, int tid, int bar) {
+    if (QC) {
+        // Row slots of base rows padded to Zp, so a warp sees one base row.
+        const uint32_t slots = static_cast<uint32_t>(p.mb) * p.Zp;
+        for (uint32_t base = 0; base < slots; base += p.T) {
+            const uint32_t f = base + tid;
+            uint32_t parity = 0;
+            if (f < slots) {
+                const uint32_t b = p.divZp.div(f);
+                const int32_t r = static_cast<int32_t>(f - b * static_cast<uint32_t>(p.Zp));
+                if (r < p.Z) {
+                    const int32_t e0 = s_eptr[b];
+                    const int deg = s_eptr[b + 1] - e0;
+                    const QcCols col_of{s_blk + e0, r, p.Z};
+                    for (int e = 0; e < deg; ++e) parity ^= a[col_of(e)] < 0.0f ? 1u : 0u;
+                }
+            }
+            if (ck::group_any(static_cast<int>(parity), bar, p.T)) return false;
+        }
+        return true;
+    }
     for (int32_t base = 0; base < p.m; base += p.T) {
         const int32_t row = base + tid;
         uint32_t parity = 0;
@@ -279,9 +370,44 @@ __global__ void __launch_bounds__(DMAX <= 16 ? 1024 : 512)
         int32_t it = 0;
         bool ok = p.early_stop && syndrome_ok<QC>(p, a, s_eptr, s_blk, tid, bar);
         while (!ok && it < p.max_iterations) {
-            for (int32_t l = 0; l < p.L; ++l) {
-                const uint32_t row0 = QC ? static_cast<uint32_t>(s_layer[l]) * p.Z : s_layer[l];
-                const uint32_t row1 = QC ? static_cast<uint32_t>(s_layer[l + 1]) * p.Z : s_layer[l + 1];
+            for (int32_t l = 0; l < p.L && QC; ++l) {
+                const uint32_t b0 = static_cast<uint32_t>(s_layer[l]);
+                const uint32_t slots = (static_cast<uint32_t>(s_layer[l + 1]) - b0) * p.Zp;
+                for (uint32_t f = tid; f < slots; f += p.T) {
+                    const uint32_t bi = p.divZp.div(f);
+                    const int32_t r = static_cast<int32_t>(f - bi * static_cast<uint32_t>(p.Zp));
+                    if (r >= p.Z) continue;  // padding lanes when Z % 32 != 0
+                    const uint32_t b = b0 + bi;
+                    const uint32_t row = b * static_cast<uint32_t>(p.Z) + static_cast<uint32_t>(r);
+                    const int32_t e0 = s_eptr[b];
+                    const int deg = s_eptr[b + 1] - e0;
+                    float m1, m2;
+                    uint32_t w;
+                    if (R_SMEM) {
+                        m1 = r1[row];
+                        m2 = r2[row];
+                        w = rw[row];
+                    } else {
+                        m1 = __ldcg(r1 + row);
+                        m2 = __ldcg(r2 + row);
+                        w = __ldcg(rw + row);
+                    }
+                    qc_row<DMAX>(a, s_blk + e0, deg, r, p.Z, m1, m2, w, p.scale, p.offset);
+                    if (R_SMEM) {
+                        r1[row] = m1;
+                        r2[row] = m2;
+                        rw[row] = w;
+                    } else {
+                        __stcg(r1 + row, m1);
+                        __stcg(r2 + row, m2);
+                        __stcg(rw + row, w);
+                    }
+                }
+                group_sync(bar, p.T);
+            }
+            for (int32_t l = 0; l < p.L && !QC; ++l) {
+                const uint32_t row0 = s_layer[l];
+                const uint32_t row1 = s_layer[l + 1];
                 for (uint32_t row = row0 + tid; row < row1; row += p.T) {
                     int deg;
                     const auto col_of = RowOf<QC>::get(p, s_eptr, s_blk, row, deg);
@@ -340,7 +466,9 @@ KernelFn pick_placement(bool app_smem, bool r_smem) {
 
 template <bool QC>
 KernelFn pick_degree(int dmax, bool app_smem, bool r_smem) {
-    if (dmax <= 8) return pick_placement<QC, 8>(app_smem, r_smem);
+    if constexpr (!QC) {
+        if (dmax <= 8) return pick_placement<QC, 8>(app_smem, r_smem);
+    }
     if (dmax <= 16) return pick_placement<QC, 16>(app_smem, r_smem);
     return pick_placement<QC, 27>(app_smem, r_smem);
 }
@@ -540,6 +668,8 @@ extern "C" int ck_ldpc_decode(const ck_ldpc_plan* plan, const float* llr_in, flo
     p.mb = plan->qc ? plan->mb : 0;
     p.nnzb = plan->qc ? plan->nnzb : 0;
     p.divZ = plan->divZ;
+    p.Zp = plan->qc ? (plan->Z + 31) / 32 * 32 : 32;
+    p.divZp = ck::FastDiv::make(static_cast<uint32_t>(p.Zp));
     p.layer = plan->d_layer;
     p.eptr = plan->d_eptr;
     p.blk = reinterpret_cast<const int2*>(plan->d_blk);
@@ -661,6 +791,8 @@ int ck::ldpc_decode_in_scratch(const ck_ldpc_plan* plan, const float* llr_in, fl
     p.mb = plan->qc ? plan->mb : 0;
     p.nnzb = plan->qc ? plan->nnzb : 0;
     p.divZ = plan->divZ;
+    p.Zp = plan->qc ? (plan->Z + 31) / 32 * 32 : 32;
+    p.divZp = ck::FastDiv::make(static_cast<uint32_t>(p.Zp));
     p.layer = plan->d_layer;
     p.eptr = plan->d_eptr;
     p.blk = reinterpret_cast<const int2*>(plan->d_blk);
