@@ -59,8 +59,8 @@ struct Params {
     int32_t N, m, L;
     int32_t Z, mb, nnzb;
     ck::FastDiv divZ;
-    int32_t Zp;          // QC: row slots per base row, Z rounded up to a multiple of 32
-    ck::FastDiv divZp;
+    int32_t Zp;       // QC: row slots per base row, Z rounded up to a multiple of 32
+    int32_t q_bstep;  // QC: base-row stride of a thread (T / Zp when T >= Zp, else 1)
     const int32_t* layer;  // QC: base rows per layer; CSR: rows per layer (L + 1)
     const int32_t* eptr;   // QC: circulants per base row (mb + 1); CSR: row_ptr (m + 1)
     const int2* blk;       // QC: (j Z, shift) per circulant
@@ -72,18 +72,29 @@ struct Params {
     // launch
     int32_t T;  // threads per frame group
     int32_t G;  // frame groups per block
-    uint32_t tables_bytes, group_bytes, app_off, r_off, r_stride;
+    uint32_t tables_bytes, group_bytes, app_off, r_off, r_stride, gblk_off;
     int32_t bulk_load;  // 1: stage the LLRs with one bulk copy
     // workspace
     uint32_t* counter;
     uint32_t* status;
-    float* g_r;    // R-state slots in device memory (3 r_stride words per slot)
+    uint32_t* g_r;  // R-state slots in device memory (3 arrays of r_stride words per slot)
     float* g_app;  // posterior slots in device memory (N per slot)
     int32_t app_stride;
 };
 
 __device__ __forceinline__ float flip_sign(float v, uint32_t bit) {
     return __uint_as_float(__float_as_uint(v) ^ (bit << 31));
+}
+
+// Shared-memory load and store at a 32-bit shared address (volatile: their
+// order against each other and the barriers stays as written).
+__device__ __forceinline__ float ld_shared_f32(uint32_t addr) {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
+    return v;
+}
+__device__ __forceinline__ void st_shared_f32(uint32_t addr, float v) {
+    asm volatile("st.shared.f32 [%0], %1;" ::"r"(addr), "f"(v));
 }
 
 // One check row, min-sum: reads the row's compressed state (m1, m2, w),
@@ -133,47 +144,63 @@ __device__ __forceinline__ void min_sum_row(float* __restrict__ a, const int deg
     w = (signs & 0x07ffffffu) | (idx << 27);
 }
 
-// The same update for a circulant row of exactly D edges: fully unrolled,
-// no per-slot predicates, the columns computed once and kept in registers
-// for the second pass.  A warp's rows all belong to one base row, so the
-// degree dispatch that picks D is uniform across the warp.
+// The same update for a circulant row of exactly D edges, shaped for the
+// ALU pipe, which bounds this kernel: fully unrolled, columns computed once
+// and kept in registers, and
+//  * the sign bits of Q taken from the float sign (no -0 ever reaches the
+//    posterior: frames are loaded as x + 0, and from such values Q = APP - R
+//    and APP = Q + R_new cannot produce -0 either, so "sign bit set" is
+//    "Q < 0"), one funnel shift per edge;
+//  * the new signs applied with one multiply by the parity sign (exact) and
+//    one bitwise or;
+//  * no running argmin: an edge takes min2' when |Q| equals min1 (a tie
+//    means min2 == min1, so every tied edge gets the same value), and the
+//    stored argmin is the first such edge, found in the second pass.
+// The compressed state keeps the sign of edge e at bit D - 1 - e here.
 template <int D>
-__device__ __forceinline__ void qc_row_fixed(float* __restrict__ a, const int2* __restrict__ blk,
-                                             const int32_t r, const int32_t Z, float& m1,
-                                             float& m2, uint32_t& w, const float scale,
-                                             const float offset) {
+__device__ __forceinline__ void qc_row_fixed(const int2* __restrict__ gblk, const uint32_t r4,
+                                             const uint32_t Z4, float& m1, float& m2, uint32_t& w,
+                                             const float scale, const float offset) {
     const uint32_t oidx = w >> 27;
     const uint32_t osign = w;
     const float om1 = m1, om2 = m2;
     float q[D];
-    int c[D];
+    uint32_t c[D];
     float min1 = CUDART_INF_F, min2 = CUDART_INF_F;
-    uint32_t idx = 31u;
     uint32_t negs = 0u;
 #pragma unroll
     for (int e = 0; e < D; ++e) {
-        const int2 b = blk[e];
-        int o = r + b.y;
-        o = o >= Z ? o - Z : o;
-        c[e] = b.x + o;
-        const float r_old =
-            flip_sign(static_cast<uint32_t>(e) == oidx ? om2 : om1, (osign >> e) & 1u);
-        const float qe = __fsub_rn(a[c[e]], r_old);
+        // gblk[e] = (shared address of the circulant's row-0 column, address
+        // of the block's end): row r's column, wrapped once at the end.
+        const int2 b = gblk[e];
+        uint32_t ce = r4 + static_cast<uint32_t>(b.x);
+        ce = ce >= static_cast<uint32_t>(b.y) ? ce - Z4 : ce;
+        c[e] = ce;
+        const float mag_old = static_cast<uint32_t>(e) == oidx ? om2 : om1;
+        const float r_old = __uint_as_float(__float_as_uint(mag_old) ^
+                                            ((osign << (32 - D + e)) & 0x80000000u));
+        const float qe = __fsub_rn(ld_shared_f32(ce), r_old);
         q[e] = qe;
-        negs |= (qe < 0.0f ? 1u : 0u) << e;
+        negs = __funnelshift_l(__float_as_uint(qe), negs, 1);
         const float mag = fabsf(qe);
-        if (mag < min1) idx = static_cast<uint32_t>(e);
         min2 = fminf(min2, fmaxf(min1, mag));
         min1 = fminf(min1, mag);
     }
     const float n1 = fmaxf(__fsub_rn(__fmul_rn(scale, min1), offset), 0.0f);
     const float n2 = fmaxf(__fsub_rn(__fmul_rn(scale, min2), offset), 0.0f);
-    const uint32_t signs = negs ^ ((__popc(negs) & 1u) ? 0xffffffffu : 0u);
+    const bool odd = __popc(negs) & 1u;
+    const float psign = odd ? -1.0f : 1.0f;
+    uint32_t idx = 31u;
 #pragma unroll
-    for (int e = 0; e < D; ++e) {
-        const float rn = flip_sign(static_cast<uint32_t>(e) == idx ? n2 : n1, (signs >> e) & 1u);
-        a[c[e]] = __fadd_rn(q[e], rn);
+    for (int e = D - 1; e >= 0; --e) {
+        const bool at_min = fabsf(q[e]) == min1;
+        if (at_min) idx = static_cast<uint32_t>(e);
+        const float mag = at_min ? n2 : n1;
+        const float t = __fmul_rn(q[e], psign);
+        const float rn = __uint_as_float(__float_as_uint(mag) | (__float_as_uint(t) & 0x80000000u));
+        st_shared_f32(c[e], __fadd_rn(q[e], rn));
     }
+    const uint32_t signs = negs ^ (odd ? ((1u << D) - 1u) : 0u);
     m1 = n1;
     m2 = n2;
     w = (signs & 0x07ffffffu) | (idx << 27);
@@ -181,14 +208,13 @@ __device__ __forceinline__ void qc_row_fixed(float* __restrict__ a, const int2* 
 
 // Degree dispatch of a circulant row (warp-uniform): D = 2..DMAX unrolled.
 template <int DMAX>
-__device__ __forceinline__ void qc_row(float* __restrict__ a, const int2* __restrict__ blk,
-                                       const int deg, const int32_t r, const int32_t Z, float& m1,
-                                       float& m2, uint32_t& w, const float scale,
-                                       const float offset) {
+__device__ __forceinline__ void qc_row(const int2* __restrict__ gblk, const int deg,
+                                       const uint32_t r4, const uint32_t Z4, float& m1, float& m2,
+                                       uint32_t& w, const float scale, const float offset) {
     switch (deg) {
 #define CK_ROW_CASE(D) \
     case D:            \
-        if (D <= DMAX) qc_row_fixed<(D <= DMAX ? D : 2)>(a, blk, r, Z, m1, m2, w, scale, offset); \
+        if (D <= DMAX) qc_row_fixed<(D <= DMAX ? D : 2)>(gblk, r4, Z4, m1, m2, w, scale, offset); \
         break;
         CK_ROW_CASE(2) CK_ROW_CASE(3) CK_ROW_CASE(4) CK_ROW_CASE(5) CK_ROW_CASE(6)
         CK_ROW_CASE(7) CK_ROW_CASE(8) CK_ROW_CASE(9) CK_ROW_CASE(10) CK_ROW_CASE(11)
@@ -202,15 +228,15 @@ __device__ __forceinline__ void qc_row(float* __restrict__ a, const int2* __rest
     }
 }
 
-// Columns of row r of a circulant base row: j Z + (r + shift) mod Z.
+// Columns of row r of a circulant base row: j Z + (r + shift) mod Z, from
+// the table entry (j Z + shift, (j + 1) Z).
 struct QcCols {
     const int2* blk;
     int32_t r, Z;
     __device__ __forceinline__ int operator()(int e) const {
         const int2 b = blk[e];
-        int o = r + b.y;
-        o = o >= Z ? o - Z : o;
-        return b.x + o;
+        const int c = r + b.x;
+        return c >= b.y ? c - Z : c;
     }
 };
 
@@ -248,24 +274,24 @@ struct RowOf<false> {
 // chunks of T; the first chunk with an unsatisfied row ends the test.
 template <bool QC>
 __device__ __forceinline__ bool syndrome_ok(const Params& p, const float* a, const int32_t* s_eptr,
-                                            const int2* s_blk, int tid, int bar) {
+                                            const int2* s_blk, int tid, int bar, int32_t qr0,
+                                            int32_t qb0) {
     if (QC) {
-        // Row slots of base rows padded to Zp, so a warp sees one base row.
-        const uint32_t slots = static_cast<uint32_t>(p.mb) * p.Zp;
-        for (uint32_t base = 0; base < slots; base += p.T) {
-            const uint32_t f = base + tid;
-            uint32_t parity = 0;
-            if (f < slots) {
-                const uint32_t b = p.divZp.div(f);
-                const int32_t r = static_cast<int32_t>(f - b * static_cast<uint32_t>(p.Zp));
-                if (r < p.Z) {
+        // Rounds of T row slots, each covering whole warps of one base row
+        // (the thread's rows as in the layer loop); an OR per round.
+        const int32_t rounds = (p.mb + p.q_bstep - 1) / p.q_bstep;
+        for (int32_t k = 0; k < rounds; ++k) {
+            const int32_t b = k * p.q_bstep + qb0;
+            for (int32_t r = qr0; r - qr0 < p.Zp; r += p.T) {
+                uint32_t parity = 0;
+                if (b < p.mb && r < p.Z) {
                     const int32_t e0 = s_eptr[b];
                     const int deg = s_eptr[b + 1] - e0;
                     const QcCols col_of{s_blk + e0, r, p.Z};
                     for (int e = 0; e < deg; ++e) parity ^= a[col_of(e)] < 0.0f ? 1u : 0u;
                 }
+                if (ck::group_any(static_cast<int>(parity), bar, p.T)) return false;
             }
-            if (ck::group_any(static_cast<int>(parity), bar, p.T)) return false;
         }
         return true;
     }
@@ -282,8 +308,13 @@ __device__ __forceinline__ bool syndrome_ok(const Params& p, const float* a, con
     return true;
 }
 
+// Threads per block the kernels are built for (registers scale inversely).
+__host__ __device__ constexpr int max_block_threads(bool qc, int dmax) {
+    return dmax > 16 ? 512 : (qc ? 768 : 1024);
+}
+
 template <bool QC, int DMAX, bool APP_SMEM, bool R_SMEM>
-__global__ void __launch_bounds__(DMAX <= 16 ? 1024 : 512)
+__global__ void __launch_bounds__(max_block_threads(QC, DMAX))
     ldpc_decode_kernel(const __grid_constant__ Params p) {
     extern __shared__ __align__(128) unsigned char smem[];
     using ck::group_any;
@@ -303,28 +334,41 @@ __global__ void __launch_bounds__(DMAX <= 16 ? 1024 : 512)
     const int g = threadIdx.x / p.T;
     const int tid = threadIdx.x - g * p.T;
     const int bar = g + 1;
+    // Circulant rows of this thread: row qr0 (+ T, + 2T, ... when T < Zp) of
+    // base rows qb0, qb0 + q_bstep, ...  Zp and T are multiples of 32 and one
+    // divides the other, so a warp's lanes always share their base row.
+    const int32_t qr0 = QC ? (p.T >= p.Zp ? tid % p.Zp : tid) : 0;
+    const int32_t qb0 = QC ? (p.T >= p.Zp ? tid / p.Zp : 0) : 0;
     const uint32_t slot = blockIdx.x * static_cast<uint32_t>(p.G) + static_cast<uint32_t>(g);
     unsigned char* gbase = smem + p.tables_bytes + static_cast<uint32_t>(g) * p.group_bytes;
     uint64_t* mbar = reinterpret_cast<uint64_t*>(gbase);
     volatile uint32_t* s_frame = reinterpret_cast<volatile uint32_t*>(gbase + 8);
     float* a = APP_SMEM ? reinterpret_cast<float*>(gbase + p.app_off)
                         : p.g_app + static_cast<size_t>(slot) * p.app_stride;
-    float* r1;
-    float* r2;
-    uint32_t* rw;
-    if (R_SMEM) {
-        r1 = reinterpret_cast<float*>(gbase + p.r_off);
-    } else {
-        r1 = p.g_r + static_cast<size_t>(slot) * 3 * p.r_stride;
-    }
-    r2 = r1 + p.r_stride;
-    rw = reinterpret_cast<uint32_t*>(r2 + p.r_stride);
+    // Check-message state of a row: (min1', min2', signs and argmin).  In
+    // shared memory one 16-byte record per row (one vector access); in device
+    // memory three arrays of 4 bytes, so the resident frames' state (code C:
+    // 304 frames x 17664 rows x 12 B = 64 MB) stays in L2.
+    uint4* rs = reinterpret_cast<uint4*>(gbase + p.r_off);
+    uint32_t* g1 = p.g_r + static_cast<size_t>(slot) * 3 * p.r_stride;
+    uint32_t* g2 = g1 + p.r_stride;
+    uint32_t* g3 = g2 + p.r_stride;
+    // This group's copy of the circulant table as shared addresses into `a`.
+    int2* gblk = reinterpret_cast<int2*>(gbase + p.gblk_off);
 
     if (tid == 0) {
         ck::mbar_init(mbar, 1);
         ck::fence_mbar_init();
     }
     __syncthreads();
+    if (QC) {
+        const uint32_t a_addr = ck::smem_addr(a);
+        for (int i = tid; i < p.nnzb; i += p.T)
+            gblk[i] = make_int2(static_cast<int>(a_addr + 4u * static_cast<uint32_t>(s_blk[i].x)),
+                                static_cast<int>(a_addr + 4u * static_cast<uint32_t>(s_blk[i].y)));
+    }
+    const uint32_t r4 = 4u * static_cast<uint32_t>(qr0);
+    const uint32_t Z4 = 4u * static_cast<uint32_t>(p.Z);
 
     uint32_t phase = 0;
     for (;;) {
@@ -345,8 +389,12 @@ __global__ void __launch_bounds__(DMAX <= 16 ? 1024 : 512)
             for (int i = p.n_in + tid; i < p.N; i += p.T) a[i] = 0.0f;
             loaded = ck::mbar_wait(mbar, phase);
             phase ^= 1u;
+            // x + 0 turns -0 into +0 and keeps every other value: the decoder
+            // then never meets -0 (see qc_row_fixed).
+            if (loaded)
+                for (int i = tid; i < p.n_in; i += p.T) a[i] = __fadd_rn(a[i], 0.0f);
         } else {
-            for (int i = tid; i < p.n_in; i += p.T) a[i] = __ldcs(src + i);
+            for (int i = tid; i < p.n_in; i += p.T) a[i] = __fadd_rn(__ldcs(src + i), 0.0f);
             for (int i = p.n_in + tid; i < p.N; i += p.T) a[i] = 0.0f;
         }
         if (group_any(loaded ? 0 : 1, bar, p.T)) {
@@ -361,46 +409,42 @@ __global__ void __launch_bounds__(DMAX <= 16 ? 1024 : 512)
             return;
         }
         for (int i = tid; i < p.m; i += p.T) {
-            r1[i] = 0.0f;
-            r2[i] = 0.0f;
-            rw[i] = 0u;
+            if (R_SMEM) {
+                rs[i] = make_uint4(0u, 0u, 0u, 0u);
+            } else {
+                g1[i] = 0u;
+                g2[i] = 0u;
+                g3[i] = 0u;
+            }
         }
         group_sync(bar, p.T);
 
         int32_t it = 0;
-        bool ok = p.early_stop && syndrome_ok<QC>(p, a, s_eptr, s_blk, tid, bar);
+        bool ok = p.early_stop && syndrome_ok<QC>(p, a, s_eptr, s_blk, tid, bar, qr0, qb0);
         while (!ok && it < p.max_iterations) {
             for (int32_t l = 0; l < p.L && QC; ++l) {
-                const uint32_t b0 = static_cast<uint32_t>(s_layer[l]);
-                const uint32_t slots = (static_cast<uint32_t>(s_layer[l + 1]) - b0) * p.Zp;
-                for (uint32_t f = tid; f < slots; f += p.T) {
-                    const uint32_t bi = p.divZp.div(f);
-                    const int32_t r = static_cast<int32_t>(f - bi * static_cast<uint32_t>(p.Zp));
-                    if (r >= p.Z) continue;  // padding lanes when Z % 32 != 0
-                    const uint32_t b = b0 + bi;
-                    const uint32_t row = b * static_cast<uint32_t>(p.Z) + static_cast<uint32_t>(r);
+                const int32_t b1 = s_layer[l + 1];
+                for (int32_t b = s_layer[l] + qb0; b < b1; b += p.q_bstep) {
                     const int32_t e0 = s_eptr[b];
                     const int deg = s_eptr[b + 1] - e0;
-                    float m1, m2;
-                    uint32_t w;
-                    if (R_SMEM) {
-                        m1 = r1[row];
-                        m2 = r2[row];
-                        w = rw[row];
-                    } else {
-                        m1 = __ldcg(r1 + row);
-                        m2 = __ldcg(r2 + row);
-                        w = __ldcg(rw + row);
-                    }
-                    qc_row<DMAX>(a, s_blk + e0, deg, r, p.Z, m1, m2, w, p.scale, p.offset);
-                    if (R_SMEM) {
-                        r1[row] = m1;
-                        r2[row] = m2;
-                        rw[row] = w;
-                    } else {
-                        __stcg(r1 + row, m1);
-                        __stcg(r2 + row, m2);
-                        __stcg(rw + row, w);
+                    for (int32_t r = qr0; r - qr0 < p.Zp; r += p.T) {
+                        if (r >= p.Z) continue;  // padding lanes when Z % 32 != 0
+                        const uint32_t row = static_cast<uint32_t>(b) * static_cast<uint32_t>(p.Z) +
+                                             static_cast<uint32_t>(r);
+                        const uint4 st = R_SMEM ? rs[row]
+                                                : make_uint4(__ldcg(g1 + row), __ldcg(g2 + row),
+                                                             __ldcg(g3 + row), 0u);
+                        float m1 = __uint_as_float(st.x), m2 = __uint_as_float(st.y);
+                        uint32_t w = st.z;
+                        qc_row<DMAX>(gblk + e0, deg, r4 + 4u * static_cast<uint32_t>(r - qr0), Z4, m1,
+                                     m2, w, p.scale, p.offset);
+                        if (R_SMEM) {
+                            rs[row] = make_uint4(__float_as_uint(m1), __float_as_uint(m2), w, 0u);
+                        } else {
+                            __stcg(g1 + row, __float_as_uint(m1));
+                            __stcg(g2 + row, __float_as_uint(m2));
+                            __stcg(g3 + row, w);
+                        }
                     }
                 }
                 group_sync(bar, p.T);
@@ -411,34 +455,26 @@ __global__ void __launch_bounds__(DMAX <= 16 ? 1024 : 512)
                 for (uint32_t row = row0 + tid; row < row1; row += p.T) {
                     int deg;
                     const auto col_of = RowOf<QC>::get(p, s_eptr, s_blk, row, deg);
-                    float m1, m2;
-                    uint32_t w;
-                    if (R_SMEM) {
-                        m1 = r1[row];
-                        m2 = r2[row];
-                        w = rw[row];
-                    } else {
-                        m1 = __ldcg(r1 + row);
-                        m2 = __ldcg(r2 + row);
-                        w = __ldcg(rw + row);
-                    }
+                    const uint4 st = R_SMEM ? rs[row]
+                                            : make_uint4(__ldcg(g1 + row), __ldcg(g2 + row),
+                                                         __ldcg(g3 + row), 0u);
+                    float m1 = __uint_as_float(st.x), m2 = __uint_as_float(st.y);
+                    uint32_t w = st.z;
                     min_sum_row<DMAX>(a, deg, col_of, m1, m2, w, p.scale, p.offset);
                     if (R_SMEM) {
-                        r1[row] = m1;
-                        r2[row] = m2;
-                        rw[row] = w;
+                        rs[row] = make_uint4(__float_as_uint(m1), __float_as_uint(m2), w, 0u);
                     } else {
-                        __stcg(r1 + row, m1);
-                        __stcg(r2 + row, m2);
-                        __stcg(rw + row, w);
+                        __stcg(g1 + row, __float_as_uint(m1));
+                        __stcg(g2 + row, __float_as_uint(m2));
+                        __stcg(g3 + row, w);
                     }
                 }
                 group_sync(bar, p.T);
             }
             ++it;
-            if (p.early_stop) ok = syndrome_ok<QC>(p, a, s_eptr, s_blk, tid, bar);
+            if (p.early_stop) ok = syndrome_ok<QC>(p, a, s_eptr, s_blk, tid, bar, qr0, qb0);
         }
-        if (!p.early_stop) ok = syndrome_ok<QC>(p, a, s_eptr, s_blk, tid, bar);
+        if (!p.early_stop) ok = syndrome_ok<QC>(p, a, s_eptr, s_blk, tid, bar, qr0, qb0);
 
         float* dst = p.llr_out + static_cast<size_t>(f) * p.n_in;
         for (int i = tid; i < p.n_in; i += p.T) __stcs(dst + i, a[i]);
@@ -461,7 +497,11 @@ template <bool QC, int DMAX>
 KernelFn pick_placement(bool app_smem, bool r_smem) {
     if (app_smem && r_smem) return ldpc_decode_kernel<QC, DMAX, true, true>;
     if (app_smem) return ldpc_decode_kernel<QC, DMAX, true, false>;
-    return ldpc_decode_kernel<QC, DMAX, false, false>;
+    if constexpr (QC) {
+        return nullptr;  // circulant rows address the posterior in shared memory
+    } else {
+        return ldpc_decode_kernel<QC, DMAX, false, false>;
+    }
 }
 
 template <bool QC>
@@ -479,7 +519,7 @@ struct Resolved {
     KernelFn kernel;
     int32_t T, G;
     bool app_smem, r_smem;
-    uint32_t tables_bytes, group_bytes, app_off, r_off, r_stride, smem;
+    uint32_t tables_bytes, group_bytes, gblk_off, app_off, r_off, r_stride, smem;
     int32_t app_stride;
     int grid;
     size_t ws_bytes, r_ws_off, app_ws_off;
@@ -506,29 +546,50 @@ int resolve(const ck_ldpc_plan* plan, int64_t B, Resolved* r) {
     const uint32_t ctrl = 128;
     const uint32_t app_bytes = align_up(static_cast<uint32_t>(plan->N) * 4, 128);
     const uint32_t r_stride = align_up(static_cast<uint32_t>(plan->m), 32);
-    const uint32_t r_bytes = 3 * r_stride * 4;
+    const uint32_t r_bytes = r_stride * 16;       // in shared memory
+    const uint32_t r_bytes_dev = r_stride * 12;   // in device memory
+    // Per group: its copy of the circulant table with shared addresses.
+    const uint32_t gblk_bytes = plan->qc ? align_up(static_cast<uint32_t>(plan->nnzb) * 8, 128) : 0;
     const uint32_t budget = static_cast<uint32_t>(optin) > tables ? optin - tables : 0;
 
-    bool app_smem = ctrl + app_bytes <= budget;
+    bool app_smem = ctrl + gblk_bytes + app_bytes <= budget;
+    if (plan->qc && !app_smem)
+        return ck::fail(CK_ERR_UNSUPPORTED,
+                        "quasi-cyclic code of N = %d: its posterior (%u bytes) does not fit in shared "
+                        "memory",
+                        plan->N, app_bytes);
     bool r_smem;
     const int32_t place = plan->launch.placement;
     if (!app_smem || place == CK_LDPC_PLACE_GLOBAL) {
         r_smem = false;
     } else if (place == CK_LDPC_PLACE_SHARED) {
-        r_smem = ctrl + app_bytes + r_bytes <= budget;
+        r_smem = ctrl + gblk_bytes + app_bytes + r_bytes <= budget;
     } else {
         // Auto: beside the LLRs when two frames still fit per block budget.
-        r_smem = 2 * (ctrl + app_bytes + r_bytes) <= budget;
+        r_smem = 2 * (ctrl + gblk_bytes + app_bytes + r_bytes) <= budget;
     }
-    uint32_t group = ctrl + (app_smem ? app_bytes : 0) + (r_smem ? r_bytes : 0);
+    uint32_t group = ctrl + gblk_bytes + (app_smem ? app_bytes : 0) + (r_smem ? r_bytes : 0);
 
     int32_t T = plan->launch.threads_per_frame;
+    const int32_t Zp = plan->qc ? (plan->Z + 31) / 32 * 32 : 0;
     if (T == 0) {
-        const int32_t avg = std::max(1, plan->m / plan->L);
-        T = 32;
-        while (T < 512 && T < avg / 2) T *= 2;
+        if (plan->qc) {
+            // One base row's rows per round: the padded lifting, halved while
+            // above 512 threads and still a multiple of 32.
+            T = Zp;
+            while (T > 512 && T % 64 == 0) T /= 2;
+        } else {
+            const int32_t avg = std::max(1, plan->m / plan->L);
+            T = 32;
+            while (T < 512 && T < avg / 2) T *= 2;
+        }
     }
-    const int32_t max_threads = plan->max_deg <= 16 ? 1024 : 512;
+    if (plan->qc && T % Zp != 0 && Zp % T != 0)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT,
+                        "threads_per_frame %d must divide or be a multiple of %d (the lifting %d "
+                        "rounded up to whole warps)",
+                        T, Zp, plan->Z);
+    const int32_t max_threads = max_block_threads(plan->qc, plan->max_deg <= 16 ? 16 : 27);
     if (T > max_threads)
         return ck::fail(CK_ERR_INVALID_ARGUMENT,
                         "threads_per_frame %d above %d for row degree %d", T, max_threads,
@@ -541,23 +602,41 @@ int resolve(const ck_ldpc_plan* plan, int64_t B, Resolved* r) {
     if (gmax < 1)
         return ck::fail(CK_ERR_UNSUPPORTED, "a frame needs %u bytes of shared memory, %u available",
                         group, budget);
-    if (G == 0) G = std::max(1, std::min(gmax, 512 / T));
+    KernelFn kernel = plan->qc ? pick_degree<true>(plan->max_deg, app_smem, r_smem)
+                               : pick_degree<false>(plan->max_deg, app_smem, r_smem);
+    if (G == 0) {
+        // The most resident frames per SM (registers, shared memory, threads),
+        // the smaller block on a tie.
+        CK_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void*>(kernel),
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+        int best = 0;
+        for (int32_t g = 1; g <= gmax; ++g) {
+            int per_sm = 0;
+            CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &per_sm, reinterpret_cast<const void*>(kernel), T * g, tables + g * group));
+            if (per_sm * g > best) {
+                best = per_sm * g;
+                G = g;
+            }
+        }
+        if (G == 0) G = 1;
+    }
     if (G > gmax)
         return ck::fail(CK_ERR_INVALID_ARGUMENT,
                         "frames_per_block %d above the %d that fit (threads, shared memory, "
                         "barriers)",
                         G, gmax);
 
-    r->kernel = plan->qc ? pick_degree<true>(plan->max_deg, app_smem, r_smem)
-                         : pick_degree<false>(plan->max_deg, app_smem, r_smem);
+    r->kernel = kernel;
     r->T = T;
     r->G = G;
     r->app_smem = app_smem;
     r->r_smem = r_smem;
     r->tables_bytes = tables;
     r->group_bytes = group;
-    r->app_off = ctrl;
-    r->r_off = ctrl + (app_smem ? app_bytes : 0);
+    r->gblk_off = ctrl;
+    r->app_off = ctrl + gblk_bytes;
+    r->r_off = ctrl + gblk_bytes + (app_smem ? app_bytes : 0);
     r->r_stride = r_stride;
     r->smem = tables + static_cast<uint32_t>(G) * group;
     r->app_stride = static_cast<int32_t>(app_bytes / 4);
@@ -577,7 +656,7 @@ int resolve(const ck_ldpc_plan* plan, int64_t B, Resolved* r) {
     r->grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(need, int64_t(sms) * per_sm)));
     const size_t slots = static_cast<size_t>(r->grid) * G;
     r->r_ws_off = kHeaderBytes;
-    const size_t r_ws = r_smem ? 0 : slots * r_bytes;
+    const size_t r_ws = r_smem ? 0 : slots * r_bytes_dev;
     r->app_ws_off = kHeaderBytes + ((r_ws + 255) / 256) * 256;
     const size_t app_ws = app_smem ? 0 : slots * app_bytes;
     r->ws_bytes = r->app_ws_off + app_ws;
@@ -669,7 +748,7 @@ extern "C" int ck_ldpc_decode(const ck_ldpc_plan* plan, const float* llr_in, flo
     p.nnzb = plan->qc ? plan->nnzb : 0;
     p.divZ = plan->divZ;
     p.Zp = plan->qc ? (plan->Z + 31) / 32 * 32 : 32;
-    p.divZp = ck::FastDiv::make(static_cast<uint32_t>(p.Zp));
+    p.q_bstep = (plan->qc && r.T >= p.Zp) ? r.T / p.Zp : 1;
     p.layer = plan->d_layer;
     p.eptr = plan->d_eptr;
     p.blk = reinterpret_cast<const int2*>(plan->d_blk);
@@ -682,6 +761,7 @@ extern "C" int ck_ldpc_decode(const ck_ldpc_plan* plan, const float* llr_in, flo
     p.G = r.G;
     p.tables_bytes = r.tables_bytes;
     p.group_bytes = r.group_bytes;
+    p.gblk_off = r.gblk_off;
     p.app_off = r.app_off;
     p.r_off = r.r_off;
     p.r_stride = r.r_stride;
@@ -691,7 +771,7 @@ extern "C" int ck_ldpc_decode(const ck_ldpc_plan* plan, const float* llr_in, flo
                       : 0;
     p.counter = reinterpret_cast<uint32_t*>(wsb);
     p.status = reinterpret_cast<uint32_t*>(wsb + 4);
-    p.g_r = reinterpret_cast<float*>(wsb + r.r_ws_off);
+    p.g_r = reinterpret_cast<uint32_t*>(wsb + r.r_ws_off);
     p.g_app = reinterpret_cast<float*>(wsb + r.app_ws_off);
     p.app_stride = r.app_stride;
     if (status == CK_OK) {
@@ -750,7 +830,7 @@ int ck::ldpc_decode_in_scratch(const ck_ldpc_plan* plan, const float* llr_in, fl
     Resolved r;
     CK_TRY(resolve(plan, B, &r));
     // Bytes of device-memory state per frame slot (the header is shared).
-    const size_t r_bytes = r.r_smem ? 0 : static_cast<size_t>(3) * r.r_stride * 4;
+    const size_t r_bytes = r.r_smem ? 0 : static_cast<size_t>(r.r_stride) * 12;
     const size_t app_bytes = r.app_smem ? 0 : static_cast<size_t>(r.app_stride) * 4;
     const size_t per_slot = r_bytes + app_bytes;
     if (per_slot > 0) {
@@ -792,7 +872,7 @@ int ck::ldpc_decode_in_scratch(const ck_ldpc_plan* plan, const float* llr_in, fl
     p.nnzb = plan->qc ? plan->nnzb : 0;
     p.divZ = plan->divZ;
     p.Zp = plan->qc ? (plan->Z + 31) / 32 * 32 : 32;
-    p.divZp = ck::FastDiv::make(static_cast<uint32_t>(p.Zp));
+    p.q_bstep = (plan->qc && r.T >= p.Zp) ? r.T / p.Zp : 1;
     p.layer = plan->d_layer;
     p.eptr = plan->d_eptr;
     p.blk = reinterpret_cast<const int2*>(plan->d_blk);
@@ -805,6 +885,7 @@ int ck::ldpc_decode_in_scratch(const ck_ldpc_plan* plan, const float* llr_in, fl
     p.G = r.G;
     p.tables_bytes = r.tables_bytes;
     p.group_bytes = r.group_bytes;
+    p.gblk_off = r.gblk_off;
     p.app_off = r.app_off;
     p.r_off = r.r_off;
     p.r_stride = r.r_stride;
@@ -814,7 +895,7 @@ int ck::ldpc_decode_in_scratch(const ck_ldpc_plan* plan, const float* llr_in, fl
                       : 0;
     p.counter = reinterpret_cast<uint32_t*>(wsb);
     p.status = reinterpret_cast<uint32_t*>(wsb + 4);
-    p.g_r = reinterpret_cast<float*>(wsb + r.r_ws_off);
+    p.g_r = reinterpret_cast<uint32_t*>(wsb + r.r_ws_off);
     p.g_app = reinterpret_cast<float*>(wsb + r.app_ws_off);
     p.app_stride = r.app_stride;
     r.kernel<<<r.grid, r.T * r.G, r.smem, s>>>(p);

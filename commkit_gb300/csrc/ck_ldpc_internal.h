@@ -41,8 +41,9 @@ struct ck_ldpc_plan {
     int32_t max_deg = 0;
     int32_t max_layer_rows = 0;
     // Quasi-cyclic form: layer l holds base rows [h_layer[l], h_layer[l+1]),
-    // base row b has the circulants h_blk[2 i] (j Z), h_blk[2 i + 1] (shift)
-    // for i in [h_eptr[b], h_eptr[b+1]); schedule row b Z + r is its row r.
+    // base row b has the circulants h_blk[2 i] (j Z + shift), h_blk[2 i + 1]
+    // ((j + 1) Z) for i in [h_eptr[b], h_eptr[b+1]); schedule row b Z + r is
+    // its row r, with column r + h_blk[2 i] wrapped by Z at h_blk[2 i + 1].
     // CSR form: h_layer is layer_ptr, d_eptr row_ptr, d_cols cols.
     bool qc = false;
     int32_t Z = 0, mb = 0, nb = 0, nnzb = 0;

@@ -142,9 +142,11 @@ bool try_qc(const int32_t* row_ptr, const int32_t* cols, const int32_t* layer_pt
     for (int32_t l = 0; l <= L; ++l) plan->h_layer[l] = layer_ptr[l] / Z;
     plan->h_eptr = eptr;
     plan->h_blk.resize(blk_col.size() * 2);
+    // Per circulant: (j Z + shift, (j + 1) Z), so that row r's column is
+    // r + first, wrapped back by Z once it reaches the block's end.
     for (size_t i = 0; i < blk_col.size(); ++i) {
-        plan->h_blk[2 * i] = blk_col[i];
-        plan->h_blk[2 * i + 1] = blk_shift[i];
+        plan->h_blk[2 * i] = blk_col[i] + blk_shift[i];
+        plan->h_blk[2 * i + 1] = blk_col[i] + Z;
     }
     return true;
 }
