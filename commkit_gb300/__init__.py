@@ -6,7 +6,7 @@ commkit, rebuilt as hand-written CUDA behind the reference's public
 signatures and kernel-registry interface (:mod:`commkit_gb300.plugin`).
 """
 
-from .coding import DecodeResult, LDPCCode, MinSum, SumProduct, decode
+from .coding import DecodeResult, LDPCCode, MinSum, SumProduct, decode, decode_mixed
 from .mapping import Constellation, PrecisionWarning, compute_llr, compute_llr_frames
 
 __all__ = [
@@ -19,6 +19,7 @@ __all__ = [
     "compute_llr",
     "compute_llr_frames",
     "decode",
+    "decode_mixed",
 ]
 
 __version__ = "0.1.0"

@@ -47,6 +47,8 @@ EXPORTS = (
     "ck_ldpc_decode",
     "ck_ldpc_workspace_status",
     "ck_ldpc_decode_static",
+    "ck_ldpc_mixed_workspace_size",
+    "ck_ldpc_decode_mixed",
 )
 
 
@@ -81,6 +83,25 @@ class PlanInfo(ctypes.Structure):
             "num_variables", "num_edges", "num_layers", "max_row_degree", "device",
         )
     ]  # fmt: skip
+
+
+class Batch(ctypes.Structure):
+    _fields_ = [
+        ("plan", ctypes.c_void_p),
+        ("llr_in", ctypes.c_void_p),
+        ("llr_out", ctypes.c_void_p),
+        ("B", ctypes.c_int64),
+        ("n_in", ctypes.c_int32),
+        ("rule", ctypes.c_int32),
+        ("scale", ctypes.c_float),
+        ("offset", ctypes.c_float),
+        ("max_iterations", ctypes.c_int32),
+        ("early_stop", ctypes.c_int32),
+        ("iters", ctypes.c_void_p),
+        ("valid", ctypes.c_void_p),
+        ("bits", ctypes.c_void_p),
+        ("k_bits", ctypes.c_int32),
+    ]
 
 
 class Launch(ctypes.Structure):
@@ -124,6 +145,8 @@ def _declare(lib: ctypes.CDLL) -> None:
             [p, p, p, i64, i32, i32, f32, f32, i32, i32, p, p, p, i32, p, ctypes.c_size_t, p],
             ctypes.c_int),
         "ck_ldpc_workspace_status": ([p, p], ctypes.c_int),
+        "ck_ldpc_mixed_workspace_size": ([ctypes.POINTER(Batch), i32, size_p], ctypes.c_int),
+        "ck_ldpc_decode_mixed": ([ctypes.POINTER(Batch), i32, p, ctypes.c_size_t, p], ctypes.c_int),
         "ck_ldpc_decode_static": (
             [p, p, p, i64, i32, i32, f32, f32, i32, i32, p, p, p, i32, p], ctypes.c_int),
     }  # fmt: skip

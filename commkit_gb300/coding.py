@@ -24,7 +24,7 @@ import numpy as np
 from . import _device, _lib
 from .mapping import PrecisionWarning
 
-__all__ = ["DecodeResult", "LDPCCode", "MinSum", "SumProduct", "decode"]
+__all__ = ["DecodeResult", "LDPCCode", "MinSum", "SumProduct", "decode", "decode_mixed"]
 
 _HARD_LLR = 1.0
 
@@ -371,3 +371,67 @@ def _bool_dtype(xd: _device.DeviceArray):
 
         return torch.bool
     return np.bool_
+
+
+def decode_mixed(batches, *, workspace: Any = None, outputs: list | None = None) -> list[DecodeResult]:
+    """Decode frames of several quasi-cyclic codes in one launch.
+
+    ``batches`` is a sequence of ``(llrs, code, method)``: per code, LLRs
+    ``(B, n)`` (or ``(B n,)``) float32 on one CUDA device.  One persistent
+    kernel decodes them all; each block works on one code at a time and
+    moves to the code with the most frames left when its queue empties
+    (``ck_ldpc_decode_mixed``).  Returns one :class:`DecodeResult` per batch,
+    each bit-identical to ``decode(llrs, code=code, method=method)``.
+    """
+    items = []
+    device = None
+    for llrs, code, method in batches:
+        if not isinstance(code, LDPCCode):
+            raise TypeError(f"decode_mixed(): code must be an LDPCCode, got {type(code).__name__}.")
+        method = _resolve_method(method)
+        x0 = _device.wrap(llrs, "llrs")
+        x = _as_llrs(llrs, x0).reshape(-1)
+        if x.shape[0] % code.n:
+            raise ValueError(f"decode_mixed(): {x.shape[0]} LLRs is not a multiple of n = {code.n}.")
+        B = x.shape[0] // code.n
+        xd = _device.wrap(x, "llrs")
+        if device is None:
+            device = xd
+        elif xd.device != device.device:
+            raise ValueError("decode_mixed(): all batches must be on one device.")
+        if outputs is not None:
+            # Preallocated (llrs (B, n) f32, bits (B, k) i8, iters (B,) i32, valid (B,) u8):
+            # nothing is allocated, so the call can be captured in a CUDA graph.
+            out, bits, iters, valid = outputs[len(items)]
+        else:
+            out = _device.empty(xd, (B, code.n), np.float32)
+            bits = _device.empty(xd, (B, code.k), np.int8)
+            iters = _device.empty(xd, (B,), np.int32)
+            valid = _device.empty(xd, (B,), np.uint8)
+        items.append((x, xd, code, method, B, out, bits, iters, valid))
+    if len(items) > 4:
+        raise ValueError("decode_mixed(): at most 4 codes per launch.")
+    results = []
+    if items:
+        with _device.on_device(device):
+            arr = (_lib.Batch * len(items))()
+            for i, (x, xd, code, method, B, out, bits, iters, valid) in enumerate(items):
+                plan = code._plan(xd.device)
+                arr[i] = _lib.Batch(plan.handle, xd.ptr, _device.wrap(out).ptr, B, code.n,
+                                    _lib.CK_LDPC_MIN_SUM, np.float32(method.scale),
+                                    np.float32(method.offset), int(method.max_iterations),
+                                    1 if method.early_stop else 0, _device.wrap(iters).ptr,
+                                    _device.wrap(valid).ptr, _device.wrap(bits).ptr, code.k)  # fmt: skip
+            lib = _lib.lib()
+            if workspace is None:
+                need = ctypes.c_size_t(0)
+                _lib.check(lib.ck_ldpc_mixed_workspace_size(arr, len(items), ctypes.byref(need)),
+                           "decode_mixed()")  # fmt: skip
+                workspace = _device.empty(device, (max(int(need.value), 256),), np.uint8)
+            wsd = _device.wrap(workspace, "workspace")
+            st = lib.ck_ldpc_decode_mixed(arr, len(items), wsd.ptr, wsd.size, _device.stream_of(device))
+            _lib.check(st, "decode_mixed()")
+    for x, xd, code, method, B, out, bits, iters, valid in items:
+        results.append(DecodeResult(bits=bits, llrs=out, valid=valid.view(_bool_dtype(xd)),
+                                    iterations=iters, checked=True))  # fmt: skip
+    return results

@@ -38,6 +38,7 @@
 // schedule's order, as in the reference.
 #include <math_constants.h>
 #include <stdint.h>
+#include <string.h>
 
 #include <algorithm>
 
@@ -491,7 +492,215 @@ __global__ void __launch_bounds__(max_block_threads(QC, DMAX))
     }
 }
 
+// ---------------------------------------------------------------------------
+// Mixed-code persistent kernel: frames of several quasi-cyclic codes in one
+// launch.  Every block can host any code's frame groups (its shared memory
+// and threads are sized for the largest); it starts on a code chosen in
+// proportion to the work and, once that code's queue is empty, switches to
+// the code with the most work left.  The frame loop is the plain kernel's:
+// same rows, same order, same bits.
+// ---------------------------------------------------------------------------
+
+constexpr int kMaxMixed = CK_LDPC_MAX_MIXED;
+constexpr int kMixedThreads = 768;
+
+struct MixedCode {
+    const int32_t* layer;
+    const int32_t* eptr;
+    const int2* blk;
+    int32_t N, m, L, Z, Zp, mb, nnzb;
+    const float* llr_in;
+    float* llr_out;
+    uint32_t B;
+    int32_t n_in;
+    int32_t* iters;
+    uint8_t* valid;
+    int8_t* bits;
+    int32_t k_bits;
+    float scale, offset;
+    int32_t max_iterations, early_stop;
+    int32_t T, G, q_bstep, r_smem;
+    uint32_t tables_bytes, group_bytes, gblk_off, app_off, r_off, r_stride;
+    uint32_t* g_r;
+    uint32_t* counter;
+    float weight;  // edges per frame
+};
+
+struct MixedParams {
+    MixedCode code[kMaxMixed];
+    int32_t num_codes;
+    int32_t start_block[kMaxMixed + 1];  // blocks [start_block[c], start_block[c+1]) begin on c
+};
+
+// The code this block should work on next: `prefer` while its queue has
+// frames, else the one with the most edges left; -1 when all are drained.
+__device__ int mixed_pick(const MixedParams& p, int prefer) {
+    if (prefer >= 0) {
+        const uint32_t taken = *reinterpret_cast<volatile uint32_t*>(p.code[prefer].counter);
+        if (taken < p.code[prefer].B) return prefer;
+    }
+    int best = -1;
+    float most = 0.0f;
+    for (int c = 0; c < p.num_codes; ++c) {
+        const uint32_t taken = *reinterpret_cast<volatile uint32_t*>(p.code[c].counter);
+        if (taken >= p.code[c].B) continue;
+        const float left = static_cast<float>(p.code[c].B - taken) * p.code[c].weight;
+        if (best < 0 || left > most) {
+            best = c;
+            most = left;
+        }
+    }
+    return best;
+}
+
+// Decodes frames of code K with group g until K's queue is empty.
+template <int DMAX, bool R_SMEM>
+__device__ void mixed_frames(const MixedCode& K, unsigned char* smem, const int32_t* s_layer,
+                             const int32_t* s_eptr, const int2* s_blk, const int g,
+                             const int tid) {
+    using ck::group_any;
+    using ck::group_sync;
+    const int bar = g + 1;
+    unsigned char* gbase = smem + K.tables_bytes + static_cast<uint32_t>(g) * K.group_bytes;
+    volatile uint32_t* s_frame = reinterpret_cast<volatile uint32_t*>(gbase + 8);
+    float* a = reinterpret_cast<float*>(gbase + K.app_off);
+    uint4* rs = reinterpret_cast<uint4*>(gbase + K.r_off);
+    const uint32_t slot = blockIdx.x * static_cast<uint32_t>(K.G) + static_cast<uint32_t>(g);
+    uint32_t* g1 = K.g_r + static_cast<size_t>(slot) * 3 * K.r_stride;
+    uint32_t* g2 = g1 + K.r_stride;
+    uint32_t* g3 = g2 + K.r_stride;
+    int2* gblk = reinterpret_cast<int2*>(gbase + K.gblk_off);
+    const uint32_t a_addr = ck::smem_addr(a);
+    for (int i = tid; i < K.nnzb; i += K.T)
+        gblk[i] = make_int2(static_cast<int>(a_addr + 4u * static_cast<uint32_t>(s_blk[i].x)),
+                            static_cast<int>(a_addr + 4u * static_cast<uint32_t>(s_blk[i].y)));
+    const int32_t qr0 = K.T >= K.Zp ? tid % K.Zp : tid;
+    const int32_t qb0 = K.T >= K.Zp ? tid / K.Zp : 0;
+    const uint32_t r4 = 4u * static_cast<uint32_t>(qr0);
+    const uint32_t Z4 = 4u * static_cast<uint32_t>(K.Z);
+
+    auto syndrome_ok = [&]() -> bool {
+        const int32_t rounds = (K.mb + K.q_bstep - 1) / K.q_bstep;
+        for (int32_t k = 0; k < rounds; ++k) {
+            const int32_t b = k * K.q_bstep + qb0;
+            for (int32_t r = qr0; r - qr0 < K.Zp; r += K.T) {
+                uint32_t parity = 0;
+                if (b < K.mb && r < K.Z) {
+                    const int32_t e0 = s_eptr[b];
+                    const int deg = s_eptr[b + 1] - e0;
+                    const QcCols col_of{s_blk + e0, r, K.Z};
+                    for (int e = 0; e < deg; ++e) parity ^= a[col_of(e)] < 0.0f ? 1u : 0u;
+                }
+                if (group_any(static_cast<int>(parity), bar, K.T)) return false;
+            }
+        }
+        return true;
+    };
+
+    for (;;) {
+        if (tid == 0) *s_frame = atomicAdd(K.counter, 1u);
+        group_sync(bar, K.T);
+        const uint32_t f = *s_frame;
+        if (f >= K.B) break;
+        const float* src = K.llr_in + static_cast<size_t>(f) * K.n_in;
+        for (int i = tid; i < K.n_in; i += K.T) a[i] = __fadd_rn(__ldcs(src + i), 0.0f);
+        for (int i = K.n_in + tid; i < K.N; i += K.T) a[i] = 0.0f;
+        for (int i = tid; i < K.m; i += K.T) {
+            if (R_SMEM) {
+                rs[i] = make_uint4(0u, 0u, 0u, 0u);
+            } else {
+                g1[i] = 0u;
+                g2[i] = 0u;
+                g3[i] = 0u;
+            }
+        }
+        group_sync(bar, K.T);
+        int32_t it = 0;
+        bool ok = K.early_stop && syndrome_ok();
+        while (!ok && it < K.max_iterations) {
+            for (int32_t l = 0; l < K.L; ++l) {
+                const int32_t b1 = s_layer[l + 1];
+                for (int32_t b = s_layer[l] + qb0; b < b1; b += K.q_bstep) {
+                    const int32_t e0 = s_eptr[b];
+                    const int deg = s_eptr[b + 1] - e0;
+                    for (int32_t r = qr0; r - qr0 < K.Zp; r += K.T) {
+                        if (r >= K.Z) continue;
+                        const uint32_t row = static_cast<uint32_t>(b) * static_cast<uint32_t>(K.Z) +
+                                             static_cast<uint32_t>(r);
+                        const uint4 st = R_SMEM ? rs[row]
+                                                : make_uint4(__ldcg(g1 + row), __ldcg(g2 + row),
+                                                             __ldcg(g3 + row), 0u);
+                        float m1 = __uint_as_float(st.x), m2 = __uint_as_float(st.y);
+                        uint32_t w = st.z;
+                        qc_row<DMAX>(gblk + e0, deg, r4 + 4u * static_cast<uint32_t>(r - qr0), Z4, m1,
+                                     m2, w, K.scale, K.offset);
+                        if (R_SMEM) {
+                            rs[row] = make_uint4(__float_as_uint(m1), __float_as_uint(m2), w, 0u);
+                        } else {
+                            __stcg(g1 + row, __float_as_uint(m1));
+                            __stcg(g2 + row, __float_as_uint(m2));
+                            __stcg(g3 + row, w);
+                        }
+                    }
+                }
+                group_sync(bar, K.T);
+            }
+            ++it;
+            if (K.early_stop) ok = syndrome_ok();
+        }
+        if (!K.early_stop) ok = syndrome_ok();
+        float* dst = K.llr_out + static_cast<size_t>(f) * K.n_in;
+        for (int i = tid; i < K.n_in; i += K.T) __stcs(dst + i, a[i]);
+        if (K.bits) {
+            int8_t* bdst = K.bits + static_cast<size_t>(f) * K.k_bits;
+            for (int i = tid; i < K.k_bits; i += K.T) bdst[i] = a[i] < 0.0f ? 1 : 0;
+        }
+        if (tid == 0) {
+            K.iters[f] = it;
+            K.valid[f] = ok ? 1 : 0;
+        }
+        group_sync(bar, K.T);
+    }
+}
+
+template <int DMAX>
+__global__ void __launch_bounds__(kMixedThreads) ldpc_mixed_kernel(const __grid_constant__ MixedParams p) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ int s_code;
+    if (threadIdx.x == 0) {
+        int c = 0;
+        while (c + 1 < p.num_codes && static_cast<int32_t>(blockIdx.x) >= p.start_block[c + 1]) ++c;
+        s_code = mixed_pick(p, c);
+    }
+    __syncthreads();
+    for (;;) {
+        const int c = s_code;
+        if (c < 0) break;
+        const MixedCode& K = p.code[c];
+        int32_t* s_layer = reinterpret_cast<int32_t*>(smem);
+        int32_t* s_eptr = s_layer + (K.L + 1);
+        int2* s_blk = reinterpret_cast<int2*>(
+            smem + ((static_cast<uint32_t>(K.L + 1 + K.mb + 1) * 4 + 7) & ~7u));
+        for (int i = threadIdx.x; i <= K.L; i += blockDim.x) s_layer[i] = K.layer[i];
+        for (int i = threadIdx.x; i <= K.mb; i += blockDim.x) s_eptr[i] = K.eptr[i];
+        for (int i = threadIdx.x; i < K.nnzb; i += blockDim.x) s_blk[i] = K.blk[i];
+        __syncthreads();
+        const int g = threadIdx.x / K.T;
+        if (g < K.G) {
+            const int tid = threadIdx.x - g * K.T;
+            if (K.r_smem)
+                mixed_frames<DMAX, true>(K, smem, s_layer, s_eptr, s_blk, g, tid);
+            else
+                mixed_frames<DMAX, false>(K, smem, s_layer, s_eptr, s_blk, g, tid);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_code = mixed_pick(p, -1);
+        __syncthreads();
+    }
+}
+
 using KernelFn = void (*)(Params);
+using KernelMixed = void (*)(MixedParams);
 
 template <bool QC, int DMAX>
 KernelFn pick_placement(bool app_smem, bool r_smem) {
@@ -900,4 +1109,206 @@ int ck::ldpc_decode_in_scratch(const ck_ldpc_plan* plan, const float* llr_in, fl
     p.app_stride = r.app_stride;
     r.kernel<<<r.grid, r.T * r.G, r.smem, s>>>(p);
     return ck::cuda_check(cudaGetLastError(), "decoder launch");
+}
+
+
+// ---------------------------------------------------------------------------
+// Mixed-code launch
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct MixedResolved {
+    MixedParams p;
+    int block_threads;
+    uint32_t smem;
+    int grid;
+    size_t ws_bytes;
+    size_t r_off[kMaxMixed];
+    bool wide;  // some code has rows above degree 16
+};
+
+int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
+    if (!batches || n < 1 || n > kMaxMixed)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "1 to %d batches per mixed launch, got %d", kMaxMixed, n);
+    int dev = -1;
+    CK_CUDA(cudaGetDevice(&dev));
+    int sms = 0, optin = 0;
+    CK_TRY(device_limits(dev, &sms, &optin));
+    memset(&R->p, 0, sizeof(R->p));
+    R->p.num_codes = n;
+    R->block_threads = 32;
+    R->smem = 0;
+    R->wide = false;
+    for (int c = 0; c < n; ++c) {
+        const ck_ldpc_batch& b = batches[c];
+        const ck_ldpc_plan* plan = b.plan;
+        if (!plan) return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d has no plan", c);
+        if (plan->device != dev)
+            return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: plan is for device %d, current is %d", c,
+                            plan->device, dev);
+        if (!plan->qc) return ck::fail(CK_ERR_UNSUPPORTED, "batch %d: mixed launches take quasi-cyclic codes", c);
+        if (b.rule != CK_LDPC_MIN_SUM) return ck::fail(CK_ERR_UNSUPPORTED, "only the min-sum rule is implemented");
+        if (b.B < 0 || b.B >= (int64_t(1) << 31)) return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: bad B", c);
+        if (b.n_in < 1 || b.n_in > plan->N) return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: bad n_in", c);
+        if (b.max_iterations < 0) return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: bad max_iterations", c);
+        if (b.bits && (b.k_bits < 0 || b.k_bits > b.n_in))
+            return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: bad k_bits", c);
+        if (b.B > 0 && (!b.llr_in || !b.llr_out || !b.iters || !b.valid))
+            return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: missing arrays", c);
+        if (plan->max_deg > 16) R->wide = true;
+        const int32_t Zp = (plan->Z + 31) / 32 * 32;
+        int32_t T = plan->launch.threads_per_frame;
+        if (T == 0) {
+            T = Zp;
+            while (T > 512 && T % 64 == 0) T /= 2;
+        }
+        if (T % Zp != 0 && Zp % T != 0)
+            return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: threads_per_frame %d vs lifting", c, T);
+        const uint32_t tables = align_up(align_up(static_cast<uint32_t>(plan->L + 1 + plan->mb + 1) * 4, 8) +
+                                             static_cast<uint32_t>(plan->nnzb) * 8, 128);
+        const uint32_t ctrl = 128;
+        const uint32_t gblk = align_up(static_cast<uint32_t>(plan->nnzb) * 8, 128);
+        const uint32_t app = align_up(static_cast<uint32_t>(plan->N) * 4, 128);
+        const uint32_t r_stride = align_up(static_cast<uint32_t>(plan->m), 32);
+        const uint32_t rsm = r_stride * 16;
+        // 1 KB stays free for the kernel's static shared variable.
+        const uint32_t budget = static_cast<uint32_t>(optin) > tables + 1024 ? optin - tables - 1024 : 0;
+        const int32_t max_threads = R->wide ? 512 : kMixedThreads;
+        int32_t gmax = std::min(max_threads / T, T > 32 ? ck::kMaxNamedGroups : 32);
+        // Message state in shared memory when two frames still fit with it.
+        const bool r_smem = plan->launch.placement == CK_LDPC_PLACE_GLOBAL
+                                ? false
+                                : 2 * (ctrl + gblk + app + rsm) <= budget;
+        const uint32_t group = ctrl + gblk + app + (r_smem ? rsm : 0);
+        gmax = std::min<int32_t>(gmax, static_cast<int32_t>(budget / group));
+        int32_t G = plan->launch.frames_per_block > 0 ? std::min(plan->launch.frames_per_block, gmax) : gmax;
+        if (G < 1) return ck::fail(CK_ERR_UNSUPPORTED, "batch %d: a frame does not fit a block", c);
+        MixedCode& K = R->p.code[c];
+        K.layer = plan->d_layer;
+        K.eptr = plan->d_eptr;
+        K.blk = reinterpret_cast<const int2*>(plan->d_blk);
+        K.N = plan->N;
+        K.m = plan->m;
+        K.L = plan->L;
+        K.Z = plan->Z;
+        K.Zp = Zp;
+        K.mb = plan->mb;
+        K.nnzb = plan->nnzb;
+        K.llr_in = b.llr_in;
+        K.llr_out = b.llr_out;
+        K.B = static_cast<uint32_t>(b.B);
+        K.n_in = b.n_in;
+        K.iters = b.iters;
+        K.valid = b.valid;
+        K.bits = b.k_bits > 0 ? b.bits : nullptr;
+        K.k_bits = b.k_bits;
+        K.scale = b.scale;
+        K.offset = b.offset;
+        K.max_iterations = b.max_iterations;
+        K.early_stop = b.early_stop ? 1 : 0;
+        K.T = T;
+        K.G = G;
+        K.q_bstep = T >= Zp ? T / Zp : 1;
+        K.r_smem = r_smem ? 1 : 0;
+        K.tables_bytes = tables;
+        K.group_bytes = group;
+        K.gblk_off = ctrl;
+        K.app_off = ctrl + gblk;
+        K.r_off = ctrl + gblk + app;
+        K.r_stride = r_stride;
+        K.weight = static_cast<float>(plan->E);
+        R->block_threads = std::max(R->block_threads, T * G);
+        R->smem = std::max(R->smem, tables + static_cast<uint32_t>(G) * group);
+    }
+    if (R->wide && R->block_threads > 512)
+        return ck::fail(CK_ERR_UNSUPPORTED, "mixed launch of %d threads with rows above degree 16",
+                        R->block_threads);
+    KernelMixed kernel = R->wide ? ldpc_mixed_kernel<27> : ldpc_mixed_kernel<16>;
+    CK_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void*>(kernel),
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(R->smem)));
+    int per_sm = 0;
+    CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(kernel),
+                                                          R->block_threads, R->smem));
+    if (per_sm < 1) return ck::fail(CK_ERR_UNSUPPORTED, "mixed block does not fit an SM");
+    int64_t need = 0;
+    for (int c = 0; c < n; ++c)
+        need += (R->p.code[c].B + R->p.code[c].G - 1) / R->p.code[c].G;
+    R->grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(need, int64_t(sms) * per_sm)));
+    // Starting split of the blocks in proportion to each code's work
+    // (frames x edges x iteration budget), at least one block per code with frames.
+    double total = 0.0, work[kMaxMixed] = {0, 0, 0, 0};
+    for (int c = 0; c < n; ++c) {
+        const MixedCode& K = R->p.code[c];
+        work[c] = static_cast<double>(K.B) * K.weight * std::max(1, K.max_iterations) / K.G;
+        total += work[c];
+    }
+    int start = 0;
+    for (int c = 0; c < n; ++c) {
+        R->p.start_block[c] = start;
+        int share = total > 0 ? static_cast<int>(R->grid * work[c] / total + 0.5) : 0;
+        if (R->p.code[c].B > 0) share = std::max(share, 1);
+        start = std::min(R->grid, start + share);
+    }
+    R->p.start_block[n] = R->grid;
+    // Workspace: counters, then each code's device-memory message slots.
+    size_t off = kHeaderBytes;
+    for (int c = 0; c < n; ++c) {
+        R->r_off[c] = off;
+        if (!R->p.code[c].r_smem)
+            off += ((static_cast<size_t>(R->grid) * R->p.code[c].G * R->p.code[c].r_stride * 12 + 255) / 256) * 256;
+    }
+    R->ws_bytes = off;
+    return CK_OK;
+}
+
+}  // namespace
+
+extern "C" int ck_ldpc_mixed_workspace_size(const ck_ldpc_batch* batches, int32_t num_batches,
+                                            size_t* bytes) {
+    ck::clear_error();
+    if (!bytes) return ck::fail(CK_ERR_INVALID_ARGUMENT, "bytes is NULL");
+    MixedResolved R;
+    CK_TRY(resolve_mixed(batches, num_batches, &R));
+    *bytes = R.ws_bytes;
+    return CK_OK;
+}
+
+extern "C" int ck_ldpc_decode_mixed(const ck_ldpc_batch* batches, int32_t num_batches,
+                                    void* workspace, size_t workspace_bytes, void* stream) {
+    ck::clear_error();
+    MixedResolved R;
+    CK_TRY(resolve_mixed(batches, num_batches, &R));
+    int64_t total = 0;
+    for (int c = 0; c < num_batches; ++c) total += batches[c].B;
+    if (total == 0) return CK_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    void* ws = workspace;
+    bool owned = false;
+    if (ws == nullptr) {
+        CK_CUDA(cudaMallocAsync(&ws, R.ws_bytes, s));
+        owned = true;
+    } else {
+        if (workspace_bytes < R.ws_bytes)
+            return ck::fail(CK_ERR_INVALID_ARGUMENT, "workspace of %zu bytes, %zu needed", workspace_bytes,
+                            R.ws_bytes);
+        if (reinterpret_cast<uintptr_t>(ws) % 256)
+            return ck::fail(CK_ERR_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
+    }
+    unsigned char* wsb = static_cast<unsigned char*>(ws);
+    for (int c = 0; c < num_batches; ++c) {
+        R.p.code[c].counter = reinterpret_cast<uint32_t*>(wsb + 4 * c);
+        R.p.code[c].g_r = reinterpret_cast<uint32_t*>(wsb + R.r_off[c]);
+    }
+    int status = ck::cuda_check(cudaMemsetAsync(wsb, 0, kHeaderBytes, s), "cudaMemsetAsync");
+    if (status == CK_OK) {
+        KernelMixed kernel = R.wide ? ldpc_mixed_kernel<27> : ldpc_mixed_kernel<16>;
+        kernel<<<R.grid, R.block_threads, R.smem, s>>>(R.p);
+        status = ck::cuda_check(cudaGetLastError(), "mixed decoder launch");
+    }
+    if (owned) {
+        const int st = ck::cuda_check(cudaFreeAsync(ws, s), "cudaFreeAsync");
+        if (status == CK_OK) status = st;
+    }
+    return status;
 }

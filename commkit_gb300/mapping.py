@@ -27,7 +27,7 @@ import numpy as np
 from . import _device, _lib
 from .workloads import gray_qam_points
 
-__all__ = ["Constellation", "PrecisionWarning", "compute_llr", "compute_llr_frames"]
+__all__ = ["Constellation", "PrecisionWarning", "compute_llr", "compute_llr_frames", "inv_s2_frames"]
 
 
 class PrecisionWarning(UserWarning):
@@ -282,34 +282,50 @@ def compute_llr(symbols: Any, *, noise_var: float | None = None, esn0_db: float 
     return constellation.llr(symbols, noise_var=nv, method=method)
 
 
-def compute_llr_frames(symbols: Any, *, noise_var: Any, constellation: Constellation,
-                       method: str = "maxlog") -> Any:  # fmt: skip
+def inv_s2_frames(noise_var: Any) -> np.ndarray:
+    """Per-frame ``float32(1 / max(nv, 1e-20))``, as :func:`inv_s2` for each frame."""
+    nv = np.asarray(noise_var, dtype=np.float64).reshape(-1)
+    if not np.all(np.isfinite(nv)) or np.any(nv < 0):
+        raise ValueError("noise_var must be finite and >= 0")
+    return (1.0 / np.maximum(nv, 1e-20)).astype(np.float32)
+
+
+def compute_llr_frames(symbols: Any, *, noise_var: Any = None, constellation: Constellation,
+                       method: str = "maxlog", inv_s2: Any = None, out: Any = None) -> Any:  # fmt: skip
     """Batched demapping with one noise variance per frame (an extension).
 
     ``symbols`` ``(F, S)`` complex64 on a CUDA device, ``noise_var`` ``(F,)``
     (host array or sequence).  Returns ``(F, S * k)`` float32; row ``f``
     equals ``compute_llr(symbols[f], noise_var=noise_var[f], ...)`` bit for
-    bit, in one launch instead of F.
+    bit, in one launch instead of F.  Instead of ``noise_var``, ``inv_s2``
+    may give the per-frame ``float32(1 / max(nv, 1e-20))`` already on the
+    device (:func:`inv_s2_frames`), and ``out`` a preallocated output; with
+    both, the call does no host-to-device copy and no allocation, so it can
+    be captured in a CUDA graph.
     """
     _check_method(method)
     x = _device.wrap(symbols, "symbols")
     _device.check(x, "symbols", np.complex64, (None, None))
     F, S = x.shape
-    nv = np.asarray(noise_var, dtype=np.float64).reshape(-1)
-    if nv.size != F:
-        raise ValueError(f"noise_var needs one value per frame ({F}), got {nv.size}")
-    if not np.all(np.isfinite(nv)) or np.any(nv < 0):
-        raise ValueError("noise_var must be finite and >= 0")
-    s2_host = (1.0 / np.maximum(nv, 1e-20)).astype(np.float32)
     k = constellation.bits_per_symbol
-    out = _device.empty(x, (F, S * k), np.float32)
+    if (noise_var is None) == (inv_s2 is None):
+        raise ValueError("compute_llr_frames(): give one of noise_var and inv_s2.")
+    s2_host = None
+    if inv_s2 is None:
+        s2_host = inv_s2_frames(noise_var)
+        if s2_host.size != F:
+            raise ValueError(f"noise_var needs one value per frame ({F}), got {s2_host.size}")
+    if out is None:
+        out = _device.empty(x, (F, S * k), np.float32)
+    od = _device.wrap(out, "out")
+    _device.check(od, "out", np.float32, (F, S * k))
     if F * S == 0:
         return out
-    od = _device.wrap(out, "out")
     kind = "maxlog" if method == "maxlog" else "levels"
     with _device.on_device(x):
-        s2 = _device.to_device(x, s2_host)
+        s2 = _device.to_device(x, s2_host) if s2_host is not None else inv_s2
         sd = _device.wrap(s2, "inv_s2")
+        _device.check(sd, "inv_s2", np.float32, (F,))
         tables = device_tables(constellation, kind, x)
         half = len(tables) // 2
         re, im = _axis_struct(tables[:half], kind), _axis_struct(tables[half:], kind)

@@ -1,0 +1,122 @@
+"""Device-resident receiver pipelines: demap + decode with no per-step allocation.
+
+:class:`MixedReceiver` holds, per code, the symbol buffer, the per-frame
+``1/sigma^2``, the LLRs, the decoder outputs and one shared workspace on the
+device.  A step demaps every code's frames (``compute_llr_frames``) and
+decodes all of them in ONE launch of the mixed-code persistent kernel
+(``decode_mixed``).  Nothing is allocated or copied from the host inside a
+step, so :meth:`capture` records it once as a CUDA graph and :meth:`run`
+replays it: one graph launch per batch of mixed traffic.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import Any
+
+import numpy as np
+
+from . import _device, _lib
+from .coding import DecodeResult, LDPCCode, MinSum, decode_mixed
+from .mapping import Constellation, compute_llr_frames, inv_s2_frames
+
+
+@dataclass
+class CodeSlot:
+    """One code's frames in a :class:`MixedReceiver`."""
+
+    code: LDPCCode
+    constellation: Constellation
+    frames: int
+    method: MinSum
+    demap: str = "maxlog"
+
+
+class MixedReceiver:
+    """Demap + mixed-code decode of fixed-size batches on one CUDA device."""
+
+    def __init__(self, slots: list[CodeSlot], device: Any = None):
+        import torch
+
+        if not slots or len(slots) > 4:
+            raise ValueError("MixedReceiver: 1 to 4 code slots")
+        self.torch = torch
+        self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        self.slots = slots
+        self.sym, self.s2, self.llr, self.outputs = [], [], [], []
+        for s in slots:
+            k = s.constellation.bits_per_symbol
+            if s.code.n % k:
+                raise ValueError(f"n = {s.code.n} is not a multiple of {k} bits per symbol")
+            S = s.code.n // k
+            self.sym.append(torch.zeros((s.frames, S), dtype=torch.complex64, device=self.device))
+            self.s2.append(torch.ones((s.frames,), dtype=torch.float32, device=self.device))
+            self.llr.append(torch.empty((s.frames, s.code.n), dtype=torch.float32, device=self.device))
+            self.outputs.append((
+                torch.empty((s.frames, s.code.n), dtype=torch.float32, device=self.device),
+                torch.empty((s.frames, s.code.k), dtype=torch.int8, device=self.device),
+                torch.empty((s.frames,), dtype=torch.int32, device=self.device),
+                torch.empty((s.frames,), dtype=torch.uint8, device=self.device),
+            ))  # fmt: skip
+        self.workspace = torch.empty(max(self._workspace_bytes(), 256), dtype=torch.uint8, device=self.device)
+        self.graph = None
+
+    def _batches(self) -> Any:
+        arr = (_lib.Batch * len(self.slots))()
+        for i, s in enumerate(self.slots):
+            plan = s.code._plan(self.device.index)
+            out = self.outputs[i]
+            arr[i] = _lib.Batch(plan.handle, self.llr[i].data_ptr(), out[0].data_ptr(), s.frames, s.code.n,
+                                _lib.CK_LDPC_MIN_SUM, np.float32(s.method.scale), np.float32(s.method.offset),
+                                int(s.method.max_iterations), 1 if s.method.early_stop else 0,
+                                out[2].data_ptr(), out[3].data_ptr(), out[1].data_ptr(), s.code.k)  # fmt: skip
+        return arr
+
+    def _workspace_bytes(self) -> int:
+        need = ctypes.c_size_t(0)
+        with self.torch.cuda.device(self.device):
+            _lib.check(_lib.lib().ck_ldpc_mixed_workspace_size(self._batches(), len(self.slots),
+                                                              ctypes.byref(need)), "MixedReceiver")  # fmt: skip
+        return int(need.value)
+
+    def load(self, symbols: list, noise_var: list) -> None:
+        """Stage one batch: per slot ``(frames, S)`` complex64 symbols (host
+        or device) and per-frame noise variances (host)."""
+        for i, (x, nv) in enumerate(zip(symbols, noise_var, strict=True)):
+            t = x if isinstance(x, self.torch.Tensor) else self.torch.from_numpy(np.ascontiguousarray(x))
+            self.sym[i].copy_(t, non_blocking=True)
+            self.s2[i].copy_(self.torch.from_numpy(inv_s2_frames(nv)), non_blocking=False)
+
+    def step(self) -> None:
+        """Demap every slot and decode them all in one mixed launch (no allocation)."""
+        for i, s in enumerate(self.slots):
+            compute_llr_frames(self.sym[i], constellation=s.constellation, method=s.demap,
+                               inv_s2=self.s2[i], out=self.llr[i])  # fmt: skip
+        decode_mixed([(self.llr[i], s.code, s.method) for i, s in enumerate(self.slots)],
+                     workspace=self.workspace, outputs=self.outputs)  # fmt: skip
+
+    def capture(self, warmup: int = 2) -> None:
+        """Record :meth:`step` as a CUDA graph (after ``warmup`` eager steps)."""
+        torch = self.torch
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(side):
+            for _ in range(warmup):
+                self.step()
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.step()
+
+    def run(self) -> None:
+        """One step: replay the captured graph, or run eagerly if none."""
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self.step()
+
+    def results(self) -> list[DecodeResult]:
+        torch = self.torch
+        return [DecodeResult(bits=o[1], llrs=o[0], valid=o[3].view(torch.bool), iterations=o[2], checked=True)
+                for o in self.outputs]  # fmt: skip

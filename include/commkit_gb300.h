@@ -227,6 +227,44 @@ int ck_ldpc_decode(const ck_ldpc_plan* plan, const float* llr_in, float* llr_out
  */
 int ck_ldpc_workspace_status(const void* workspace, void* stream);
 
+/* One code's frames in a mixed-code launch (as ck_ldpc_decode's arguments). */
+typedef struct ck_ldpc_batch {
+    const ck_ldpc_plan* plan;
+    const float* llr_in;  /* (B, n_in) */
+    float* llr_out;       /* (B, n_in), may equal llr_in */
+    int64_t B;
+    int32_t n_in;
+    int32_t rule;         /* CK_LDPC_MIN_SUM */
+    float scale;
+    float offset;
+    int32_t max_iterations;
+    int32_t early_stop;
+    int32_t* iters;       /* (B,) */
+    uint8_t* valid;       /* (B,) */
+    int8_t* bits;         /* (B, k_bits) or NULL */
+    int32_t k_bits;
+} ck_ldpc_batch;
+
+#define CK_LDPC_MAX_MIXED 4
+
+/* Device scratch bytes of a mixed-code launch of these batches. */
+int ck_ldpc_mixed_workspace_size(const ck_ldpc_batch* batches, int32_t num_batches,
+                                 size_t* bytes);
+
+/*
+ * Frames of up to CK_LDPC_MAX_MIXED different quasi-cyclic codes (lengths,
+ * rates, iteration budgets) decoded in ONE launch of a persistent kernel.
+ * Every block can host any code's frame groups; it starts on a code chosen
+ * in proportion to the work, pulls that code's frames from a device queue
+ * (a frame retires as soon as its syndrome passes, and its group takes the
+ * next), and when that queue is empty switches to the code with the most
+ * frames left.  Each frame's results are bit-identical to ck_ldpc_decode's.
+ * No counterpart in the reference, which decodes one code per call.  All
+ * plans must be quasi-cyclic and on the current device.
+ */
+int ck_ldpc_decode_mixed(const ck_ldpc_batch* batches, int32_t num_batches, void* workspace,
+                         size_t workspace_bytes, void* stream);
+
 /* Capacity of the decoder's static scratch array (64 MiB per GPU). */
 #define CK_LDPC_STATIC_SCRATCH_BYTES (64u * 1024u * 1024u)
 
