@@ -191,6 +191,9 @@ class LDPCCode:
         plan = self._plans.get(device)
         if plan is None:
             plan = self._plans[device] = _Plan(*self._schedule, self.num_checks, self.num_variables)
+            from .tuning import apply_cached
+
+            apply_cached(self, plan, device)
         return plan
 
 
