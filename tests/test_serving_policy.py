@@ -8,36 +8,34 @@ import pytest
 from commkit_gb300.serving import Admission, Request
 
 
-def _req(rid, frames):
-    return Request(rid, "A", 4, np.zeros((frames, 8), np.complex64), 0.1, arrival=rid * 1e-3)
+def _req(rid, frames, code="A"):
+    return Request(rid, code, 4, np.zeros((frames, 8), np.complex64), 0.1, arrival=rid * 1e-3)
 
 
-def test_admission_respects_budget_order_and_slots():
-    adm = Admission(budget=1000, max_inflight=2, batch_overhead=100)
-    for i, f in enumerate([3, 4, 3, 5]):
-        adm.arrive(_req(i, f))
-    cost = lambda r: 100 * r.frames  # noqa: E731
-    b1 = adm.next_batch(cost)  # 100 + 300 + 400 = 800; the next (300) would exceed 1000
-    assert [r.rid for r in b1] == [0, 1] and adm.in_use == 800 and adm.inflight == 1
-    assert adm.next_batch(cost) == []  # 800 + 100 + 300 > 1000: waits for memory
-    adm.release(800)
-    b2 = adm.next_batch(cost)  # no overtaking: 2 (300) then 3 (500) -> 900
-    assert [r.rid for r in b2] == [2, 3] and adm.in_use == 900
+def _fits(cap):
+    def fits(batch, r):
+        return sum(q.frames for q in batch if q.code == r.code) + r.frames <= cap[r.code]
+
+    return fits
 
 
-def test_admission_limits_batches_in_flight():
-    adm = Admission(budget=10**9, max_inflight=1)
-    adm.arrive(_req(0, 1))
-    adm.arrive(_req(1, 1))
-    assert len(adm.next_batch(lambda r: 1)) == 2
-    adm.arrive(_req(2, 1))
-    assert adm.next_batch(lambda r: 1) == []  # the slot is busy
-    adm.release(2)
-    assert [r.rid for r in adm.next_batch(lambda r: 1)] == [2]
+def test_batches_take_fifo_requests_that_fit_a_slot():
+    adm = Admission(slots=2)
+    for i, (f, c) in enumerate([(3, "A"), (4, "A"), (2, "B"), (5, "A"), (1, "B")]):
+        adm.arrive(_req(i, f, c))
+    fits = _fits({"A": 8, "B": 8})
+    b1 = adm.next_batch(fits)  # 3 + 4 A frames, 2 B frames, then 5 more A frames do not fit
+    assert [r.rid for r in b1] == [0, 1, 2] and adm.free == 1
+    b2 = adm.next_batch(fits)  # no overtaking: request 3 first
+    assert [r.rid for r in b2] == [3, 4] and adm.free == 0
+    adm.arrive(_req(5, 1))
+    assert adm.next_batch(fits) == []  # no free slot
+    adm.release()
+    assert [r.rid for r in adm.next_batch(fits)] == [5]
 
 
-def test_request_too_large_for_the_budget_raises():
-    adm = Admission(budget=100, max_inflight=2, batch_overhead=10)
+def test_request_larger_than_a_slot_raises():
+    adm = Admission(slots=1)
     adm.arrive(_req(0, 50))
-    with pytest.raises(MemoryError, match="budget"):
-        adm.next_batch(lambda r: 10 * r.frames)
+    with pytest.raises(MemoryError, match="does not fit"):
+        adm.next_batch(_fits({"A": 16}))
