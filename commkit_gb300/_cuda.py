@@ -169,9 +169,10 @@ _PLANS = _PlanCache()
 
 
 def _ldpc_layered_factory(sum_product: bool = False) -> Callable:
-    """Layered LDPC decoding of ``app`` in place (the reference's ``ldpc_layered``)."""
-    if sum_product:
-        raise ValueError("ldpc_layered: sum_product=True is not implemented on sm_103a yet")
+    """Layered LDPC decoding of ``app`` in place (the reference's ``ldpc_layered``,
+    ``commkit/_cuda/coding.py:11-67``); ``sum_product`` picks the check rule as
+    its template argument does (``scale``/``offset`` then unused)."""
+    rule = _lib.CK_LDPC_SUM_PRODUCT if sum_product else _lib.CK_LDPC_MIN_SUM
 
     def launch(app: Any, row_ptr: Any, cols: Any, layer_ptr: Any, *, scale: float,
                offset: float, max_iterations: int, early_stop: bool) -> tuple[Any, Any]:  # fmt: skip
@@ -194,9 +195,9 @@ def _ldpc_layered_factory(sum_product: bool = False) -> Callable:
             return iters, valid.view(_bool(ad))
         with _device.on_device(ad):
             plan = _PLANS.get(row_ptr, cols, layer_ptr, N)
-            ws = _device.empty(ad, (plan.workspace_size(B),), np.uint8)
+            ws = _device.empty(ad, (plan.workspace_size(B, rule),), np.uint8)
             st = _lib.lib().ck_ldpc_decode(
-                plan.handle, ad.ptr, ad.ptr, B, N, _lib.CK_LDPC_MIN_SUM, float(np.float32(scale)),
+                plan.handle, ad.ptr, ad.ptr, B, N, rule, float(np.float32(scale)),
                 float(np.float32(offset)), int(max_iterations), 1 if early_stop else 0,
                 _device.wrap(iters).ptr, _device.wrap(valid).ptr, None, 0,
                 _device.wrap(ws).ptr, _device.wrap(ws).size, _device.stream_of(ad),

@@ -24,6 +24,7 @@ CK_ERR_DEVICE_TIMEOUT = 5
 CK_LLR_MAX_K = 16
 CK_LDPC_MIN_SUM = 0
 CK_LDPC_SUM_PRODUCT = 1
+CK_LDPC_SUM_PRODUCT = 1
 CK_LDPC_PLACE_AUTO = 0
 CK_LDPC_PLACE_SHARED = 1
 CK_LDPC_PLACE_GLOBAL = 2

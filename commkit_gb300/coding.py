@@ -256,10 +256,9 @@ class _Plan:
         _lib.check(_lib.lib().ck_ldpc_plan_get_launch(self.handle, ctypes.byref(cfg)), "get_launch")
         return cfg.threads_per_frame, cfg.frames_per_block, cfg.placement
 
-    def workspace_size(self, frames: int) -> int:
+    def workspace_size(self, frames: int, rule: int = _lib.CK_LDPC_MIN_SUM) -> int:
         size = ctypes.c_size_t(0)
-        st = _lib.lib().ck_ldpc_workspace_size(self.handle, int(frames), _lib.CK_LDPC_MIN_SUM,
-                                                ctypes.byref(size))  # fmt: skip
+        st = _lib.lib().ck_ldpc_workspace_size(self.handle, int(frames), int(rule), ctypes.byref(size))
         _lib.check(st, "workspace size")
         return int(size.value)
 
@@ -270,14 +269,22 @@ class _Plan:
             self.handle = None
 
 
-def _resolve_method(method: Any) -> MinSum:
+def _resolve_method(method: Any) -> MinSum | SumProduct:
     if method is None:
         return MinSum()
-    if isinstance(method, SumProduct):
-        raise NotImplementedError("decode(): SumProduct is not implemented on sm_103a yet; use MinSum")
-    if not isinstance(method, MinSum):
-        raise TypeError(f"decode(): method {type(method).__name__} does not decode LDPCCode; use MinSum.")
+    if not isinstance(method, (MinSum, SumProduct)):
+        raise TypeError(
+            f"decode(): method {type(method).__name__} does not decode LDPCCode; use MinSum or SumProduct."
+        )
     return method
+
+
+def _rule_args(method: MinSum | SumProduct) -> tuple[int, np.float32, np.float32]:
+    """(rule, scale, offset) of the C ABI; sum-product has neither parameter
+    (``commkit/coding/ldpc.py:547-549`` passes 1 and 0)."""
+    if isinstance(method, SumProduct):
+        return _lib.CK_LDPC_SUM_PRODUCT, np.float32(1.0), np.float32(0.0)
+    return _lib.CK_LDPC_MIN_SUM, np.float32(method.scale), np.float32(method.offset)
 
 
 def _as_llrs(llrs: Any, x: _device.DeviceArray):
@@ -305,7 +312,7 @@ def _as_llrs(llrs: Any, x: _device.DeviceArray):
     return t.to(torch.float32).contiguous()
 
 
-def decode(llrs: Any, *, code: LDPCCode, method: MinSum | None = None,
+def decode(llrs: Any, *, code: LDPCCode, method: MinSum | SumProduct | None = None,
            workspace: Any = None) -> DecodeResult:  # fmt: skip
     """Decode LLRs of a code's transmitted bits (``commkit/coding/base.py:317-379``).
 
@@ -314,7 +321,7 @@ def decode(llrs: Any, *, code: LDPCCode, method: MinSum | None = None,
     a-posteriori llrs float32 ``(..., B n)``, valid bool ``(..., B)`` and
     iterations int32 ``(..., B)``, all on the input's device.
     ``workspace``: optional device scratch (uint8) reused across calls, at
-    least ``code._plan(dev).workspace_size(B)`` bytes.
+    least ``code._plan(dev).workspace_size(B, rule)`` bytes.
     """
     if not isinstance(code, LDPCCode):
         raise TypeError(f"decode(): code must be an LDPCCode, got {type(code).__name__}.")
@@ -345,14 +352,15 @@ def decode(llrs: Any, *, code: LDPCCode, method: MinSum | None = None,
             plan = code._plan(xd.device)
             stream = _device.stream_of(xd)
             ws_ptr, ws_bytes = 0, 0
+            rule, scale, offset = _rule_args(method)
             if workspace is None:
-                need = plan.workspace_size(rows)
+                need = plan.workspace_size(rows, rule)
                 workspace = _device.empty(xd, (need,), np.uint8)
             wsd = _device.wrap(workspace, "workspace")
             ws_ptr, ws_bytes = wsd.ptr, wsd.size
             st = _lib.lib().ck_ldpc_decode(
                 plan.handle, xd.ptr, _device.wrap(out_llrs).ptr, rows, code.n,
-                _lib.CK_LDPC_MIN_SUM, np.float32(method.scale), np.float32(method.offset),
+                rule, scale, offset,
                 int(method.max_iterations), 1 if method.early_stop else 0,
                 _device.wrap(iters).ptr, _device.wrap(valid_u8).ptr, _device.wrap(bits).ptr, k,
                 ws_ptr, ws_bytes, stream,
@@ -392,6 +400,9 @@ def decode_mixed(batches, *, workspace: Any = None, outputs: list | None = None)
         if not isinstance(code, LDPCCode):
             raise TypeError(f"decode_mixed(): code must be an LDPCCode, got {type(code).__name__}.")
         method = _resolve_method(method)
+        if not isinstance(method, MinSum):
+            raise NotImplementedError("decode_mixed(): mixed launches decode with MinSum; decode "
+                                      "SumProduct batches with decode()")  # fmt: skip
         x0 = _device.wrap(llrs, "llrs")
         x = _as_llrs(llrs, x0).reshape(-1)
         if x.shape[0] % code.n:

@@ -42,61 +42,12 @@
 
 #include <algorithm>
 
-#include "ck_ldpc_internal.h"
+#include "ck_ldpc_kernel.cuh"
+
+
+using namespace ck::ldpc;
 
 namespace {
-
-struct Params {
-    // frames
-    const float* llr_in;
-    float* llr_out;
-    uint32_t B;
-    int32_t n_in;
-    int32_t* iters;
-    uint8_t* valid;
-    int8_t* bits;
-    int32_t k_bits;
-    // code
-    int32_t N, m, L;
-    int32_t Z, mb, nnzb;
-    ck::FastDiv divZ;
-    int32_t Zp;       // QC: row slots per base row, Z rounded up to a multiple of 32
-    int32_t q_bstep;  // QC: base-row stride of a thread (T / Zp when T >= Zp, else 1)
-    const int32_t* layer;  // QC: base rows per layer; CSR: rows per layer (L + 1)
-    const int32_t* eptr;   // QC: circulants per base row (mb + 1); CSR: row_ptr (m + 1)
-    const int2* blk;       // QC: (j Z, shift) per circulant
-    const int32_t* cols;   // CSR: column per edge
-    // method
-    float scale, offset;
-    int32_t max_iterations;
-    int32_t early_stop;
-    // launch
-    int32_t T;  // threads per frame group
-    int32_t G;  // frame groups per block
-    uint32_t tables_bytes, group_bytes, app_off, r_off, r_stride, gblk_off;
-    int32_t bulk_load;  // 1: stage the LLRs with one bulk copy
-    // workspace
-    uint32_t* counter;
-    uint32_t* status;
-    uint32_t* g_r;  // R-state slots in device memory (3 arrays of r_stride words per slot)
-    float* g_app;  // posterior slots in device memory (N per slot)
-    int32_t app_stride;
-};
-
-__device__ __forceinline__ float flip_sign(float v, uint32_t bit) {
-    return __uint_as_float(__float_as_uint(v) ^ (bit << 31));
-}
-
-// Shared-memory load and store at a 32-bit shared address (volatile: their
-// order against each other and the barriers stays as written).
-__device__ __forceinline__ float ld_shared_f32(uint32_t addr) {
-    float v;
-    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
-    return v;
-}
-__device__ __forceinline__ void st_shared_f32(uint32_t addr, float v) {
-    asm volatile("st.shared.f32 [%0], %1;" ::"r"(addr), "f"(v));
-}
 
 // One check row, min-sum: reads the row's compressed state (m1, m2, w),
 // updates the posterior `a` of its deg variables (columns from col_of) and
@@ -229,186 +180,25 @@ __device__ __forceinline__ void qc_row(const int2* __restrict__ gblk, const int 
     }
 }
 
-// Columns of row r of a circulant base row: j Z + (r + shift) mod Z, from
-// the table entry (j Z + shift, (j + 1) Z).
-struct QcCols {
-    const int2* blk;
-    int32_t r, Z;
-    __device__ __forceinline__ int operator()(int e) const {
-        const int2 b = blk[e];
-        const int c = r + b.x;
-        return c >= b.y ? c - Z : c;
-    }
-};
+// Min-sum check-message state of a frame slot: per row (min1', min2', one
+// word of signs and argmin).  In shared memory one 16-byte record per row
+// (one vector access); in device memory three arrays of 4 bytes, so the
+// resident frames' state (code C: 304 frames x 17664 rows x 12 B = 64 MB)
+// stays in L2.
+template <bool R_SMEM>
+struct MinSumState {
+    uint4* rs;
+    uint32_t* g1;
+    uint32_t* g2;
+    uint32_t* g3;
 
-struct CsrCols {
-    const int32_t* cols;
-    __device__ __forceinline__ int operator()(int e) const { return __ldg(cols + e); }
-};
+    __device__ __forceinline__ MinSumState(const Params& p, unsigned char* gbase, uint32_t slot)
+        : rs(reinterpret_cast<uint4*>(gbase + p.r_off)),
+          g1(p.g_r + static_cast<size_t>(slot) * 3 * p.r_stride),
+          g2(g1 + p.r_stride),
+          g3(g2 + p.r_stride) {}
 
-// Row `row` (schedule order) of the code: its degree and column functor.
-template <bool QC>
-struct RowOf;
-template <>
-struct RowOf<true> {
-    __device__ __forceinline__ static QcCols get(const Params& p, const int32_t* s_eptr,
-                                                 const int2* s_blk, uint32_t row, int& deg) {
-        const uint32_t b = p.divZ.div(row);
-        const int32_t r = static_cast<int32_t>(row - b * static_cast<uint32_t>(p.Z));
-        const int32_t e0 = s_eptr[b];
-        deg = s_eptr[b + 1] - e0;
-        return QcCols{s_blk + e0, r, p.Z};
-    }
-};
-template <>
-struct RowOf<false> {
-    __device__ __forceinline__ static CsrCols get(const Params& p, const int32_t*, const int2*,
-                                                  uint32_t row, int& deg) {
-        const int32_t e0 = __ldg(p.eptr + row);
-        deg = __ldg(p.eptr + row + 1) - e0;
-        return CsrCols{p.cols + e0};
-    }
-};
-
-// True in every thread of the group when every check is satisfied by the
-// hard decisions of `a` (commkit/_cuda/src/ldpc.cu:94-105).  Rows go in
-// chunks of T; the first chunk with an unsatisfied row ends the test.
-template <bool QC>
-__device__ __forceinline__ bool syndrome_ok(const Params& p, const float* a, const int32_t* s_eptr,
-                                            const int2* s_blk, int tid, int bar, int32_t qr0,
-                                            int32_t qb0) {
-    if (QC) {
-        // Rounds of T row slots, each covering whole warps of one base row
-        // (the thread's rows as in the layer loop); an OR per round.
-        const int32_t rounds = (p.mb + p.q_bstep - 1) / p.q_bstep;
-        for (int32_t k = 0; k < rounds; ++k) {
-            const int32_t b = k * p.q_bstep + qb0;
-            for (int32_t r = qr0; r - qr0 < p.Zp; r += p.T) {
-                uint32_t parity = 0;
-                if (b < p.mb && r < p.Z) {
-                    const int32_t e0 = s_eptr[b];
-                    const int deg = s_eptr[b + 1] - e0;
-                    const QcCols col_of{s_blk + e0, r, p.Z};
-                    for (int e = 0; e < deg; ++e) parity ^= a[col_of(e)] < 0.0f ? 1u : 0u;
-                }
-                if (ck::group_any(static_cast<int>(parity), bar, p.T)) return false;
-            }
-        }
-        return true;
-    }
-    for (int32_t base = 0; base < p.m; base += p.T) {
-        const int32_t row = base + tid;
-        uint32_t parity = 0;
-        if (row < p.m) {
-            int deg;
-            const auto col_of = RowOf<QC>::get(p, s_eptr, s_blk, static_cast<uint32_t>(row), deg);
-            for (int e = 0; e < deg; ++e) parity ^= a[col_of(e)] < 0.0f ? 1u : 0u;
-        }
-        if (ck::group_any(static_cast<int>(parity), bar, p.T)) return false;
-    }
-    return true;
-}
-
-// Threads per block the kernels are built for (registers scale inversely).
-__host__ __device__ constexpr int max_block_threads(bool qc, int dmax) {
-    return dmax > 16 ? 512 : (qc ? 768 : 1024);
-}
-
-template <bool QC, int DMAX, bool APP_SMEM, bool R_SMEM>
-__global__ void __launch_bounds__(max_block_threads(QC, DMAX))
-    ldpc_decode_kernel(const __grid_constant__ Params p) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    using ck::group_any;
-    using ck::group_sync;
-
-    // Tables: layer pointers, then (QC) circulants per base row and the
-    // circulants themselves.
-    int32_t* s_layer = reinterpret_cast<int32_t*>(smem);
-    int32_t* s_eptr = s_layer + (p.L + 1);
-    int2* s_blk = reinterpret_cast<int2*>(smem + ((static_cast<uint32_t>(p.L + 1 + p.mb + 1) * 4 + 7) & ~7u));
-    for (int i = threadIdx.x; i <= p.L; i += blockDim.x) s_layer[i] = p.layer[i];
-    if (QC) {
-        for (int i = threadIdx.x; i <= p.mb; i += blockDim.x) s_eptr[i] = p.eptr[i];
-        for (int i = threadIdx.x; i < p.nnzb; i += blockDim.x) s_blk[i] = p.blk[i];
-    }
-
-    const int g = threadIdx.x / p.T;
-    const int tid = threadIdx.x - g * p.T;
-    const int bar = g + 1;
-    // Circulant rows of this thread: row qr0 (+ T, + 2T, ... when T < Zp) of
-    // base rows qb0, qb0 + q_bstep, ...  Zp and T are multiples of 32 and one
-    // divides the other, so a warp's lanes always share their base row.
-    const int32_t qr0 = QC ? (p.T >= p.Zp ? tid % p.Zp : tid) : 0;
-    const int32_t qb0 = QC ? (p.T >= p.Zp ? tid / p.Zp : 0) : 0;
-    const uint32_t slot = blockIdx.x * static_cast<uint32_t>(p.G) + static_cast<uint32_t>(g);
-    unsigned char* gbase = smem + p.tables_bytes + static_cast<uint32_t>(g) * p.group_bytes;
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(gbase);
-    volatile uint32_t* s_frame = reinterpret_cast<volatile uint32_t*>(gbase + 8);
-    float* a = APP_SMEM ? reinterpret_cast<float*>(gbase + p.app_off)
-                        : p.g_app + static_cast<size_t>(slot) * p.app_stride;
-    // Check-message state of a row: (min1', min2', signs and argmin).  In
-    // shared memory one 16-byte record per row (one vector access); in device
-    // memory three arrays of 4 bytes, so the resident frames' state (code C:
-    // 304 frames x 17664 rows x 12 B = 64 MB) stays in L2.
-    uint4* rs = reinterpret_cast<uint4*>(gbase + p.r_off);
-    uint32_t* g1 = p.g_r + static_cast<size_t>(slot) * 3 * p.r_stride;
-    uint32_t* g2 = g1 + p.r_stride;
-    uint32_t* g3 = g2 + p.r_stride;
-    // This group's copy of the circulant table as shared addresses into `a`.
-    int2* gblk = reinterpret_cast<int2*>(gbase + p.gblk_off);
-
-    if (tid == 0) {
-        ck::mbar_init(mbar, 1);
-        ck::fence_mbar_init();
-    }
-    __syncthreads();
-    if (QC) {
-        const uint32_t a_addr = ck::smem_addr(a);
-        for (int i = tid; i < p.nnzb; i += p.T)
-            gblk[i] = make_int2(static_cast<int>(a_addr + 4u * static_cast<uint32_t>(s_blk[i].x)),
-                                static_cast<int>(a_addr + 4u * static_cast<uint32_t>(s_blk[i].y)));
-    }
-    const uint32_t r4 = 4u * static_cast<uint32_t>(qr0);
-    const uint32_t Z4 = 4u * static_cast<uint32_t>(p.Z);
-
-    uint32_t phase = 0;
-    for (;;) {
-        if (tid == 0) *s_frame = atomicAdd(p.counter, 1u);
-        group_sync(bar, p.T);
-        const uint32_t f = *s_frame;
-        if (f >= p.B) break;
-        const float* src = p.llr_in + static_cast<size_t>(f) * p.n_in;
-
-        // Stage the frame's channel LLRs; punctured variables start at 0.
-        bool loaded = true;
-        if (APP_SMEM && p.bulk_load) {
-            if (tid == 0) {
-                ck::fence_proxy_async_smem();
-                ck::mbar_arrive_expect_tx(mbar, static_cast<uint32_t>(p.n_in) * 4u);
-                ck::bulk_g2s(a, src, static_cast<uint32_t>(p.n_in) * 4u, mbar);
-            }
-            for (int i = p.n_in + tid; i < p.N; i += p.T) a[i] = 0.0f;
-            loaded = ck::mbar_wait(mbar, phase);
-            phase ^= 1u;
-            // x + 0 turns -0 into +0 and keeps every other value: the decoder
-            // then never meets -0 (see qc_row_fixed).
-            if (loaded)
-                for (int i = tid; i < p.n_in; i += p.T) a[i] = __fadd_rn(a[i], 0.0f);
-        } else {
-            for (int i = tid; i < p.n_in; i += p.T) a[i] = __fadd_rn(__ldcs(src + i), 0.0f);
-            for (int i = p.n_in + tid; i < p.N; i += p.T) a[i] = 0.0f;
-        }
-        if (group_any(loaded ? 0 : 1, bar, p.T)) {
-            // A bulk copy did not complete in time: report and stop this
-            // group after a last bounded wait for the copy in flight.
-            if (tid == 0) {
-                atomicOr(p.status, ck::kStatusTimeout);
-                p.iters[f] = -1;
-                p.valid[f] = 0;
-            }
-            (void)ck::mbar_wait(mbar, phase ^ 1u);
-            return;
-        }
+    __device__ __forceinline__ void zero(const Params& p, int tid) const {
         for (int i = tid; i < p.m; i += p.T) {
             if (R_SMEM) {
                 rs[i] = make_uint4(0u, 0u, 0u, 0u);
@@ -418,79 +208,62 @@ __global__ void __launch_bounds__(max_block_threads(QC, DMAX))
                 g3[i] = 0u;
             }
         }
-        group_sync(bar, p.T);
-
-        int32_t it = 0;
-        bool ok = p.early_stop && syndrome_ok<QC>(p, a, s_eptr, s_blk, tid, bar, qr0, qb0);
-        while (!ok && it < p.max_iterations) {
-            for (int32_t l = 0; l < p.L && QC; ++l) {
-                const int32_t b1 = s_layer[l + 1];
-                for (int32_t b = s_layer[l] + qb0; b < b1; b += p.q_bstep) {
-                    const int32_t e0 = s_eptr[b];
-                    const int deg = s_eptr[b + 1] - e0;
-                    for (int32_t r = qr0; r - qr0 < p.Zp; r += p.T) {
-                        if (r >= p.Z) continue;  // padding lanes when Z % 32 != 0
-                        const uint32_t row = static_cast<uint32_t>(b) * static_cast<uint32_t>(p.Z) +
-                                             static_cast<uint32_t>(r);
-                        const uint4 st = R_SMEM ? rs[row]
-                                                : make_uint4(__ldcg(g1 + row), __ldcg(g2 + row),
-                                                             __ldcg(g3 + row), 0u);
-                        float m1 = __uint_as_float(st.x), m2 = __uint_as_float(st.y);
-                        uint32_t w = st.z;
-                        qc_row<DMAX>(gblk + e0, deg, r4 + 4u * static_cast<uint32_t>(r - qr0), Z4, m1,
-                                     m2, w, p.scale, p.offset);
-                        if (R_SMEM) {
-                            rs[row] = make_uint4(__float_as_uint(m1), __float_as_uint(m2), w, 0u);
-                        } else {
-                            __stcg(g1 + row, __float_as_uint(m1));
-                            __stcg(g2 + row, __float_as_uint(m2));
-                            __stcg(g3 + row, w);
-                        }
-                    }
-                }
-                group_sync(bar, p.T);
-            }
-            for (int32_t l = 0; l < p.L && !QC; ++l) {
-                const uint32_t row0 = s_layer[l];
-                const uint32_t row1 = s_layer[l + 1];
-                for (uint32_t row = row0 + tid; row < row1; row += p.T) {
-                    int deg;
-                    const auto col_of = RowOf<QC>::get(p, s_eptr, s_blk, row, deg);
-                    const uint4 st = R_SMEM ? rs[row]
-                                            : make_uint4(__ldcg(g1 + row), __ldcg(g2 + row),
-                                                         __ldcg(g3 + row), 0u);
-                    float m1 = __uint_as_float(st.x), m2 = __uint_as_float(st.y);
-                    uint32_t w = st.z;
-                    min_sum_row<DMAX>(a, deg, col_of, m1, m2, w, p.scale, p.offset);
-                    if (R_SMEM) {
-                        rs[row] = make_uint4(__float_as_uint(m1), __float_as_uint(m2), w, 0u);
-                    } else {
-                        __stcg(g1 + row, __float_as_uint(m1));
-                        __stcg(g2 + row, __float_as_uint(m2));
-                        __stcg(g3 + row, w);
-                    }
-                }
-                group_sync(bar, p.T);
-            }
-            ++it;
-            if (p.early_stop) ok = syndrome_ok<QC>(p, a, s_eptr, s_blk, tid, bar, qr0, qb0);
-        }
-        if (!p.early_stop) ok = syndrome_ok<QC>(p, a, s_eptr, s_blk, tid, bar, qr0, qb0);
-
-        float* dst = p.llr_out + static_cast<size_t>(f) * p.n_in;
-        for (int i = tid; i < p.n_in; i += p.T) __stcs(dst + i, a[i]);
-        if (p.bits) {
-            int8_t* bdst = p.bits + static_cast<size_t>(f) * p.k_bits;
-            for (int i = tid; i < p.k_bits; i += p.T) bdst[i] = a[i] < 0.0f ? 1 : 0;
-        }
-        if (tid == 0) {
-            p.iters[f] = it;
-            p.valid[f] = ok ? 1 : 0;
-        }
-        // Everyone has read `a` before the next frame overwrites it.
-        group_sync(bar, p.T);
     }
+    __device__ __forceinline__ uint4 load(uint32_t row) const {
+        return R_SMEM ? rs[row] : make_uint4(__ldcg(g1 + row), __ldcg(g2 + row), __ldcg(g3 + row), 0u);
+    }
+    __device__ __forceinline__ void store(uint32_t row, float m1, float m2, uint32_t w) const {
+        if (R_SMEM) {
+            rs[row] = make_uint4(__float_as_uint(m1), __float_as_uint(m2), w, 0u);
+        } else {
+            __stcg(g1 + row, __float_as_uint(m1));
+            __stcg(g2 + row, __float_as_uint(m2));
+            __stcg(g3 + row, w);
+        }
+    }
+    template <int DMAX>
+    __device__ __forceinline__ void qc_row(const Params& p, const int2* gblk, int deg, uint32_t row,
+                                           int32_t, int32_t, uint32_t r4, uint32_t Z4) const {
+        const uint4 s = load(row);
+        float m1 = __uint_as_float(s.x), m2 = __uint_as_float(s.y);
+        uint32_t w = s.z;
+        ::qc_row<DMAX>(gblk, deg, r4, Z4, m1, m2, w, p.scale, p.offset);
+        store(row, m1, m2, w);
+    }
+    template <int DMAX, class ColOf>
+    __device__ __forceinline__ void csr_row(const Params& p, float* a, uint32_t row, int deg, int32_t,
+                                            const ColOf& col_of) const {
+        const uint4 s = load(row);
+        float m1 = __uint_as_float(s.x), m2 = __uint_as_float(s.y);
+        uint32_t w = s.z;
+        min_sum_row<DMAX>(a, deg, col_of, m1, m2, w, p.scale, p.offset);
+        store(row, m1, m2, w);
+    }
+};
+
+}  // namespace
+
+namespace ck {
+namespace ldpc {
+
+struct MinSumPick {
+    template <bool QC, int DMAX>
+    static KernelFn get(bool app_smem, bool r_smem) {
+        if (app_smem && r_smem) return decode_kernel<MinSumState, QC, DMAX, true, true>;
+        if (app_smem) return decode_kernel<MinSumState, QC, DMAX, true, false>;
+        if constexpr (!QC) return decode_kernel<MinSumState, QC, DMAX, false, false>;
+        return nullptr;
+    }
+};
+
+KernelFn min_sum_kernel(bool qc, int dmax, bool app_smem, bool r_smem) {
+    return pick_shape<MinSumPick>(qc, dmax, app_smem, r_smem);
 }
+
+}  // namespace ldpc
+}  // namespace ck
+
+namespace {
 
 // ---------------------------------------------------------------------------
 // Mixed-code persistent kernel: frames of several quasi-cyclic codes in one
@@ -699,28 +472,7 @@ __global__ void __launch_bounds__(kMixedThreads) ldpc_mixed_kernel(const __grid_
     }
 }
 
-using KernelFn = void (*)(Params);
 using KernelMixed = void (*)(MixedParams);
-
-template <bool QC, int DMAX>
-KernelFn pick_placement(bool app_smem, bool r_smem) {
-    if (app_smem && r_smem) return ldpc_decode_kernel<QC, DMAX, true, true>;
-    if (app_smem) return ldpc_decode_kernel<QC, DMAX, true, false>;
-    if constexpr (QC) {
-        return nullptr;  // circulant rows address the posterior in shared memory
-    } else {
-        return ldpc_decode_kernel<QC, DMAX, false, false>;
-    }
-}
-
-template <bool QC>
-KernelFn pick_degree(int dmax, bool app_smem, bool r_smem) {
-    if constexpr (!QC) {
-        if (dmax <= 8) return pick_placement<QC, 8>(app_smem, r_smem);
-    }
-    if (dmax <= 16) return pick_placement<QC, 16>(app_smem, r_smem);
-    return pick_placement<QC, 27>(app_smem, r_smem);
-}
 
 uint32_t align_up(uint32_t v, uint32_t a) { return (v + a - 1) / a * a; }
 
@@ -731,6 +483,7 @@ struct Resolved {
     uint32_t tables_bytes, group_bytes, gblk_off, app_off, r_off, r_stride, smem;
     int32_t app_stride;
     int grid;
+    size_t r_slot_bytes;  // message state of one frame slot in device memory (0 in shared)
     size_t ws_bytes, r_ws_off, app_ws_off;
 };
 
@@ -743,8 +496,12 @@ int device_limits(int dev, int* sms, int* smem_optin) {
 }
 
 // Launch shape, shared-memory layout, grid and workspace of a decode of B
-// frames; a pure function of the plan, its launch setting and B.
-int resolve(const ck_ldpc_plan* plan, int64_t B, Resolved* r) {
+// frames by `rule`; a pure function of the plan, its launch setting, the
+// rule and B.
+int resolve(const ck_ldpc_plan* plan, int32_t rule, int64_t B, Resolved* r) {
+    if (rule != CK_LDPC_MIN_SUM && rule != CK_LDPC_SUM_PRODUCT)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "unknown check rule %d", rule);
+    const bool sp = rule == CK_LDPC_SUM_PRODUCT;
     int sms = 0, optin = 0;
     CK_TRY(device_limits(plan->device, &sms, &optin));
     const uint32_t tables =
@@ -754,9 +511,12 @@ int resolve(const ck_ldpc_plan* plan, int64_t B, Resolved* r) {
                  : align_up(static_cast<uint32_t>(plan->L + 1) * 4, 128);
     const uint32_t ctrl = 128;
     const uint32_t app_bytes = align_up(static_cast<uint32_t>(plan->N) * 4, 128);
-    const uint32_t r_stride = align_up(static_cast<uint32_t>(plan->m), 32);
-    const uint32_t r_bytes = r_stride * 16;       // in shared memory
-    const uint32_t r_bytes_dev = r_stride * 12;   // in device memory
+    // Message state per frame: min-sum keeps a 16-byte record per row in
+    // shared memory (12 bytes in device memory), sum-product one float per
+    // edge in either.
+    const uint32_t r_stride = align_up(static_cast<uint32_t>(sp ? plan->E : plan->m), 32);
+    const uint32_t r_bytes = r_stride * (sp ? 4 : 16);      // in shared memory
+    const uint32_t r_bytes_dev = r_stride * (sp ? 4 : 12);  // in device memory
     // Per group: its copy of the circulant table with shared addresses.
     const uint32_t gblk_bytes = plan->qc ? align_up(static_cast<uint32_t>(plan->nnzb) * 8, 128) : 0;
     const uint32_t budget = static_cast<uint32_t>(optin) > tables ? optin - tables : 0;
@@ -768,7 +528,10 @@ int resolve(const ck_ldpc_plan* plan, int64_t B, Resolved* r) {
                         "memory",
                         plan->N, app_bytes);
     bool r_smem;
-    const int32_t place = plan->launch.placement;
+    // A plan's frames per block and placement are min-sum shapes (tuned or
+    // set); sum-product, whose per-edge state is several times larger,
+    // always picks its own.
+    const int32_t place = sp ? CK_LDPC_PLACE_AUTO : plan->launch.placement;
     if (!app_smem || place == CK_LDPC_PLACE_GLOBAL) {
         r_smem = false;
     } else if (place == CK_LDPC_PLACE_SHARED) {
@@ -803,7 +566,7 @@ int resolve(const ck_ldpc_plan* plan, int64_t B, Resolved* r) {
         return ck::fail(CK_ERR_INVALID_ARGUMENT,
                         "threads_per_frame %d above %d for row degree %d", T, max_threads,
                         plan->max_deg);
-    int32_t G = plan->launch.frames_per_block;
+    int32_t G = sp ? 0 : plan->launch.frames_per_block;
     const int32_t gmax_threads = max_threads / T;
     const int32_t gmax_smem = static_cast<int32_t>(budget / group);
     const int32_t gmax_bar = T > 32 ? ck::kMaxNamedGroups : 32;
@@ -811,8 +574,9 @@ int resolve(const ck_ldpc_plan* plan, int64_t B, Resolved* r) {
     if (gmax < 1)
         return ck::fail(CK_ERR_UNSUPPORTED, "a frame needs %u bytes of shared memory, %u available",
                         group, budget);
-    KernelFn kernel = plan->qc ? pick_degree<true>(plan->max_deg, app_smem, r_smem)
-                               : pick_degree<false>(plan->max_deg, app_smem, r_smem);
+    KernelFn kernel = sp ? sum_product_kernel(plan->qc, plan->max_deg, app_smem, r_smem)
+                         : min_sum_kernel(plan->qc, plan->max_deg, app_smem, r_smem);
+    if (!kernel) return ck::fail(CK_ERR_UNSUPPORTED, "no decoder kernel for this code shape");
     if (G == 0) {
         // The most resident frames per SM (registers, shared memory, threads),
         // the smaller block on a tie.
@@ -864,8 +628,9 @@ int resolve(const ck_ldpc_plan* plan, int64_t B, Resolved* r) {
     const int64_t need = (B + G - 1) / G;
     r->grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(need, int64_t(sms) * per_sm)));
     const size_t slots = static_cast<size_t>(r->grid) * G;
+    r->r_slot_bytes = r_smem ? 0 : r_bytes_dev;
     r->r_ws_off = kHeaderBytes;
-    const size_t r_ws = r_smem ? 0 : slots * r_bytes_dev;
+    const size_t r_ws = slots * r->r_slot_bytes;
     r->app_ws_off = kHeaderBytes + ((r_ws + 255) / 256) * 256;
     const size_t app_ws = app_smem ? 0 : slots * app_bytes;
     r->ws_bytes = r->app_ws_off + app_ws;
@@ -881,31 +646,15 @@ int check_device(const ck_ldpc_plan* plan) {
     return CK_OK;
 }
 
-}  // namespace
-
-extern "C" int ck_ldpc_workspace_size(const ck_ldpc_plan* plan, int64_t B, int32_t rule,
-                                      size_t* bytes) {
-    ck::clear_error();
-    if (!plan || !bytes) return ck::fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (rule != CK_LDPC_MIN_SUM)
-        return ck::fail(CK_ERR_UNSUPPORTED, "only the min-sum rule is implemented");
-    if (B < 0) return ck::fail(CK_ERR_INVALID_ARGUMENT, "B must be >= 0");
-    CK_TRY(check_device(plan));
-    Resolved r;
-    CK_TRY(resolve(plan, std::max<int64_t>(B, 1), &r));
-    *bytes = r.ws_bytes;
-    return CK_OK;
-}
-
-extern "C" int ck_ldpc_decode(const ck_ldpc_plan* plan, const float* llr_in, float* llr_out,
-                              int64_t B, int32_t n_in, int32_t rule, float scale, float offset,
-                              int32_t max_iterations, int32_t early_stop, int32_t* iters,
-                              uint8_t* valid, int8_t* bits, int32_t k_bits, void* workspace,
-                              size_t workspace_bytes, void* stream) {
-    ck::clear_error();
+// Argument checks shared by the decode entry points (the reference's
+// wrapper checks, commkit/_cuda/coding.py:27-67, plus this ABI's own).
+int check_decode_args(const ck_ldpc_plan* plan, const float* llr_in, const float* llr_out,
+                      int64_t B, int32_t n_in, int32_t rule, int32_t max_iterations,
+                      const int32_t* iters, const uint8_t* valid, const int8_t* bits,
+                      int32_t k_bits) {
     if (!plan) return ck::fail(CK_ERR_INVALID_ARGUMENT, "plan is NULL");
-    if (rule != CK_LDPC_MIN_SUM)
-        return ck::fail(CK_ERR_UNSUPPORTED, "only the min-sum rule is implemented");
+    if (rule != CK_LDPC_MIN_SUM && rule != CK_LDPC_SUM_PRODUCT)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "unknown check rule %d", rule);
     if (B < 0 || B >= (int64_t(1) << 31))
         return ck::fail(CK_ERR_INVALID_ARGUMENT, "B must be in [0, 2**31), got %lld",
                         static_cast<long long>(B));
@@ -921,25 +670,14 @@ extern "C" int ck_ldpc_decode(const ck_ldpc_plan* plan, const float* llr_in, flo
         return ck::fail(CK_ERR_INVALID_ARGUMENT, "llr_in, llr_out, iters and valid are required");
     if (reinterpret_cast<uintptr_t>(llr_in) % 4 || reinterpret_cast<uintptr_t>(llr_out) % 4)
         return ck::fail(CK_ERR_INVALID_ARGUMENT, "LLR buffers must be 4-byte aligned");
-    CK_TRY(check_device(plan));
-    Resolved r;
-    CK_TRY(resolve(plan, B, &r));
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    void* ws = workspace;
-    bool owned = false;
-    if (ws == nullptr) {
-        CK_CUDA(cudaMallocAsync(&ws, r.ws_bytes, s));
-        owned = true;
-    } else {
-        if (workspace_bytes < r.ws_bytes)
-            return ck::fail(CK_ERR_INVALID_ARGUMENT, "workspace of %zu bytes, %zu needed",
-                            workspace_bytes, r.ws_bytes);
-        if (reinterpret_cast<uintptr_t>(ws) % 256)
-            return ck::fail(CK_ERR_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
-    }
-    unsigned char* wsb = static_cast<unsigned char*>(ws);
-    int status = ck::cuda_check(cudaMemsetAsync(wsb, 0, kHeaderBytes, s), "cudaMemsetAsync");
+    return CK_OK;
+}
 
+// Kernel parameters of a resolved decode over the workspace `wsb`.
+Params make_params(const ck_ldpc_plan* plan, const Resolved& r, const float* llr_in, float* llr_out,
+                   int64_t B, int32_t n_in, float scale, float offset, int32_t max_iterations,
+                   int32_t early_stop, int32_t* iters, uint8_t* valid, int8_t* bits,
+                   int32_t k_bits, unsigned char* wsb) {
     Params p;
     p.llr_in = llr_in;
     p.llr_out = llr_out;
@@ -952,6 +690,7 @@ extern "C" int ck_ldpc_decode(const ck_ldpc_plan* plan, const float* llr_in, flo
     p.N = plan->N;
     p.m = plan->m;
     p.L = plan->L;
+    p.E = plan->E;
     p.Z = plan->qc ? plan->Z : 1;
     p.mb = plan->qc ? plan->mb : 0;
     p.nnzb = plan->qc ? plan->nnzb : 0;
@@ -983,6 +722,52 @@ extern "C" int ck_ldpc_decode(const ck_ldpc_plan* plan, const float* llr_in, flo
     p.g_r = reinterpret_cast<uint32_t*>(wsb + r.r_ws_off);
     p.g_app = reinterpret_cast<float*>(wsb + r.app_ws_off);
     p.app_stride = r.app_stride;
+    return p;
+}
+
+}  // namespace
+
+extern "C" int ck_ldpc_workspace_size(const ck_ldpc_plan* plan, int64_t B, int32_t rule,
+                                      size_t* bytes) {
+    ck::clear_error();
+    if (!plan || !bytes) return ck::fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (B < 0) return ck::fail(CK_ERR_INVALID_ARGUMENT, "B must be >= 0");
+    CK_TRY(check_device(plan));
+    Resolved r;
+    CK_TRY(resolve(plan, rule, std::max<int64_t>(B, 1), &r));
+    *bytes = r.ws_bytes;
+    return CK_OK;
+}
+
+extern "C" int ck_ldpc_decode(const ck_ldpc_plan* plan, const float* llr_in, float* llr_out,
+                              int64_t B, int32_t n_in, int32_t rule, float scale, float offset,
+                              int32_t max_iterations, int32_t early_stop, int32_t* iters,
+                              uint8_t* valid, int8_t* bits, int32_t k_bits, void* workspace,
+                              size_t workspace_bytes, void* stream) {
+    ck::clear_error();
+    CK_TRY(check_decode_args(plan, llr_in, llr_out, B, n_in, rule, max_iterations, iters, valid,
+                             bits, k_bits));
+    if (B == 0) return CK_OK;
+    CK_TRY(check_device(plan));
+    Resolved r;
+    CK_TRY(resolve(plan, rule, B, &r));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    void* ws = workspace;
+    bool owned = false;
+    if (ws == nullptr) {
+        CK_CUDA(cudaMallocAsync(&ws, r.ws_bytes, s));
+        owned = true;
+    } else {
+        if (workspace_bytes < r.ws_bytes)
+            return ck::fail(CK_ERR_INVALID_ARGUMENT, "workspace of %zu bytes, %zu needed",
+                            workspace_bytes, r.ws_bytes);
+        if (reinterpret_cast<uintptr_t>(ws) % 256)
+            return ck::fail(CK_ERR_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
+    }
+    unsigned char* wsb = static_cast<unsigned char*>(ws);
+    int status = ck::cuda_check(cudaMemsetAsync(wsb, 0, kHeaderBytes, s), "cudaMemsetAsync");
+    const Params p = make_params(plan, r, llr_in, llr_out, B, n_in, scale, offset, max_iterations,
+                                 early_stop, iters, valid, bits, k_bits, wsb);
     if (status == CK_OK) {
         r.kernel<<<r.grid, r.T * r.G, r.smem, s>>>(p);
         status = ck::cuda_check(cudaGetLastError(), "decoder launch");
@@ -1014,34 +799,21 @@ extern "C" int ck_ldpc_workspace_status(const void* workspace, void* stream) {
 // in the device queue, so any B fits; a code whose one slot does not fit is
 // rejected.
 int ck::ldpc_decode_in_scratch(const ck_ldpc_plan* plan, const float* llr_in, float* llr_out,
-                               int64_t B, int32_t n_in, float scale, float offset,
+                               int64_t B, int32_t n_in, int32_t rule, float scale, float offset,
                                int32_t max_iterations, int32_t early_stop, int32_t* iters,
                                uint8_t* valid, int8_t* bits, int32_t k_bits, void* scratch,
                                size_t scratch_bytes, cudaStream_t s) {
-    if (B < 0 || B >= (int64_t(1) << 31))
-        return ck::fail(CK_ERR_INVALID_ARGUMENT, "B must be in [0, 2**31), got %lld",
-                        static_cast<long long>(B));
-    if (n_in < 1 || n_in > plan->N)
-        return ck::fail(CK_ERR_INVALID_ARGUMENT, "n_in must be in [1, N=%d], got %d", plan->N,
-                        n_in);
-    if (max_iterations < 0)
-        return ck::fail(CK_ERR_INVALID_ARGUMENT, "max_iterations must be >= 0");
-    if (bits && (k_bits < 0 || k_bits > n_in))
-        return ck::fail(CK_ERR_INVALID_ARGUMENT, "k_bits must be in [0, n_in]");
+    CK_TRY(check_decode_args(plan, llr_in, llr_out, B, n_in, rule, max_iterations, iters, valid,
+                             bits, k_bits));
     if (B == 0) return CK_OK;
-    if (!llr_in || !llr_out || !iters || !valid)
-        return ck::fail(CK_ERR_INVALID_ARGUMENT, "llr_in, llr_out, iters and valid are required");
-    if (reinterpret_cast<uintptr_t>(llr_in) % 4 || reinterpret_cast<uintptr_t>(llr_out) % 4)
-        return ck::fail(CK_ERR_INVALID_ARGUMENT, "LLR buffers must be 4-byte aligned");
     if (reinterpret_cast<uintptr_t>(scratch) % 256)
         return ck::fail(CK_ERR_INVALID_ARGUMENT, "scratch must be 256-byte aligned");
     CK_TRY(check_device(plan));
     Resolved r;
-    CK_TRY(resolve(plan, B, &r));
+    CK_TRY(resolve(plan, rule, B, &r));
     // Bytes of device-memory state per frame slot (the header is shared).
-    const size_t r_bytes = r.r_smem ? 0 : static_cast<size_t>(r.r_stride) * 12;
     const size_t app_bytes = r.app_smem ? 0 : static_cast<size_t>(r.app_stride) * 4;
-    const size_t per_slot = r_bytes + app_bytes;
+    const size_t per_slot = r.r_slot_bytes + app_bytes;
     if (per_slot > 0) {
         const size_t usable = scratch_bytes > kHeaderBytes + 256 ? scratch_bytes - kHeaderBytes - 256 : 0;
         const size_t max_slots = usable / per_slot;
@@ -1055,7 +827,7 @@ int ck::ldpc_decode_in_scratch(const ck_ldpc_plan* plan, const float* llr_in, fl
     }
     const size_t slots = static_cast<size_t>(r.grid) * r.G;
     r.r_ws_off = kHeaderBytes;
-    r.app_ws_off = kHeaderBytes + ((slots * r_bytes + 255) / 256) * 256;
+    r.app_ws_off = kHeaderBytes + ((slots * r.r_slot_bytes + 255) / 256) * 256;
     r.ws_bytes = r.app_ws_off + slots * app_bytes;
     if (r.ws_bytes > scratch_bytes)
         return ck::fail(CK_ERR_UNSUPPORTED, "decode needs %zu bytes of scratch, %zu available",
@@ -1063,54 +835,11 @@ int ck::ldpc_decode_in_scratch(const ck_ldpc_plan* plan, const float* llr_in, fl
     unsigned char* wsb = static_cast<unsigned char*>(scratch);
     // The queue counter and status word must start at zero on every call.
     CK_CUDA(cudaMemsetAsync(wsb, 0, kHeaderBytes, s));
-
-    Params p;
-    p.llr_in = llr_in;
-    p.llr_out = llr_out;
-    p.B = static_cast<uint32_t>(B);
-    p.n_in = n_in;
-    p.iters = iters;
-    p.valid = valid;
-    p.bits = k_bits > 0 ? bits : nullptr;
-    p.k_bits = k_bits;
-    p.N = plan->N;
-    p.m = plan->m;
-    p.L = plan->L;
-    p.Z = plan->qc ? plan->Z : 1;
-    p.mb = plan->qc ? plan->mb : 0;
-    p.nnzb = plan->qc ? plan->nnzb : 0;
-    p.divZ = plan->divZ;
-    p.Zp = plan->qc ? (plan->Z + 31) / 32 * 32 : 32;
-    p.q_bstep = (plan->qc && r.T >= p.Zp) ? r.T / p.Zp : 1;
-    p.layer = plan->d_layer;
-    p.eptr = plan->d_eptr;
-    p.blk = reinterpret_cast<const int2*>(plan->d_blk);
-    p.cols = plan->d_cols;
-    p.scale = scale;
-    p.offset = offset;
-    p.max_iterations = max_iterations;
-    p.early_stop = early_stop ? 1 : 0;
-    p.T = r.T;
-    p.G = r.G;
-    p.tables_bytes = r.tables_bytes;
-    p.group_bytes = r.group_bytes;
-    p.gblk_off = r.gblk_off;
-    p.app_off = r.app_off;
-    p.r_off = r.r_off;
-    p.r_stride = r.r_stride;
-    p.bulk_load = (r.app_smem && (static_cast<uint32_t>(n_in) * 4u) % 16u == 0 &&
-                   reinterpret_cast<uintptr_t>(llr_in) % 16 == 0)
-                      ? 1
-                      : 0;
-    p.counter = reinterpret_cast<uint32_t*>(wsb);
-    p.status = reinterpret_cast<uint32_t*>(wsb + 4);
-    p.g_r = reinterpret_cast<uint32_t*>(wsb + r.r_ws_off);
-    p.g_app = reinterpret_cast<float*>(wsb + r.app_ws_off);
-    p.app_stride = r.app_stride;
+    const Params p = make_params(plan, r, llr_in, llr_out, B, n_in, scale, offset, max_iterations,
+                                 early_stop, iters, valid, bits, k_bits, wsb);
     r.kernel<<<r.grid, r.T * r.G, r.smem, s>>>(p);
     return ck::cuda_check(cudaGetLastError(), "decoder launch");
 }
-
 
 // ---------------------------------------------------------------------------
 // Mixed-code launch

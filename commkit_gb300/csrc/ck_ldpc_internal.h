@@ -24,11 +24,11 @@ struct ck_ldpc_plan;
 
 namespace ck {
 
-// Min-sum decode with all device scratch taken from `scratch` (capacity
+// Decode with all device scratch taken from `scratch` (capacity
 // `scratch_bytes`, 256-byte aligned); defined in ck_ldpc.cu, used by the
 // allocation-free entry point.
 int ldpc_decode_in_scratch(const ck_ldpc_plan* plan, const float* llr_in, float* llr_out,
-                           int64_t B, int32_t n_in, float scale, float offset,
+                           int64_t B, int32_t n_in, int32_t rule, float scale, float offset,
                            int32_t max_iterations, int32_t early_stop, int32_t* iters,
                            uint8_t* valid, int8_t* bits, int32_t k_bits, void* scratch,
                            size_t scratch_bytes, cudaStream_t stream);

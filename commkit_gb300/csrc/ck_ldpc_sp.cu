@@ -1,0 +1,138 @@
+// Layered sum-product LDPC decoding on sm_103a: the check rule of the
+// reference's `ldpc_layered<true>` (commkit/_cuda/src/ldpc.cu:74-91; CPU twin
+// commkit/coding/_numba_loops.py:71-94) run by the persistent frame loop the
+// min-sum rule uses (ck_ldpc_kernel.cuh): same layers, same order, same
+// early stop.
+//
+// The check-to-variable message of edge e is
+//     sign_e * phi(sum_e' phi(|Q_e'|) - phi(|Q_e|)),   phi(x) = -log tanh(x / 2)
+// on x clipped to [1e-7, 30], with sign_e the parity of the row's Q signs
+// times Q_e's own.  Unlike min-sum a row's messages do not compress, so the
+// state is one float per edge: in shared memory beside the posterior when it
+// fits (codes of a few thousand edges), else in the frame slot's device
+// memory.  Circulant c of a quasi-cyclic code keeps the message of its row r
+// at c Z + r, so a warp's lanes (consecutive r) touch consecutive words; a
+// CSR code keeps the message of edge e at e, as the reference does.
+//
+// Arithmetic: Q = APP - R, the running total of phi values (edge by edge, in
+// column order), total - phi(|Q_e|) and APP = Q + R_new are explicit
+// round-to-nearest float32 operations in the reference's order; phi calls
+// logf and tanhf as the reference's kernel does.  Results therefore match
+// the CPU decoder up to the rounding of those two functions (the reference
+// tests its own GPU path against the CPU at 1e-3).
+#include "ck_ldpc_kernel.cuh"
+
+namespace ck {
+namespace ldpc {
+namespace sp {
+
+__device__ __forceinline__ float phi(float x) {
+    x = fminf(fmaxf(x, 1e-7f), 30.0f);
+    return -logf(tanhf(__fmul_rn(0.5f, x)));
+}
+
+template <bool R_SMEM>
+struct SumProductState {
+    float* r;  // this slot's messages
+
+    __device__ __forceinline__ SumProductState(const Params& p, unsigned char* gbase, uint32_t slot)
+        : r(R_SMEM ? reinterpret_cast<float*>(gbase + p.r_off)
+                   : reinterpret_cast<float*>(p.g_r) + static_cast<size_t>(slot) * p.r_stride) {}
+
+    __device__ __forceinline__ void zero(const Params& p, int tid) const {
+        for (int i = tid; i < p.E; i += p.T) r[i] = 0.0f;
+    }
+    __device__ __forceinline__ float ld(uint32_t i) const { return R_SMEM ? r[i] : __ldcg(r + i); }
+    __device__ __forceinline__ void st(uint32_t i, float v) const {
+        if (R_SMEM)
+            r[i] = v;
+        else
+            __stcg(r + i, v);
+    }
+
+    // Row r of base row b: circulants e0 .. e0 + deg of the table, their
+    // columns from the group's shared-address copy `gblk`.
+    template <int DMAX>
+    __device__ __forceinline__ void qc_row(const Params& p, const int2* __restrict__ gblk,
+                                           const int deg, uint32_t, const int32_t e0,
+                                           const int32_t rr, const uint32_t r4,
+                                           const uint32_t Z4) const {
+        const uint32_t Z = static_cast<uint32_t>(p.Z);
+        const uint32_t base = static_cast<uint32_t>(e0) * Z + static_cast<uint32_t>(rr);
+        float q[DMAX], ph[DMAX];
+        float total = 0.0f;
+        bool neg = false;
+#pragma unroll
+        for (int e = 0; e < DMAX; ++e) {
+            if (e < deg) {
+                const int2 b = gblk[e];
+                uint32_t ce = r4 + static_cast<uint32_t>(b.x);
+                ce = ce >= static_cast<uint32_t>(b.y) ? ce - Z4 : ce;
+                const float qe = __fsub_rn(ld_shared_f32(ce), ld(base + e * Z));
+                q[e] = qe;
+                neg ^= qe < 0.0f;
+                ph[e] = phi(fabsf(qe));
+                total = __fadd_rn(total, ph[e]);
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < DMAX; ++e) {
+            if (e < deg) {
+                const int2 b = gblk[e];
+                uint32_t ce = r4 + static_cast<uint32_t>(b.x);
+                ce = ce >= static_cast<uint32_t>(b.y) ? ce - Z4 : ce;
+                const float mag = phi(__fsub_rn(total, ph[e]));
+                const float rn = (neg != (q[e] < 0.0f)) ? -mag : mag;
+                st_shared_f32(ce, __fadd_rn(q[e], rn));
+                st(base + e * Z, rn);
+            }
+        }
+    }
+
+    template <int DMAX, class ColOf>
+    __device__ __forceinline__ void csr_row(const Params&, float* __restrict__ a, uint32_t,
+                                            const int deg, const int32_t e0,
+                                            const ColOf& col_of) const {
+        float q[DMAX], ph[DMAX];
+        float total = 0.0f;
+        bool neg = false;
+#pragma unroll
+        for (int e = 0; e < DMAX; ++e) {
+            if (e < deg) {
+                const float qe = __fsub_rn(a[col_of(e)], ld(static_cast<uint32_t>(e0 + e)));
+                q[e] = qe;
+                neg ^= qe < 0.0f;
+                ph[e] = phi(fabsf(qe));
+                total = __fadd_rn(total, ph[e]);
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < DMAX; ++e) {
+            if (e < deg) {
+                const float mag = phi(__fsub_rn(total, ph[e]));
+                const float rn = (neg != (q[e] < 0.0f)) ? -mag : mag;
+                a[col_of(e)] = __fadd_rn(q[e], rn);
+                st(static_cast<uint32_t>(e0 + e), rn);
+            }
+        }
+    }
+};
+
+struct SumProductPick {
+    template <bool QC, int DMAX>
+    static KernelFn get(bool app_smem, bool r_smem) {
+        if (app_smem && r_smem) return decode_kernel<SumProductState, QC, DMAX, true, true>;
+        if (app_smem) return decode_kernel<SumProductState, QC, DMAX, true, false>;
+        if constexpr (!QC) return decode_kernel<SumProductState, QC, DMAX, false, false>;
+        return nullptr;
+    }
+};
+
+}  // namespace sp
+
+KernelFn sum_product_kernel(bool qc, int dmax, bool app_smem, bool r_smem) {
+    return pick_shape<sp::SumProductPick>(qc, dmax, app_smem, r_smem);
+}
+
+}  // namespace ldpc
+}  // namespace ck

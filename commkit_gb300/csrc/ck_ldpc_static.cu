@@ -65,8 +65,6 @@ extern "C" int ck_ldpc_decode_static(const ck_ldpc_plan* plan, const float* llr_
                                      int8_t* bits, int32_t k_bits, void* stream) {
     ck::clear_error();
     if (!plan) return ck::fail(CK_ERR_INVALID_ARGUMENT, "plan is NULL");
-    if (rule != CK_LDPC_MIN_SUM)
-        return ck::fail(CK_ERR_UNSUPPORTED, "only the min-sum rule is implemented");
     int device = -1;
     CK_CUDA(cudaGetDevice(&device));
     if (device != plan->device)
@@ -74,7 +72,7 @@ extern "C" int ck_ldpc_decode_static(const ck_ldpc_plan* plan, const float* llr_
                         plan->device, device);
     void* scratch = nullptr;
     CK_TRY(scratch_address(device, &scratch));
-    return ck::ldpc_decode_in_scratch(plan, llr_in, llr_out, B, n_in, scale, offset,
+    return ck::ldpc_decode_in_scratch(plan, llr_in, llr_out, B, n_in, rule, scale, offset,
                                       max_iterations, early_stop, iters, valid, bits, k_bits,
                                       scratch, CK_LDPC_STATIC_SCRATCH_BYTES,
                                       static_cast<cudaStream_t>(stream));

@@ -172,7 +172,8 @@ int ck_ldpc_plan_get_info(const ck_ldpc_plan* plan, ck_ldpc_plan_info* info);
  * most 1024), frames per thread block and where the compressed
  * check-to-variable messages live; 0 lets the plan choose.  Every shape
  * gives the same results bit for bit; it only changes speed.  The
- * autotuner sets it per code.
+ * autotuner sets it per code.  Sum-product decodes use only the threads
+ * per frame and choose their own frames per block and placement.
  */
 typedef struct ck_ldpc_launch {
     int32_t threads_per_frame;
@@ -213,7 +214,11 @@ int ck_ldpc_workspace_size(const ck_ldpc_plan* plan, int64_t B, int32_t rule, si
  *           256-byte aligned; NULL makes the call allocate and free it
  *           stream-ordered (cudaMallocAsync / cudaFreeAsync).
  * Min-sum results (LLRs, bits, iterations, valid) are bit-identical to
- * the reference's kernel and its Numba twin.  B < 2^31.
+ * the reference's kernel and its Numba twin.  Sum-product (the reference's
+ * ldpc_layered<true>, commkit/_cuda/src/ldpc.cu:74-91) runs the same
+ * float32 operations in the same order and calls logf/tanhf for
+ * phi(x) = -log tanh(x/2), so it matches up to the rounding of those
+ * functions, as the reference's own GPU and CPU paths do.  B < 2^31.
  */
 int ck_ldpc_decode(const ck_ldpc_plan* plan, const float* llr_in, float* llr_out, int64_t B,
                    int32_t n_in, int32_t rule, float scale, float offset,
@@ -234,7 +239,7 @@ typedef struct ck_ldpc_batch {
     float* llr_out;       /* (B, n_in), may equal llr_in */
     int64_t B;
     int32_t n_in;
-    int32_t rule;         /* CK_LDPC_MIN_SUM */
+    int32_t rule;         /* CK_LDPC_MIN_SUM (the only rule of mixed launches) */
     float scale;
     float offset;
     int32_t max_iterations;

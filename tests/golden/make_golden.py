@@ -20,7 +20,12 @@ Every output here is the reference's own result on seeded inputs:
   seeded codes A, B and C (``commkit_gb300.workloads``) and of the
   reference's own known-answer cases, DVB-S2 short 1/2 and PON with
   ``MinSum(0.75, 0.05, 12)`` on ``1.8 + 1.5 N(0,1)`` LLRs of seed 1
-  (``tests/coding/test_ldpc_kernel.py:16-34``).
+  (``tests/coding/test_ldpc_kernel.py:16-34``);
+* ``ldpc_sp_golden.npz``: sum-product decodes (five iterations, with and
+  without early stop) of DVB-S2 short 1/2 on the reference's own
+  GPU-vs-CPU input (``0.8 + 1.5 N(0,1)``, seed 2, four frames;
+  ``tests/coding/test_ldpc_kernel.py:37-45``) and of PON on two frames of
+  the same distribution (``--only=sp`` writes just this file).
 
 Large outputs are stored as SHA-256 digests of their bytes (negative zeros
 folded to +0) plus their first frame; inputs drawn from ``default_rng``
@@ -252,8 +257,54 @@ def kat_case(ref: str, which: str) -> dict:
     return out
 
 
-def main(ref: str) -> None:
+def sp_case(ref: str, which: str, tag: str, mean: float, seed: int, frames: int,
+            iterations: int) -> dict:  # fmt: skip
+    """Sum-product through the reference's CPU decoder on ``frames`` frames of
+    ``mean + 1.5 N(0,1)`` LLRs (``default_rng(seed)``), ``iterations`` at
+    most, with and without early stop."""
+    _import_reference(ref)
+    from commkit.coding import LDPCCode, SumProduct, decode
+
+    code = LDPCCode.dvbs2("1/2", frame="short") if which == "dvbs2s" else LDPCCode.pon()
+    rng = np.random.default_rng(seed)
+    llrs = (mean + 1.5 * rng.standard_normal((frames, code.n))).astype(np.float32)
+    out = {f"sp_{tag}_code": which, f"sp_{tag}_llrs": llrs, f"sp_{tag}_max_iterations": np.int64(iterations)}
+    for es in (False, True):
+        method = SumProduct(max_iterations=iterations, early_stop=es)
+        case = _decode_case(ref, code, llrs, method)
+        case.pop("post_first")
+        out.update({f"sp_{tag}_es{int(es)}_{k}": v for k, v in case.items()})
+        res = decode(llrs.reshape(-1), code=code, method=method)
+        out[f"sp_{tag}_es{int(es)}_post"] = np.asarray(res.llrs, np.float32).reshape(frames, -1)
+    return out
+
+
+# (tag, code, mean, seed, frames, iterations): the reference's own GPU-vs-CPU
+# case (tests/coding/test_ldpc_kernel.py:37-45), the circulant path (PON),
+# and both codes at an SNR where some frames stop early.
+SP_CASES = (
+    ("dvbs2s", "dvbs2s", 0.8, 2, 4, 5),
+    ("pon", "pon", 0.8, 2, 2, 5),
+    ("dvbs2s_hi", "dvbs2s", 1.8, 1, 4, 10),
+    ("pon_hi", "pon", 3.0, 1, 2, 10),
+)
+
+
+def main(ref: str, only: str | None = None) -> None:
     t0 = time.time()
+    if only == "sp":
+        import multiprocessing as mp
+
+        with ProcessPoolExecutor(max_workers=len(SP_CASES), mp_context=mp.get_context("spawn")) as pool:
+            futs = [pool.submit(sp_case, ref, code, tag, mean, seed, frames, its)
+                    for tag, code, mean, seed, frames, its in SP_CASES]
+            parts = [f.result() for f in futs]
+        sp = {}
+        for part in parts:
+            sp.update(part)
+        np.savez_compressed(HERE / "ldpc_sp_golden.npz", **sp)
+        print(f"sum-product fixtures written in {time.time() - t0:.0f} s")
+        return
     jobs = {
         "qam": (qam_tables, (ref,)),
         "llr": (llr_golden, (ref,)),
@@ -278,4 +329,6 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
+    only = next((a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")), None)
+    main(args[0] if args else "/root/reference", only)

@@ -220,8 +220,8 @@ def test_decode_shapes_and_errors(torch_dev, ck):
     assert res1.bits.shape == (3 * code.k,)
     with pytest.raises(ValueError, match="multiple"):
         ck.decode(x[:, :-1], code=code)
-    with pytest.raises(NotImplementedError):
-        ck.decode(x, code=code, method=ck.SumProduct())
+    with pytest.raises(TypeError, match="method"):
+        ck.decode(x, code=code, method="min-sum")
     with pytest.warns(ck.PrecisionWarning):
         ck.decode(x.to(torch.float64), code=code)
     empty = ck.decode(x[:0], code=code)

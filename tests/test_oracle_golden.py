@@ -13,7 +13,7 @@ import pytest
 import oracle
 from commkit_gb300 import workloads as W
 from commkit_gb300.mapping import Constellation, host_tables
-from tests.conftest import digest, kat_llrs
+from tests.conftest import SP_SATURATED, SP_TAGS, check_sum_product, digest, kat_llrs
 
 ORDERS = (4, 16, 64, 256)
 
@@ -158,3 +158,19 @@ def test_oracle_threads_do_not_change_results(golden_ldpc):
             for t in (1, 3)]  # fmt: skip
     for a, b in zip(*outs, strict=True):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("tag", SP_TAGS)
+@pytest.mark.parametrize("early_stop", [False, True])
+def test_sum_product_oracle_matches_reference(golden_ldpc, golden_sp, tag, early_stop):
+    """The oracle's sum-product rule against the reference's CPU decoder."""
+    g, sp = golden_ldpc, golden_sp
+    which = str(sp[f"sp_{tag}_code"])
+    m, N, k = (int(g[f"{which}_{s}"]) for s in ("m", "N", "k"))
+    row_ptr, cols, _ = oracle.schedule(g[f"{which}_checks"], g[f"{which}_variables"], m, N)
+    bits, post, valid, iters = oracle.decode(
+        sp[f"sp_{tag}_llrs"], (row_ptr, cols, N), k=k, sum_product=True,
+        max_iterations=int(sp[f"sp_{tag}_max_iterations"]), early_stop=early_stop,
+    )  # fmt: skip
+    check_sum_product(sp, f"sp_{tag}_es{int(early_stop)}", bits, post, valid, iters,
+                      saturated=tag in SP_SATURATED)  # fmt: skip

@@ -20,7 +20,7 @@ from commkit_gb300 import workloads as W
 pytestmark = pytest.mark.gpu
 
 
-def _decode_c_abi(lib, plan, llr, n, k, method, *, static, ws=None):
+def _decode_c_abi(lib, plan, llr, n, k, method, *, static, ws=None, rule=0):
     import torch
 
     from commkit_gb300 import _device, _lib
@@ -31,7 +31,7 @@ def _decode_c_abi(lib, plan, llr, n, k, method, *, static, ws=None):
     iters = torch.empty(B, dtype=torch.int32, device=llr.device)
     valid = torch.empty(B, dtype=torch.uint8, device=llr.device)
     stream = torch.cuda.current_stream(llr.device).cuda_stream
-    common = (plan.handle, llr.data_ptr(), out.data_ptr(), B, n, _lib.CK_LDPC_MIN_SUM,
+    common = (plan.handle, llr.data_ptr(), out.data_ptr(), B, n, rule,
               float(np.float32(method[0])), float(np.float32(method[1])), method[2], 1,
               iters.data_ptr(), valid.data_ptr(), bits.data_ptr(), k)  # fmt: skip
     if static:
@@ -70,3 +70,28 @@ def test_static_scratch_matches_workspace_decode(name, frames, order, ebn0):
         for a, b in zip(got, want, strict=True):
             np.testing.assert_array_equal(a, b)
     assert (want[2] > 0).any()
+
+
+def test_static_scratch_sum_product():
+    """Sum-product through the static scratch: code C's per-edge messages
+    (480 KB a frame) in the static array, fewer slots than frames."""
+    import torch
+
+    import commkit_gb300 as ck
+    from commkit_gb300 import _lib
+
+    dev = torch.device("cuda", 0)
+    spec = W.CODES["C"]
+    code = ck.LDPCCode.quasi_cyclic(spec.base(), lifting=spec.z)
+    rng = np.random.default_rng(8)
+    llr = torch.from_numpy((1.5 + 2.0 * rng.standard_normal((200, code.n))).astype(np.float32)).to(dev)
+    plan = code._plan(0)
+    ws = torch.empty(plan.workspace_size(200, _lib.CK_LDPC_SUM_PRODUCT), dtype=torch.uint8, device=dev)
+    lib = _lib.lib()
+    method = (1.0, 0.0, 4)
+    sp = _lib.CK_LDPC_SUM_PRODUCT
+    want = _decode_c_abi(lib, plan, llr, code.n, code.k, method, static=False, ws=ws, rule=sp)
+    for _ in range(2):
+        got = _decode_c_abi(lib, plan, llr, code.n, code.k, method, static=True, rule=sp)
+        for a, b in zip(got, want, strict=True):
+            np.testing.assert_array_equal(a, b)
