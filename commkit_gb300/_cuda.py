@@ -11,6 +11,7 @@ sm_103a kernel of ``libck_gb300.so``:
 ======================  ====================================  ===========================
 name                    reference launcher                    C ABI
 ======================  ====================================  ===========================
+llr                     commkit/_cuda/llr.py:37-84            ck_llr_points
 llr_separable_maxlog    commkit/_cuda/llr.py:150-206          ck_llr_separable_maxlog
 llr_separable           commkit/_cuda/llr.py:87-147           ck_llr_separable
 ldpc_layered            commkit/_cuda/coding.py:11-69         ck_ldpc_plan_create + ck_ldpc_decode
@@ -32,6 +33,42 @@ import numpy as np
 from . import _device, _lib
 
 LLR_MAX_K = _lib.CK_LLR_MAX_K
+
+
+def _llr_factory() -> Callable:
+    """Max-log or exact LLRs from the metrics of every point."""
+
+    def launch(x: Any, points: Any, log_pmf: Any, labels: Any, *, k: int, inv_s2: float,
+               exact: bool) -> Any:  # fmt: skip
+        """LLRs of the ``(n,)`` complex64 symbols ``x``, shape ``(n, k)``;
+        ``points`` ``(M,)`` complex64, ``log_pmf`` ``(M,)`` float32 and
+        ``labels`` ``(M,)`` int32 (each point's k-bit label, MSB first)."""
+        if not 1 <= k <= LLR_MAX_K:
+            raise ValueError(f"bits per symbol must be in [1, {LLR_MAX_K}], got {k}")
+        xd, pd = _device.wrap(x, "x"), _device.wrap(points, "points")
+        _device.check(xd, "x", np.complex64, (None,))
+        _device.check(pd, "points", np.complex64, (None,))
+        M = pd.shape[0]
+        if M < 1:
+            raise ValueError(f"points must be non-empty, got M={M}")
+        lp, la = _device.wrap(log_pmf, "log_pmf"), _device.wrap(labels, "labels")
+        _device.check(lp, "log_pmf", np.float32, (M,))
+        _device.check(la, "labels", np.int32, (M,))
+        n = xd.shape[0]
+        if n >= 2**31:
+            raise ValueError(f"at most 2**31 - 1 symbols per call, got {n}")
+        out = _device.empty(xd, (n, k), np.float32)
+        if n == 0:
+            return out
+        with _device.on_device(xd):
+            st = _lib.lib().ck_llr_points(
+                xd.ptr, n, pd.ptr, lp.ptr, la.ptr, M, int(k), float(np.float32(inv_s2)),
+                1 if exact else 0, _device.wrap(out).ptr, _device.stream_of(xd),
+            )  # fmt: skip
+        _lib.check(st, "llr")
+        return out
+
+    return launch
 
 
 def _llr_separable_maxlog_factory() -> Callable:
@@ -226,6 +263,7 @@ def get_kernel(name: str, **spec: Any) -> Callable:
 
 #: Kernel name -> launcher factory (the reference's names).
 _KERNEL_FACTORIES: dict[str, Callable[..., Callable]] = {
+    "llr": _llr_factory,
     "llr_separable_maxlog": _llr_separable_maxlog_factory,
     "llr_separable": _llr_separable_factory,
     "ldpc_layered": _ldpc_layered_factory,

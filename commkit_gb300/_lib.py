@@ -24,7 +24,6 @@ CK_ERR_DEVICE_TIMEOUT = 5
 CK_LLR_MAX_K = 16
 CK_LDPC_MIN_SUM = 0
 CK_LDPC_SUM_PRODUCT = 1
-CK_LDPC_SUM_PRODUCT = 1
 CK_LDPC_PLACE_AUTO = 0
 CK_LDPC_PLACE_SHARED = 1
 CK_LDPC_PLACE_GLOBAL = 2
@@ -38,6 +37,8 @@ EXPORTS = (
     "ck_llr_separable",
     "ck_llr_separable_maxlog_frames",
     "ck_llr_separable_frames",
+    "ck_llr_points",
+    "ck_llr_points_frames",
     "ck_ldpc_schedule",
     "ck_ldpc_plan_create",
     "ck_ldpc_plan_destroy",
@@ -135,6 +136,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         "ck_llr_separable_frames": (
             [p, i64, i64, p, ctypes.POINTER(AxisLevels), ctypes.POINTER(AxisLevels), i32, p, p],
             ctypes.c_int),
+        "ck_llr_points": ([p, i64, p, p, p, i32, i32, ctypes.c_float, i32, p, p], ctypes.c_int),
+        "ck_llr_points_frames": ([p, i64, i64, p, p, p, p, i32, i32, i32, p, p], ctypes.c_int),
         "ck_ldpc_schedule": ([p, p, i64, i32, i32, p, p, p, ctypes.POINTER(i32)], ctypes.c_int),
         "ck_ldpc_plan_create": ([p, p, p, i32, i32, i32, ctypes.POINTER(p)], ctypes.c_int),
         "ck_ldpc_plan_destroy": ([p], ctypes.c_int),

@@ -3,7 +3,7 @@
 // kernels are in ck_llr_kernels.cuh.
 #include <stdint.h>
 
-#include "ck_llr_kernels.cuh"
+#include "ck_llr_points.cuh"
 
 namespace ck {
 namespace llr {
@@ -54,6 +54,17 @@ CK_LLR_EXTERN(4)
 CK_LLR_EXTERN(5)
 CK_LLR_EXTERN(6)
 #undef CK_LLR_EXTERN
+
+namespace points {
+#define CK_LLR_POINTS_EXTERN(K)                                                               \
+    extern template int launch_points<K>(const float2*, uint32_t, const Table&, const NoiseScale&, \
+                                         bool, float*, cudaStream_t);
+CK_LLR_POINTS_EXTERN(1) CK_LLR_POINTS_EXTERN(2) CK_LLR_POINTS_EXTERN(3) CK_LLR_POINTS_EXTERN(4)
+CK_LLR_POINTS_EXTERN(5) CK_LLR_POINTS_EXTERN(6) CK_LLR_POINTS_EXTERN(7) CK_LLR_POINTS_EXTERN(8)
+CK_LLR_POINTS_EXTERN(9) CK_LLR_POINTS_EXTERN(10) CK_LLR_POINTS_EXTERN(11) CK_LLR_POINTS_EXTERN(12)
+CK_LLR_POINTS_EXTERN(13) CK_LLR_POINTS_EXTERN(14) CK_LLR_POINTS_EXTERN(15) CK_LLR_POINTS_EXTERN(16)
+#undef CK_LLR_POINTS_EXTERN
+}  // namespace points
 
 namespace {
 
@@ -116,6 +127,37 @@ int frame_noise(int64_t n, int64_t frame_len, const float* inv_s2, NoiseScale* s
     return CK_OK;
 }
 
+int launch_points(const void* x, int64_t n, const void* pts, const float* log_pmf,
+                  const int32_t* labels, int32_t M, int32_t k, int32_t exact, const NoiseScale& noise,
+                  float* out, void* stream) {
+    if (k < 1 || k > CK_LLR_MAX_K)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "bits per symbol must be in [1, %d], got %d",
+                        CK_LLR_MAX_K, k);
+    if (M < 1) return ck::fail(CK_ERR_INVALID_ARGUMENT, "points must be non-empty, got M=%d", M);
+    if (n < 0 || n >= (int64_t(1) << 31))
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "at most 2**31 - 1 symbols per call, got %lld",
+                        static_cast<long long>(n));
+    if (n == 0) return CK_OK;
+    if (!x || !out || !pts || !log_pmf || !labels)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "an array is NULL");
+    if (reinterpret_cast<uintptr_t>(x) % 8 != 0 || reinterpret_cast<uintptr_t>(pts) % 8 != 0 ||
+        reinterpret_cast<uintptr_t>(out) % 4 != 0)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "x and points must be 8-byte and out 4-byte aligned");
+    const points::Table t{static_cast<const float2*>(pts), log_pmf, labels, M};
+    const float2* xs = static_cast<const float2*>(x);
+    const uint32_t nn = static_cast<uint32_t>(n);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const bool ex = exact != 0;
+    switch (k) {
+#define CK_CASE(K) \
+    case K: return points::launch_points<K>(xs, nn, t, noise, ex, out, s);
+        CK_CASE(1) CK_CASE(2) CK_CASE(3) CK_CASE(4) CK_CASE(5) CK_CASE(6) CK_CASE(7) CK_CASE(8)
+        CK_CASE(9) CK_CASE(10) CK_CASE(11) CK_CASE(12) CK_CASE(13) CK_CASE(14) CK_CASE(15) CK_CASE(16)
+#undef CK_CASE
+        default: return ck::fail(CK_ERR_INVALID_ARGUMENT, "bad k");
+    }
+}
+
 int check_lo_hi(const ck_axis_maxlog* a) {
     if (a && (!a->lo || !a->hi))
         return ck::fail(CK_ERR_INVALID_ARGUMENT, "lo/hi tables are NULL");
@@ -130,6 +172,7 @@ using ck::llr::launch;
 using ck::llr::scalar_noise;
 using ck::llr::frame_noise;
 using ck::llr::check_lo_hi;
+using ck::llr::launch_points;
 using ck::llr::NoiseScale;
 
 extern "C" int ck_llr_separable_maxlog(const void* x, int64_t n, const ck_axis_maxlog* re,
@@ -170,4 +213,22 @@ extern "C" int ck_llr_separable_frames(const void* x, int64_t n, int64_t frame_l
     if (im && !im->logp) return ck::fail(CK_ERR_INVALID_ARGUMENT, "im log prior is NULL");
     return exact ? launch<2>(x, n, re, im, s, out, stream)
                  : launch<1>(x, n, re, im, s, out, stream);
+}
+
+extern "C" int ck_llr_points(const void* x, int64_t n, const void* points, const float* log_pmf,
+                             const int32_t* labels, int32_t M, int32_t k, float inv_s2,
+                             int32_t exact, float* out, void* stream) {
+    ck::clear_error();
+    return launch_points(x, n, points, log_pmf, labels, M, k, exact, scalar_noise(inv_s2), out,
+                         stream);
+}
+
+extern "C" int ck_llr_points_frames(const void* x, int64_t n, int64_t frame_len,
+                                    const float* inv_s2, const void* points,
+                                    const float* log_pmf, const int32_t* labels, int32_t M,
+                                    int32_t k, int32_t exact, float* out, void* stream) {
+    ck::clear_error();
+    NoiseScale s;
+    CK_TRY(frame_noise(n, frame_len, inv_s2, &s));
+    return launch_points(x, n, points, log_pmf, labels, M, k, exact, s, out, stream);
 }

@@ -117,6 +117,28 @@ def encode_qc(base: np.ndarray, z: int, info: np.ndarray) -> np.ndarray:
     return np.concatenate([info, p.reshape(F, mb * z)], axis=1)
 
 
+def encode_accumulate(checks: np.ndarray, variables: np.ndarray, m: int, k: int,
+                      info: np.ndarray) -> np.ndarray:  # fmt: skip
+    """Systematic codewords ``[u | p]`` (int8, ``(F, k + m)``) of a code whose
+    parity part is a staircase: check j holds parity bits k + j and, for
+    j >= 1, k + j - 1 (DVB-S2's accumulator, ``commkit/coding/ldpc.py:217-236``).
+    ``s = H_info u`` over GF(2), then ``p_j = p_{j-1} + s_j``."""
+    from scipy.sparse import csr_matrix
+
+    checks = np.asarray(checks, dtype=np.int64)
+    variables = np.asarray(variables, dtype=np.int64)
+    par = variables >= k
+    j, c = checks[par], variables[par] - k
+    if not np.all((c == j) | (c == j - 1)) or np.count_nonzero(c == j) != m:
+        raise ValueError("the parity part is not a staircase")
+    h_info = csr_matrix((np.ones(np.count_nonzero(~par), np.int32), (checks[~par], variables[~par])),
+                        shape=(m, k))  # fmt: skip
+    u = np.asarray(info, dtype=np.int8)
+    s = (h_info @ u.T.astype(np.int32)).T % 2
+    p = np.bitwise_xor.accumulate(s.astype(np.int8), axis=1)
+    return np.concatenate([u, p], axis=1)
+
+
 # ---------------------------------------------------------------------------
 # Gray QAM and AWGN
 # ---------------------------------------------------------------------------

@@ -120,6 +120,30 @@ int ck_llr_separable_frames(const void* x, int64_t n, int64_t frame_len, const f
                             const ck_axis_levels* re, const ck_axis_levels* im,
                             int32_t exact, float* out, void* stream);
 
+/*
+ * Max-log (exact = 0) or log-sum-exp (exact = 1) LLRs from the metrics of
+ * every point, -|x - s|^2 inv_s2 + log P(s): constellations without
+ * per-axis factors (PSK, 8-QAM, cross QAM, PAM as complex symbols with a
+ * zero imaginary part, arbitrary points, any prior).  Replaces
+ * `llr(x, points, log_pmf, labels, *, k, inv_s2, exact)`
+ * (commkit/_cuda/llr.py:37-84; kernel commkit/_cuda/src/llr.cu:200-223).
+ *   x       (n,) complex64 symbols (device)
+ *   points  (M,) complex64, log_pmf (M,) float32, labels (M,) int32: each
+ *           point's coordinates, log prior and k-bit label, MSB first
+ *   out     (n, k) float32 LLRs
+ * 1 <= k <= CK_LLR_MAX_K, M >= 1, n < 2^31.  Max-log results are
+ * bit-identical to the reference's float32 formula evaluated in IEEE
+ * arithmetic; exact ones agree within the rounding of exp and log.
+ */
+int ck_llr_points(const void* x, int64_t n, const void* points, const float* log_pmf,
+                  const int32_t* labels, int32_t M, int32_t k, float inv_s2, int32_t exact,
+                  float* out, void* stream);
+/* The same with one inv_s2 per frame of frame_len symbols (no reference
+ * counterpart; as ck_llr_separable_frames). */
+int ck_llr_points_frames(const void* x, int64_t n, int64_t frame_len, const float* inv_s2,
+                         const void* points, const float* log_pmf, const int32_t* labels,
+                         int32_t M, int32_t k, int32_t exact, float* out, void* stream);
+
 /* ---------------------------------------------------------------------- */
 /* Layered LDPC decoding                                                   */
 /* ---------------------------------------------------------------------- */

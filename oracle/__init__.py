@@ -77,6 +77,7 @@ def lib() -> ctypes.CDLL:
         _lib.oracle_llr_separable.argtypes = [
             p, i64, i64, p, p, p, p, p, i32, i32, p, p, p, p, i32, i32, i32, p, ctypes.c_int,
         ]  # fmt: skip
+        _lib.oracle_llr_points.argtypes = [p, i64, i64, p, p, p, p, i32, i32, i32, p, ctypes.c_int]
         _lib.oracle_max_threads.restype = ctypes.c_int
     return _lib
 
@@ -319,4 +320,53 @@ def llr(x, order: int, inv_s2_frames, *, method="maxlog", frame_len=None,
     del keep
     if rc:
         raise RuntimeError(f"oracle LLR failed ({rc})")
+    return out
+
+
+def llr_points(x, points, log_pmf, labels, k: int, inv_s2_frames, *, exact: bool = False,
+               frame_len=None, threads=0):  # fmt: skip
+    """LLRs ``(n, k)`` float32 of symbols ``x`` ``(n,)`` against every point
+    (``commkit/mapping/_numba_llr.py:95-124``): ``points`` ``(M,)`` complex,
+    ``log_pmf`` ``(M,)`` float32 and packed ``labels`` ``(M,)``; real
+    symbols or points count with a zero imaginary part."""
+    x = np.ascontiguousarray(x, dtype=np.complex64).reshape(-1)
+    pts = np.ascontiguousarray(points, dtype=np.complex64).reshape(-1)
+    logp = np.ascontiguousarray(log_pmf, dtype=np.float32)
+    lab = np.ascontiguousarray(labels, dtype=np.int32)
+    n = x.size
+    s2 = np.ascontiguousarray(np.atleast_1d(inv_s2_frames), dtype=np.float32)
+    frame_len = int(frame_len or max(n, 1))
+    if s2.size * frame_len < n:
+        raise ValueError("one inverse noise variance per frame")
+    out = np.empty((n, k), np.float32)
+    xf, pf = x.view(np.float32), pts.view(np.float32)
+    rc = lib().oracle_llr_points(_ptr(xf), n, frame_len, _ptr(s2), _ptr(pf), _ptr(logp), _ptr(lab),
+                                 pts.size, int(k), 1 if exact else 0, _ptr(out), int(threads))  # fmt: skip
+    if rc:
+        raise RuntimeError(f"oracle_llr_points failed ({rc})")
+    return out
+
+
+def llr_levels(x, axes, inv_s2_frames, *, exact: bool = False, frame_len=None, threads=0):
+    """LLRs ``(n, k)`` of complex64 symbols against a separable lattice given
+    by its two axes, each ``(levels f32, log prior f32, packed labels i32,
+    positions i32)`` (``commkit/mapping/_numba_llr.py:127-176``)."""
+    x = np.ascontiguousarray(x, dtype=np.complex64).reshape(-1)
+    n = x.size
+    s2 = np.ascontiguousarray(np.atleast_1d(inv_s2_frames), dtype=np.float32)
+    frame_len = int(frame_len or max(n, 1))
+    if s2.size * frame_len < n:
+        raise ValueError("one inverse noise variance per frame")
+    args = [[np.ascontiguousarray(a, dtype=dt) for a, dt in zip(ax, (np.float32, np.float32, np.int32, np.int32))]
+            for ax in axes]  # fmt: skip
+    k = args[0][3].size + args[1][3].size
+    out = np.empty((n, k), np.float32)
+    xf = x.view(np.float32)
+    rc = lib().oracle_llr_separable(
+        _ptr(xf), n, frame_len, _ptr(s2), *[_ptr(a) for a in args[0]], args[0][0].size,
+        args[0][3].size, *[_ptr(a) for a in args[1]], args[1][0].size, args[1][3].size,
+        1 if exact else 0, _ptr(out), int(threads),
+    )  # fmt: skip
+    if rc:
+        raise RuntimeError(f"oracle_llr_separable failed ({rc})")
     return out

@@ -18,6 +18,8 @@
  *   oracle_llr_separable     commkit/mapping/_numba_llr.py:35-92, 127-176
  *                            (prepare_exp, log_half_sum, bit_llr, axis_llrs,
  *                            llr_separable_kernel)
+ *   oracle_llr_points        commkit/mapping/_numba_llr.py:35-81, 95-124
+ *                            (the same steps over every point, llr_kernel)
  *
  * Codewords (and symbols) are independent, so the loops over them run on
  * OpenMP threads; each codeword's arithmetic is sequential and in the
@@ -332,4 +334,83 @@ int oracle_llr_separable(const float* x, int64_t n, int64_t frame_len, const flo
                     out + i * k);
     }
     return 0;
+}
+
+/*
+ * _numba_llr.py:95-124 with :35-81: LLRs from the metrics of all M points,
+ * -(dr*dr + di*di) * inv_s2 + log_pmf[m].  Halves of bit b are the points
+ * whose label bit b (MSB first over k bits) is 0 and 1, in ascending point
+ * order (commkit/mapping/_demap.py:71-79).  x (n, 2) and pts (M, 2) are
+ * interleaved float32 (complex64); inv_s2 holds one value per frame.
+ */
+static void points_llrs(float xr, float xi, const float* pts, const float* logp,
+                        const int32_t* lab, int32_t M, int32_t k, float inv_s2, int exact,
+                        float* metric, float* e, float* out) {
+    for (int32_t m = 0; m < M; ++m) {
+        const float dr = xr - pts[2 * m];
+        const float di = xi - pts[2 * m + 1];
+        metric[m] = -(dr * dr + di * di) * inv_s2 + logp[m];
+    }
+    float peak = 0.0f;
+    if (exact) {
+        peak = metric[0];
+        for (int32_t m = 1; m < M; ++m)
+            if (metric[m] > peak) peak = metric[m];
+        for (int32_t m = 0; m < M; ++m) e[m] = expf(metric[m] - peak);
+    }
+    for (int32_t b = 0; b < k; ++b) {
+        const int shift = k - 1 - b;
+        float res[2];
+        for (int v = 0; v < 2; ++v) {
+            int first = 1;
+            float p = 0.0f;
+            for (int32_t m = 0; m < M; ++m) {
+                if (((lab[m] >> shift) & 1) != v) continue;
+                if (first || metric[m] > p) p = metric[m];
+                first = 0;
+            }
+            if (!exact) {
+                res[v] = p;
+                continue;
+            }
+            float s = 0.0f;
+            for (int32_t m = 0; m < M; ++m)
+                if (((lab[m] >> shift) & 1) == v) s = s + e[m];
+            if (s >= ORACLE_EXACT_FLOOR) {
+                res[v] = logf(s);
+                continue;
+            }
+            s = 0.0f;
+            for (int32_t m = 0; m < M; ++m)
+                if (((lab[m] >> shift) & 1) == v) s = s + expf(metric[m] - p);
+            res[v] = logf(s) + (p - peak);
+        }
+        out[b] = res[0] - res[1];
+    }
+}
+
+int oracle_llr_points(const float* x, int64_t n, int64_t frame_len, const float* inv_s2,
+                      const float* pts, const float* logp, const int32_t* lab, int32_t M,
+                      int32_t k, int32_t exact, float* out, int threads) {
+    if (n < 0 || M < 1 || k < 1 || k > 30 || frame_len < 1) return 1;
+    set_threads(threads);
+    int failed = 0;
+#pragma omp parallel
+    {
+        float* metric = (float*)malloc(sizeof(float) * (size_t)M);
+        float* e = (float*)malloc(sizeof(float) * (size_t)M);
+        if (!metric || !e) {
+#pragma omp atomic write
+            failed = 1;
+        }
+#pragma omp for schedule(static)
+        for (int64_t i = 0; i < n; ++i) {
+            if (!metric || !e) continue;
+            points_llrs(x[2 * i], x[2 * i + 1], pts, logp, lab, M, k, inv_s2[i / frame_len], exact,
+                        metric, e, out + i * k);
+        }
+        free(metric);
+        free(e);
+    }
+    return failed ? 2 : 0;
 }

@@ -25,7 +25,15 @@ Every output here is the reference's own result on seeded inputs:
   without early stop) of DVB-S2 short 1/2 on the reference's own
   GPU-vs-CPU input (``0.8 + 1.5 N(0,1)``, seed 2, four frames;
   ``tests/coding/test_ldpc_kernel.py:37-45``) and of PON on two frames of
-  the same distribution (``--only=sp`` writes just this file).
+  the same distribution (``--only=sp`` writes just this file);
+* ``llr_mpoint_golden.npz``: points, labels and priors of PSK, 8-QAM,
+  cross QAM, PAM, Maxwell-Boltzmann-shaped QAM and a random labelled
+  constellation with a prior, and their LLRs through the reference's
+  ``Constellation.llr`` on CPU input (``--only=mpoint``);
+* ``dvbs2_normal.npz``: the DVB-S2 normal-frame rate-1/2 code of the
+  reference's LDPC benchmark, reference encodings of seeded words and the
+  reference's ``MinSum()`` decode of two QPSK frames at Es/N0 1.5 dB
+  (``--only=dvbs2``).
 
 Large outputs are stored as SHA-256 digests of their bytes (negative zeros
 folded to +0) plus their first frame; inputs drawn from ``default_rng``
@@ -174,6 +182,116 @@ def llr_golden(ref: str) -> dict:
     return out
 
 
+def dvbs2_symbols(words: np.ndarray, esn0_db: float, seed: int) -> tuple[np.ndarray, float]:
+    """Gray QPSK of codewords through complex AWGN at ``esn0_db``:
+    ``(symbols complex64, noise_var)``, seeded (``numpy.random.default_rng``)."""
+    from commkit_gb300.workloads import awgn, map_bits
+
+    nv = 10.0 ** (-esn0_db / 10.0)
+    return awgn(map_bits(words, 4), nv, np.random.default_rng(seed)), nv
+
+
+def dvbs2_case(ref: str) -> dict:
+    """DVB-S2 normal-frame rate 1/2 (n = 64800, k = 32400), the code of the
+    reference's LDPC benchmark (``benchmarks/bench_coding.py:37-38,55-56``):
+    its parity-check edges, three reference encodings of seeded words, and
+    the reference's ``MinSum()`` decode of two of them over QPSK at Es/N0
+    1.5 dB (its benchmark's operating point)."""
+    _import_reference(ref)
+    from commkit.coding import LDPCCode, MinSum, decode, encode
+    from commkit.mapping import Constellation, compute_llr
+
+    code = LDPCCode.dvbs2("1/2")
+    rng = np.random.default_rng(4)
+    info = rng.integers(0, 2, size=(3, code.k), dtype=np.int8)
+    words = np.asarray(encode(info.reshape(-1), code=code), np.int8).reshape(3, -1)
+    rx, nv = dvbs2_symbols(words[:2], 1.5, seed=5)
+    llrs = np.asarray(compute_llr(rx, noise_var=nv, constellation=Constellation.qam(4)), np.float32)
+    llrs = llrs.reshape(2, -1)
+    res = decode(llrs.reshape(-1), code=code, method=MinSum())
+    post = np.asarray(res.llrs, np.float32).reshape(2, -1)
+    row_ptr, cols, layer_ptr = code._schedule
+    return {
+        "dvbs2n_checks": code.checks.astype(np.int32), "dvbs2n_variables": code.variables.astype(np.int32),
+        "dvbs2n_m": np.int64(code.num_checks), "dvbs2n_N": np.int64(code.num_variables),
+        "dvbs2n_n": np.int64(code.n), "dvbs2n_k": np.int64(code.k),
+        "dvbs2n_layer_ptr": layer_ptr.astype(np.int32),
+        "dvbs2n_info": np.packbits(info.astype(np.uint8), axis=1),
+        "dvbs2n_words": np.packbits(words.astype(np.uint8), axis=1),
+        "dvbs2n_llrs_digest": digest(llrs), "dvbs2n_post_digest": digest(post), "dvbs2n_post_first": post[0],
+        "dvbs2n_bits_packed": np.packbits(np.asarray(res.bits, np.uint8).reshape(2, -1), axis=1),
+        "dvbs2n_valid": np.asarray(res.valid, bool).reshape(-1),
+        "dvbs2n_iters": np.asarray(res.iterations, np.int32).reshape(-1),
+    }  # fmt: skip
+
+
+# Constellations of the M-point and prior-weighted demapping paths:
+# (name, builder over the reference's Constellation).
+CONSTELLATIONS = (
+    ("psk2", lambda C: C.psk(2)),
+    ("psk8", lambda C: C.psk(8)),
+    ("psk16", lambda C: C.psk(16)),
+    ("qam2", lambda C: C.qam(2)),
+    ("qam8", lambda C: C.qam(8)),
+    ("qam32", lambda C: C.qam(32)),
+    ("qam128", lambda C: C.qam(128)),
+    ("qam512", lambda C: C.qam(512)),
+    ("pam4", lambda C: C.pam(4)),
+    ("pam8u", lambda C: C.pam(8, unipolar=True)),
+    ("qam16nu", lambda C: C.qam(16).shaped(nu=0.05)),
+    ("qam64h5", lambda C: C.qam(64).shaped(entropy=5.0)),
+    ("qam32h4", lambda C: C.qam(32).shaped(entropy=4.5)),
+    ("custom16", None),
+)
+
+
+def _custom16(C):
+    """16 random points, a random labelling and a random prior."""
+    rng = np.random.default_rng(99)
+    pts = rng.standard_normal(16) + 1j * rng.standard_normal(16)
+    perm = rng.permutation(16)
+    labels = ((perm[:, None] >> np.arange(3, -1, -1)) & 1).astype(np.int8)
+    pmf = rng.uniform(0.2, 1.0, 16)
+    return C(pts, bit_labels=labels, pmf=pmf / pmf.sum())
+
+
+def mpoint_golden(ref: str) -> dict:
+    """Tables and CPU LLRs of the constellations above through the
+    reference's own ``Constellation.llr`` (its CPU routing: per-axis kernels
+    for separable lattices, ``llr_kernel`` over every point otherwise), on
+    seeded noisy symbols plus the origin and far-out points, max-log and
+    exact, at two noise levels."""
+    _import_reference(ref)
+    from commkit.mapping import Constellation
+
+    out = {}
+    for ci, (name, build) in enumerate(CONSTELLATIONS):
+        c = _custom16(Constellation) if build is None else build(Constellation)
+        out[f"{name}_points"] = np.asarray(c.points)
+        out[f"{name}_bit_labels"] = np.asarray(c.bit_labels, np.int8)
+        out[f"{name}_pmf"] = np.zeros(0) if c.pmf is None else np.asarray(c.pmf, np.float64)
+        out[f"{name}_power"] = np.float64(c.power())
+        out[f"{name}_entropy"] = np.float64(c.entropy)
+        out[f"{name}_separable"] = np.bool_(c._axes is not None)
+        rng = np.random.default_rng(1000 + ci)
+        n = 300
+        pts = np.asarray(c.points)
+        idx = rng.integers(0, c.order, n)
+        if c.is_complex:
+            x = pts[idx] + 0.2 * (rng.standard_normal(n) + 1j * rng.standard_normal(n))
+            x = np.concatenate([x, [0j, 40 - 30j, -0.5 + 7j]]).astype(np.complex64)
+        else:
+            x = pts[idx] + 0.2 * rng.standard_normal(n)
+            x = np.concatenate([x, [0.0, 40.0, -9.0]]).astype(np.float32)
+        out[f"{name}_x"] = x
+        for ni, nv in enumerate((0.3, 0.02)):
+            for method in ("maxlog", "exact"):
+                llr = np.asarray(c.llr(x, noise_var=nv, method=method), np.float32)
+                out[f"{name}_n{ni}_{method}"] = llr.reshape(x.size, -1)
+            out[f"{name}_n{ni}_nv"] = np.float64(nv)
+    return out
+
+
 def _decode_case(ref: str, code, llrs: np.ndarray, method) -> dict:
     from commkit.coding import decode
 
@@ -292,6 +410,22 @@ SP_CASES = (
 
 def main(ref: str, only: str | None = None) -> None:
     t0 = time.time()
+    if only == "dvbs2":
+        import multiprocessing as mp
+
+        with ProcessPoolExecutor(max_workers=1, mp_context=mp.get_context("spawn")) as pool:
+            res = pool.submit(dvbs2_case, ref).result()
+        np.savez_compressed(HERE / "dvbs2_normal.npz", **res)
+        print(f"DVB-S2 fixtures written in {time.time() - t0:.0f} s")
+        return
+    if only == "mpoint":
+        import multiprocessing as mp
+
+        with ProcessPoolExecutor(max_workers=1, mp_context=mp.get_context("spawn")) as pool:
+            res = pool.submit(mpoint_golden, ref).result()
+        np.savez_compressed(HERE / "llr_mpoint_golden.npz", **res)
+        print(f"M-point fixtures written in {time.time() - t0:.0f} s")
+        return
     if only == "sp":
         import multiprocessing as mp
 

@@ -243,3 +243,37 @@ def test_workspace_is_reused_and_status_is_clean(torch_dev, ck):
     _assert_same(a, b)
     st = _lib.lib().ck_ldpc_workspace_status(_device.wrap(ws).ptr, _device.stream_of(_device.wrap(ws)))
     assert st == _lib.CK_OK
+
+
+def test_dvbs2_normal_frames(torch_dev, ck):
+    """DVB-S2 normal-frame rate 1/2 (N = 64800, CSR rows, posterior in
+    device memory): the reference's decode of two QPSK frames at Es/N0
+    1.5 dB bit for bit, and 64 codewords (its benchmark's batch) against the
+    oracle."""
+    from commkit_gb300.workloads import awgn, encode_accumulate, map_bits
+    from tests.conftest import GOLDEN
+    from tests.golden.make_golden import dvbs2_symbols
+
+    torch, dev = torch_dev
+    d = dict(np.load(GOLDEN / "dvbs2_normal.npz"))
+    m, N, n, k = (int(d[f"dvbs2n_{s}"]) for s in ("m", "N", "n", "k"))
+    code = ck.LDPCCode(d["dvbs2n_checks"], d["dvbs2n_variables"], m, N, N - n)
+    assert code._plan(0).info["quasi_cyclic"] == 0
+    words = np.unpackbits(d["dvbs2n_words"], axis=1)[:, :n].astype(np.int8)
+    rx, nv = dvbs2_symbols(words[:2], 1.5, seed=5)
+    c = ck.Constellation.qam(4)
+    llr = ck.compute_llr(torch.from_numpy(rx).to(dev), noise_var=nv, constellation=c)
+    assert digest(llr.cpu().numpy()) == d["dvbs2n_llrs_digest"]
+    res = ck.decode(llr, code=code)
+    bits, post, valid, iters = _to_np(res, 2)
+    np.testing.assert_array_equal(iters, d["dvbs2n_iters"])
+    np.testing.assert_array_equal(valid, d["dvbs2n_valid"])
+    np.testing.assert_array_equal(np.packbits(bits.astype(np.uint8), axis=1), d["dvbs2n_bits_packed"])
+    assert digest(post) == d["dvbs2n_post_digest"]
+
+    rng = np.random.default_rng(12)
+    info = rng.integers(0, 2, size=(64, k), dtype=np.int8)
+    sym = awgn(map_bits(encode_accumulate(d["dvbs2n_checks"], d["dvbs2n_variables"], m, k, info), 4), nv, rng)
+    llr = ck.compute_llr(torch.from_numpy(sym).to(dev), noise_var=nv, constellation=c).reshape(64, n)
+    got = _to_np(ck.decode(llr, code=code), 64)
+    _assert_same(got, _oracle(code, llr.cpu().numpy(), max_iterations=50))

@@ -174,3 +174,25 @@ def test_sum_product_oracle_matches_reference(golden_ldpc, golden_sp, tag, early
     )  # fmt: skip
     check_sum_product(sp, f"sp_{tag}_es{int(early_stop)}", bits, post, valid, iters,
                       saturated=tag in SP_SATURATED)  # fmt: skip
+
+
+def test_dvbs2_normal_oracle_and_encoder():
+    """DVB-S2 normal-frame rate 1/2, the code of the reference's LDPC
+    benchmark: schedule, accumulator encoding, QPSK LLRs and MinSum() decode
+    against the reference (``dvbs2_normal.npz``)."""
+    from commkit_gb300.workloads import encode_accumulate
+    from tests.conftest import GOLDEN
+    from tests.golden.make_golden import dvbs2_symbols
+
+    d = dict(np.load(GOLDEN / "dvbs2_normal.npz"))
+    m, N, n, k = (int(d[f"dvbs2n_{s}"]) for s in ("m", "N", "n", "k"))
+    row_ptr, cols, layer_ptr = oracle.schedule(d["dvbs2n_checks"], d["dvbs2n_variables"], m, N)
+    np.testing.assert_array_equal(layer_ptr, d["dvbs2n_layer_ptr"])
+    info = np.unpackbits(d["dvbs2n_info"], axis=1)[:, :k].astype(np.int8)
+    words = encode_accumulate(d["dvbs2n_checks"], d["dvbs2n_variables"], m, k, info)
+    np.testing.assert_array_equal(np.packbits(words.astype(np.uint8), axis=1), d["dvbs2n_words"])
+    rx, nv = dvbs2_symbols(words[:2], 1.5, seed=5)
+    llrs = oracle.llr(rx.reshape(-1), 4, oracle.inv_s2(nv)).reshape(2, -1)
+    assert digest(llrs) == d["dvbs2n_llrs_digest"]
+    bits, post, valid, iters = oracle.decode(llrs, (row_ptr, cols, N), k=k, max_iterations=50)
+    _check_case(d, "dvbs2n", bits, post, valid, iters)
