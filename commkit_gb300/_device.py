@@ -17,12 +17,17 @@ from typing import Any
 import numpy as np
 
 _TORCH_TO_NP = None
+_NP_TO_TORCH = None
+_TORCH = None
 
 
 def _torch():
-    import torch
+    global _TORCH
+    if _TORCH is None:
+        import torch
 
-    return torch
+        _TORCH = torch
+    return _TORCH
 
 
 def _torch_dtypes() -> dict:
@@ -42,6 +47,13 @@ def _torch_dtypes() -> dict:
             t.int16: np.dtype(np.int16),
         }
     return _TORCH_TO_NP
+
+
+def _np_to_torch(dt: np.dtype):
+    global _NP_TO_TORCH
+    if _NP_TO_TORCH is None:
+        _NP_TO_TORCH = {v: k for k, v in _torch_dtypes().items()}
+    return _NP_TO_TORCH[dt]
 
 
 @dataclass
@@ -138,9 +150,7 @@ def empty(like: DeviceArray, shape: tuple[int, ...], dtype: Any) -> Any:
     """A new array of the input's library on the input's device."""
     dt = np.dtype(dtype)
     if like.kind == "torch":
-        t = _torch()
-        tdt = {v: k for k, v in _torch_dtypes().items()}[dt]
-        return t.empty(shape, dtype=tdt, device=like.obj.device)
+        return _torch().empty(shape, dtype=_np_to_torch(dt), device=like.obj.device)
     import cupy  # an __cuda_array_interface__ producer other than torch
 
     with cupy.cuda.Device(like.device):
@@ -149,9 +159,7 @@ def empty(like: DeviceArray, shape: tuple[int, ...], dtype: Any) -> Any:
 
 def zeros(like: DeviceArray, shape: tuple[int, ...], dtype: Any) -> Any:
     if like.kind == "torch":
-        t = _torch()
-        tdt = {v: k for k, v in _torch_dtypes().items()}[np.dtype(dtype)]
-        return t.zeros(shape, dtype=tdt, device=like.obj.device)
+        return _torch().zeros(shape, dtype=_np_to_torch(np.dtype(dtype)), device=like.obj.device)
     import cupy
 
     with cupy.cuda.Device(like.device):
@@ -173,7 +181,11 @@ def to_device(like: DeviceArray, host: np.ndarray) -> Any:
 def stream_of(arr: DeviceArray) -> int:
     """The cudaStream_t handle work on ``arr`` is queued on (0: legacy default)."""
     if arr.kind == "torch":
-        return int(_torch().cuda.current_stream(arr.obj.device).cuda_stream)
+        t = _torch()
+        raw = getattr(t._C, "_cuda_getCurrentRawStream", None)
+        if raw is not None:
+            return int(raw(arr.device))
+        return int(t.cuda.current_stream(arr.obj.device).cuda_stream)
     try:
         import cupy
 

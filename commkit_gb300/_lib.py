@@ -22,6 +22,7 @@ CK_ERR_OUT_OF_MEMORY = 4
 CK_ERR_DEVICE_TIMEOUT = 5
 
 CK_LLR_MAX_K = 16
+CK_GMI_CHUNK = 4096
 CK_LDPC_MIN_SUM = 0
 CK_LDPC_SUM_PRODUCT = 1
 CK_LDPC_PLACE_AUTO = 0
@@ -39,6 +40,11 @@ EXPORTS = (
     "ck_llr_separable_frames",
     "ck_llr_points",
     "ck_llr_points_frames",
+    "ck_random_bits",
+    "ck_ldpc_encode",
+    "ck_map_awgn",
+    "ck_count_errors",
+    "ck_gmi_loss",
     "ck_ldpc_schedule",
     "ck_ldpc_plan_create",
     "ck_ldpc_plan_destroy",
@@ -138,6 +144,12 @@ def _declare(lib: ctypes.CDLL) -> None:
             ctypes.c_int),
         "ck_llr_points": ([p, i64, p, p, p, i32, i32, ctypes.c_float, i32, p, p], ctypes.c_int),
         "ck_llr_points_frames": ([p, i64, i64, p, p, p, p, i32, i32, i32, p, p], ctypes.c_int),
+        "ck_random_bits": ([p, i64, ctypes.c_uint64, ctypes.c_uint64, p], ctypes.c_int),
+        "ck_ldpc_encode": ([p, i64, i32, i32, i32, p, p, i32, p, p, ctypes.c_size_t, p, p], ctypes.c_int),
+        "ck_map_awgn": ([p, i64, i32, p, ctypes.c_float, ctypes.c_float, ctypes.c_uint64, ctypes.c_uint64, p, p],
+                        ctypes.c_int),
+        "ck_count_errors": ([p, p, p, p, i64, i32, i32, p, p, p, p], ctypes.c_int),
+        "ck_gmi_loss": ([p, p, i64, i64, p, p], ctypes.c_int),
         "ck_ldpc_schedule": ([p, p, i64, i32, i32, p, p, p, ctypes.POINTER(i32)], ctypes.c_int),
         "ck_ldpc_plan_create": ([p, p, p, i32, i32, i32, ctypes.POINTER(p)], ctypes.c_int),
         "ck_ldpc_plan_destroy": ([p], ctypes.c_int),

@@ -24,7 +24,7 @@ import numpy as np
 from . import _device, _lib
 from .mapping import PrecisionWarning
 
-__all__ = ["DecodeResult", "LDPCCode", "MinSum", "SumProduct", "decode", "decode_mixed"]
+__all__ = ["DecodeResult", "LDPCCode", "MinSum", "SumProduct", "decode", "decode_mixed", "encode"]
 
 _HARD_LLR = 1.0
 
@@ -187,6 +187,11 @@ class LDPCCode:
             a.setflags(write=False)
         return out
 
+    @cached_property
+    def _encoder(self) -> _Encoder:
+        """How the code encodes on the device (``commkit/coding/ldpc.py:445-486``)."""
+        return _build_encoder(self)
+
     def _plan(self, device: int) -> _Plan:
         plan = self._plans.get(device)
         if plan is None:
@@ -195,6 +200,79 @@ class LDPCCode:
 
             apply_cached(self, plan, device)
         return plan
+
+
+# Largest parity part encoded through a dense inverse (the reference's
+# _MAX_INVERSE, commkit/coding/ldpc.py:46).
+_MAX_INVERSE = 8192
+
+
+@dataclass(frozen=True)
+class _Encoder:
+    """Information columns of H as CSR (``info_row_ptr``, ``info_cols``) and
+    the parity part: an accumulator of ``stride`` (``p_j = s_j + p_{j-stride}``)
+    or the packed rows of ``H_p^-1`` (``inverse``, ``(m, ceil(m/32))`` uint32)."""
+
+    info_row_ptr: np.ndarray
+    info_cols: np.ndarray
+    stride: int
+    inverse: np.ndarray | None
+
+
+def _build_encoder(code: LDPCCode) -> _Encoder:
+    """``s = H_info u``, then the parity part by the cheapest exact rule: an
+    accumulator when every parity column c has the rows c and c + g (the
+    last g only c) -- g = 1 is the reference's "accumulate" kind, g = Z a
+    block dual-diagonal of identities -- else a GF(2) inverse of ``H_p`` (the
+    reference's "inverse" kind, ``commkit/coding/ldpc.py:445-475``)."""
+    m, n = code.num_checks, code.num_variables
+    k = n - m
+    rows, cols = code.checks.astype(np.int64), code.variables.astype(np.int64)
+    par = cols >= k
+    ir, ic = rows[~par], cols[~par]
+    order = np.lexsort((ic, ir))
+    row_ptr = np.concatenate([[0], np.cumsum(np.bincount(ir, minlength=m))]).astype(np.int32)
+    info_cols = ic[order].astype(np.int32)
+    pr, pc = rows[par], cols[par] - k
+    got = np.sort(pr * m + pc)
+    second = np.sort(pr[(pc == 0) & (pr > 0)])
+    g = int(second[0]) if second.size else max(1, m)
+    c = np.arange(m)
+    want = np.sort(np.concatenate([c * m + c, (c[c + g < m] + g) * m + c[c + g < m]]))
+    if got.size == want.size and np.array_equal(got, want):
+        return _Encoder(row_ptr, info_cols, g, None)
+    if m > _MAX_INVERSE:
+        raise NotImplementedError(
+            f"encode(): the parity part of {code!r} is not an accumulator and m = {m} is above "
+            f"{_MAX_INVERSE}; the device encoder takes accumulators and inverses only"
+        )  # fmt: skip
+    return _Encoder(row_ptr, info_cols, 0, _gf2_inverse_packed(pr, pc, m))
+
+
+def _gf2_inverse_packed(pr: np.ndarray, pc: np.ndarray, m: int) -> np.ndarray:
+    """Rows of the inverse of the m x m GF(2) matrix with ones at (pr, pc),
+    packed 32 columns to a uint32 (column j at bit j % 32 of word j // 32),
+    by Gauss-Jordan elimination on [H_p | I] in 64-bit words."""
+    w = (m + 63) // 64
+    aug = np.zeros((m, 2 * w), np.uint64)
+    one = np.uint64(1)
+    np.bitwise_or.at(aug, (pr, pc // 64), np.left_shift(one, (pc % 64).astype(np.uint64)))
+    idx = np.arange(m)
+    np.bitwise_or.at(aug, (idx, w + idx // 64), np.left_shift(one, (idx % 64).astype(np.uint64)))
+    for col in range(m):
+        word, bit = col // 64, one << np.uint64(col % 64)
+        hits = np.flatnonzero(aug[col:, word] & bit)
+        if hits.size == 0:
+            raise NotImplementedError("the parity part of H is singular; such codes are not supported")
+        piv = col + hits[0]
+        if piv != col:
+            aug[[col, piv]] = aug[[piv, col]]
+        others = np.flatnonzero(aug[:, word] & bit)
+        others = others[others != col]
+        aug[others] ^= aug[col]
+    inv64 = np.ascontiguousarray(aug[:, w:])
+    inv32 = inv64.view(np.uint32)  # little-endian: word j // 32 holds columns j
+    return np.ascontiguousarray(inv32[:, : (m + 31) // 32])
 
 
 def _require_invertible_parity(code: LDPCCode) -> None:
@@ -374,6 +452,84 @@ def decode(llrs: Any, *, code: LDPCCode, method: MinSum | SumProduct | None = No
 
     return DecodeResult(bits=shaped(bits, k), llrs=shaped(out_llrs, code.n),
                         valid=shaped(valid, 1), iterations=shaped(iters, 1), checked=True)  # fmt: skip
+
+
+def _encoder_tables(code: LDPCCode, like: _device.DeviceArray) -> tuple:
+    """The encoder's tables on ``like``'s device, cached per code and device."""
+    per = code.__dict__.setdefault("_enc_dev", {})
+    t = per.get(like.device)
+    if t is None:
+        e = code._encoder
+        inv = None if e.inverse is None else _device.to_device(like, e.inverse.view(np.int32))
+        t = per[like.device] = (_device.to_device(like, e.info_row_ptr), _device.to_device(like, e.info_cols), inv)
+    return t
+
+
+def encode_blocks(code: LDPCCode, info: Any, words: Any = None, scratch: Any = None) -> Any:
+    """``(R, k)`` int8 information rows on a CUDA device to ``(R, n)`` int8
+    codewords, systematic (``commkit/coding/ldpc.py:511-536``).  ``words``
+    and ``scratch`` (int8, ``R m`` bytes, plus ``4 R ceil(m/32) + 4`` for an
+    inverse encoder) may be preallocated."""
+    xd = _device.wrap(info, "info")
+    _device.check(xd, "info", np.int8, (None, code.k))
+    R = xd.shape[0]
+    m, k, n = code.num_checks, code.k, code.n
+    if words is None:
+        words = _device.empty(xd, (R, n), np.int8)
+    wd = _device.wrap(words, "words")
+    _device.check(wd, "words", np.int8, (R, n))
+    if R == 0:
+        return words
+    e = code._encoder
+    need = R * m + (4 * R * ((m + 31) // 32) + 4 if e.inverse is not None else 0)
+    if scratch is None:
+        scratch = _device.empty(xd, (need,), np.int8)
+    sd = _device.wrap(scratch, "scratch")
+    with _device.on_device(xd):
+        rp, ci, inv = _encoder_tables(code, xd)
+        st = _lib.lib().ck_ldpc_encode(
+            xd.ptr, R, k, m, n, _device.wrap(rp).ptr, _device.wrap(ci).ptr, e.stride,
+            None if inv is None else _device.wrap(inv).ptr, sd.ptr, sd.size, wd.ptr, _device.stream_of(xd),
+        )  # fmt: skip
+        _lib.check(st, "encode()")
+    return words
+
+
+def encode(bits: Any, *, code: LDPCCode) -> Any:
+    """Encode information bits (``commkit/coding/base.py:248-290``).
+
+    ``bits`` ``(N,)`` or ``(C, N)`` integers 0/1 on a CUDA device, ``N`` a
+    multiple of ``code.k``; returns int8 ``(..., N / k * n)`` on the same
+    device, each block ``[info | parity]`` (punctured parity bits left out).
+    """
+    if not isinstance(code, LDPCCode):
+        raise TypeError(f"encode(): code must be an LDPCCode, got {type(code).__name__}.")
+    x = _device.wrap(bits, "bits")
+    if x.dtype.kind not in "biu":
+        raise TypeError(f"encode(): bits must be integers or bool, got {x.dtype}.")
+    t = bits
+    if x.kind == "torch":
+        import torch
+
+        if x.dtype.kind != "b" and t.numel() and bool(((t < 0) | (t > 1)).any()):
+            raise ValueError("encode(): bits must be 0 or 1.")
+        t = t.to(torch.int8)
+    else:
+        if x.dtype.kind != "b" and x.size and bool(((t < 0) | (t > 1)).any()):
+            raise ValueError("encode(): bits must be 0 or 1.")
+        t = t.astype(np.int8)
+    was_1d = x.ndim == 1
+    t2 = t.reshape(1, -1) if was_1d else t
+    if t2.ndim != 2:
+        raise ValueError(f"encode(): bits must be 1-D or 2-D, got {t2.ndim}-D.")
+    if t2.shape[-1] % code.k:
+        raise ValueError(f"encode(): the last axis of bits ({t2.shape[-1]}) must be a multiple of k = {code.k}.")
+    C, nb = t2.shape[0], t2.shape[-1] // code.k
+    blocks = t2.reshape(C * nb, code.k)
+    if x.kind == "torch":
+        blocks = blocks.contiguous()
+    out = encode_blocks(code, blocks).reshape(C, nb * code.n)
+    return out.reshape(-1) if was_1d else out
 
 
 def _bool_dtype(xd: _device.DeviceArray):

@@ -20,8 +20,8 @@ Host input raises ``TypeError``; there is no CPU path.
 from __future__ import annotations
 
 import ctypes
+import math
 import warnings
-import weakref
 from functools import cached_property
 from typing import Any, NamedTuple
 
@@ -386,7 +386,7 @@ def _qam(order: int) -> Constellation:
 
 def _finite(v: float, name: str, low: float | None = None) -> float:
     f = float(v)
-    if not np.isfinite(f):
+    if not math.isfinite(f):
         raise ValueError(f"{name} must be finite, got {v!r}")
     if low is not None and f < low:
         raise ValueError(f"{name} must be >= {low}, got {v!r}")
@@ -418,7 +418,6 @@ def _check_method(method: str) -> None:
 # Device tables (``commkit/backend.py:265-287``: per owner, kind and device)
 # ---------------------------------------------------------------------------
 
-_TABLES: weakref.WeakKeyDictionary = weakref.WeakKeyDictionary()
 
 
 def _opposite_levels(labels: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
@@ -482,7 +481,11 @@ def _table_kind(c: Constellation, method: str) -> str:
 
 
 def device_tables(constellation: Constellation, kind: str, like: _device.DeviceArray):
-    per = _TABLES.setdefault(constellation, {})
+    # Kept on the (immutable) instance: a lookup by value would compare the
+    # points on every call.
+    per = constellation.__dict__.get("_device_tables")
+    if per is None:
+        per = constellation.__dict__["_device_tables"] = {}
     key = (kind, like.device)
     t = per.get(key)
     if t is None:

@@ -145,6 +145,66 @@ int ck_llr_points_frames(const void* x, int64_t n, int64_t frame_len, const floa
                          int32_t M, int32_t k, int32_t exact, float* out, void* stream);
 
 /* ---------------------------------------------------------------------- */
+/* Coded-link simulation (the Monte-Carlo error-rate loop)                 */
+/* ---------------------------------------------------------------------- */
+
+/*
+ * `count` random bits (int8 0/1) from Philox-4x32-10 (seed, stream): bit i
+ * is bit i % 32 of word (i / 32) % 4 of the generator's output for counter
+ * i / 128.  Replaces the host draws of the reference's error-rate loop
+ * (commkit/coding/performance.py:307-309) with a device stream.
+ */
+int ck_random_bits(int8_t* out, int64_t count, uint64_t seed, uint64_t stream_id, void* stream);
+
+/*
+ * Systematic LDPC encoding on the device (commkit/coding/ldpc.py:445-536):
+ * words (B, n) = [info | parity][:n] with s = H_info u over GF(2)
+ * (info_row_ptr (m + 1), info_cols: the CSR of H over the k information
+ * columns) and either
+ *   stride >= 1, inverse NULL: the accumulator p_j = s_j + p_{j - stride}
+ *     (stride 1: the reference's "accumulate" kind, a dual-diagonal parity
+ *     part; stride Z: a block dual-diagonal of identity circulants), or
+ *   stride 0, inverse (m, ceil(m/32)) uint32: rows of H_p^-1 packed 32 bits
+ *     a word, p = H_p^-1 s (the reference's "inverse" kind).
+ * scratch: at least B m bytes (+ 4 B ceil(m/32) + 4 with an inverse).
+ */
+int ck_ldpc_encode(const int8_t* info, int64_t B, int32_t k, int32_t m, int32_t n,
+                   const int32_t* info_row_ptr, const int32_t* info_cols, int32_t stride,
+                   const uint32_t* inverse, int8_t* scratch, size_t scratch_bytes, int8_t* words,
+                   void* stream);
+
+/*
+ * Symbols (n_sym,) complex64 of a bit record: symbol i is the point whose
+ * label is bits [i b, (i + 1) b) (MSB first), b = bits_per_symbol, plus
+ * Gaussian noise of standard deviation std_re / std_im per component
+ * (Box-Muller on Philox counter i of (seed, stream_id)).  Replaces
+ * Constellation.map and the AWGN of commkit/coding/performance.py:318-331.
+ */
+int ck_map_awgn(const int8_t* bits, int64_t n_sym, int32_t bits_per_symbol,
+                const void* points_by_label, float std_re, float std_im, uint64_t seed,
+                uint64_t stream_id, void* out, void* stream);
+
+/*
+ * Adds one decoded batch to counts[7] (device int64): blocks, information
+ * bit errors, block errors, pre-FEC bit errors (channel LLR < 0 against the
+ * sent bit), detected failures (valid 0), undetected errors (a block in
+ * error reported valid), iterations (commkit/coding/performance.py:332-342).
+ */
+int ck_count_errors(const int8_t* info, const int8_t* decoded, const float* llr, const int8_t* sent,
+                    int64_t B, int32_t k, int32_t n, const uint8_t* valid, const int32_t* iters,
+                    int64_t* counts, void* stream);
+
+/*
+ * GMI loss terms log2(1 + exp(-(1 - 2c) L)) in float32, summed in float64
+ * over chunks of CK_GMI_CHUNK LLRs of each of `rows` rows of `len`:
+ * partial (rows, ceil(len / CK_GMI_CHUNK)) (commkit/metrics/information.py:
+ * 40-88).
+ */
+#define CK_GMI_CHUNK 4096
+int ck_gmi_loss(const float* llr, const int8_t* bits, int64_t rows, int64_t len, double* partial,
+                void* stream);
+
+/* ---------------------------------------------------------------------- */
 /* Layered LDPC decoding                                                   */
 /* ---------------------------------------------------------------------- */
 

@@ -33,7 +33,9 @@ Every output here is the reference's own result on seeded inputs:
 * ``dvbs2_normal.npz``: the DVB-S2 normal-frame rate-1/2 code of the
   reference's LDPC benchmark, reference encodings of seeded words and the
   reference's ``MinSum()`` decode of two QPSK frames at Es/N0 1.5 dB
-  (``--only=dvbs2``).
+  (``--only=dvbs2``);
+* ``gmi_golden.npz``: the reference's ``gmi`` / ``ngmi`` of seeded 16-QAM,
+  8-PSK and shaped 64-QAM LLRs (``--only=gmi``).
 
 Large outputs are stored as SHA-256 digests of their bytes (negative zeros
 folded to +0) plus their first frame; inputs drawn from ``default_rng``
@@ -223,6 +225,37 @@ def dvbs2_case(ref: str) -> dict:
         "dvbs2n_valid": np.asarray(res.valid, bool).reshape(-1),
         "dvbs2n_iters": np.asarray(res.iterations, np.int32).reshape(-1),
     }  # fmt: skip
+
+
+def gmi_case(ref: str) -> dict:
+    """The reference's ``gmi`` and ``ngmi`` (``commkit/metrics/information.py``)
+    of seeded 16-QAM, 8-PSK and shaped 64-QAM LLRs, 1-D and 2-D, with a
+    skipped leading symbol."""
+    _import_reference(ref)
+    from commkit.mapping import Constellation, compute_llr
+    from commkit.metrics import gmi, ngmi
+
+    out = {}
+    cases = (("q16", Constellation.qam(16), 0.08), ("p8", Constellation.psk(8), 0.05),
+             ("q64s", Constellation.qam(64).shaped(entropy=5.0), 0.02))  # fmt: skip
+    for i, (name, c, nv) in enumerate(cases):
+        rng = np.random.default_rng(40 + i)
+        k = c.bits_per_symbol
+        bits = rng.integers(0, 2, size=(2, 600 * k), dtype=np.int8)
+        labels = (bits.reshape(2, 600, k).astype(np.int64) << np.arange(k - 1, -1, -1)).sum(-1)
+        from commkit.mapping._demap import _packed_labels
+
+        by_label = np.empty(c.order, complex)
+        by_label[_packed_labels(c.bit_labels)] = c.points
+        x = by_label[labels] + np.sqrt(nv / 2) * (rng.standard_normal((2, 600)) + 1j * rng.standard_normal((2, 600)))
+        x = x.astype(np.complex64)
+        llr = np.asarray(compute_llr(x, noise_var=nv, constellation=c), np.float32)
+        out[f"{name}_llrs"], out[f"{name}_bits"] = llr, bits
+        out[f"{name}_gmi2"] = np.asarray(gmi(llr, bits, constellation=c), np.float64)
+        out[f"{name}_ngmi2"] = np.asarray(ngmi(llr, bits, constellation=c), np.float64)
+        out[f"{name}_gmi1"] = np.float64(gmi(llr[0], bits[0], constellation=c))
+        out[f"{name}_gmi1_skip"] = np.float64(gmi(llr[0], bits[0], constellation=c, num_skip_symbols=5))
+    return out
 
 
 # Constellations of the M-point and prior-weighted demapping paths:
@@ -417,6 +450,14 @@ def main(ref: str, only: str | None = None) -> None:
             res = pool.submit(dvbs2_case, ref).result()
         np.savez_compressed(HERE / "dvbs2_normal.npz", **res)
         print(f"DVB-S2 fixtures written in {time.time() - t0:.0f} s")
+        return
+    if only == "gmi":
+        import multiprocessing as mp
+
+        with ProcessPoolExecutor(max_workers=1, mp_context=mp.get_context("spawn")) as pool:
+            res = pool.submit(gmi_case, ref).result()
+        np.savez_compressed(HERE / "gmi_golden.npz", **res)
+        print(f"GMI fixtures written in {time.time() - t0:.0f} s")
         return
     if only == "mpoint":
         import multiprocessing as mp
