@@ -5,7 +5,9 @@
 under the reference's own names, so commkit's unchanged ``compute_llr`` and
 ``decode`` (``commkit/mapping/_demap.py:330,349``,
 ``commkit/coding/ldpc.py:566-581``) launch the sm_103a kernels on their CuPy
-arrays.  ``uninstall()`` restores the previous factories.
+arrays: every constellation's demapper (``llr`` for non-separable ones,
+the two separable ones) and both LDPC check rules (``ldpc_layered`` with
+``sum_product`` False or True).  ``uninstall()`` restores the previous factories.
 """
 
 from __future__ import annotations
@@ -15,7 +17,7 @@ from typing import Any
 
 from . import _cuda
 
-NAMES = ("llr_separable_maxlog", "llr_separable", "ldpc_layered")
+NAMES = ("llr", "llr_separable_maxlog", "llr_separable", "ldpc_layered")
 
 _saved: dict[str, Any] = {}
 
