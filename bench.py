@@ -63,14 +63,25 @@ WORKLOADS = {
     "A": dict(code="A", frames=1024, order=4, method="exact", ebn0=2.5, max_it=20,
               desc="code A (12x24 base, Z=54, N=1296, K=648), 1024 frames, QPSK exact LLRs, "
                    "Eb/N0 2.5 dB, MinSum 20 it"),
+    "demapper": dict(desc="separable demapper: 2^22 symbols, 1024 frames x 4096, per-frame Es/N0 U[8,20] dB, "
+                          "16- and 64-QAM, max-log and exact"),
+    "mpoint": dict(desc="M-point demapper: 16-PSK, 128-cross-QAM, 8-QAM at 2^22 symbols, max-log and exact"),
     "dvbs2": dict(frames=64, max_it=50,
                   desc="the reference's LDPC benchmark: DVB-S2 normal frame rate 1/2 (N=64800, K=32400), "
                        "64 QPSK codewords at Es/N0 1.5 dB, one decode() call, MinSum() and SumProduct() defaults"),
     "served": dict(max_it=50,
                    desc="served stream: Poisson arrivals of 1-256 frames (log-uniform), codes A/B/C 50/35/15 "
                         "on QPSK/16-QAM/64-QAM, Es/N0 near each waterfall, MinSum 50 it, 4 GiB admission "
-                        "budget, load 10-100% of measured saturation"),
+                        "budget over 6 batch slots, load 10-100% of measured saturation"),
 }  # fmt: skip
+
+
+# DRAM traffic of the mixed decoder, dram__bytes_read.sum + dram__bytes_write.sum from one ncu
+# capture (--set full) of a 2048-frame batch of the same mix on GB300: 33.48 + 27.86 MB.  It grows
+# with the frames, so a launch's traffic is scaled by its frame count.
+MIXED_DRAM_BYTES_PER_FRAME = (33.480448e6 + 27.857920e6) / 2048
+MIXED_TRAFFIC_NOTE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of a 2048-frame launch of the same mix, "
+                      "scaled by frames (61.3 MB / 2048 frames)")
 
 
 def parse() -> argparse.Namespace:
@@ -330,8 +341,9 @@ def measure_mixed(args, dist: Dist) -> dict:
     method = ck.MinSum(max_iterations=w["max_it"])
     names = list(work)
     codes = {n: ck.LDPCCode.quasi_cyclic(W.CODES[n].base(), lifting=W.CODES[n].z) for n in names}
-    for n in names:
-        tuning.tune(codes[n], device=dev.index)
+    for n in names:  # tuned launch shapes: from the cache when this GPU has tuned the code before
+        if not tuning.apply_cached(codes[n], codes[n]._plan(dev.index), dev.index):
+            tuning.tune(codes[n], device=dev.index)
     consts = {n: ck.Constellation.qam(W.MIXED_ORDERS[n]) for n in names}
     rx = MixedReceiver([CodeSlot(codes[n], consts[n], work[n].symbols.shape[0], method) for n in names], dev)
     sym_host = [torch.from_numpy(work[n].symbols).pin_memory() for n in names]
@@ -368,9 +380,24 @@ def measure_mixed(args, dist: Dist) -> dict:
     reps = max(3, args.steps)
     dec_ms = timed(dist, dec_only, reps) / reps
 
+    # End to end, zero-copy: the same graph with the symbol buffers and the
+    # outputs in pinned host memory.  Every step the demapper reads the
+    # symbols from host memory and the decoder writes every result (LLRs,
+    # bits, iterations, flags) back to it over NVLink-C2C.
+    rx_io = MixedReceiver([CodeSlot(codes[n], consts[n], work[n].symbols.shape[0], method) for n in names], dev,
+                          host_io=True)  # fmt: skip
+    rx_io.load(sym_host, nv)
+    rx_io.capture()
+    for _ in range(max(1, args.warmup)):
+        rx_io.run()
+    e2e_ms = timed(dist, rx_io.run, args.steps)
+    host_same = all(np.array_equal(a.cpu().numpy(), b.numpy()) for r, h in zip(rx.outputs, rx_io.outputs, strict=True)
+                    for a, b in zip(r, h, strict=True))  # fmt: skip
+
+    # The same with explicit copies: symbols host -> device, results device -> host.
     outs = [tuple(torch.empty(t.shape, dtype=t.dtype, pin_memory=True) for t in o) for o in rx.outputs]
 
-    def e2e_step():
+    def copy_step():
         for i in range(len(names)):
             rx.sym[i].copy_(sym_host[i], non_blocking=True)
         rx.run()
@@ -379,8 +406,8 @@ def measure_mixed(args, dist: Dist) -> dict:
                 a.copy_(b, non_blocking=True)
 
     for _ in range(max(1, args.warmup)):
-        e2e_step()
-    e2e_ms = timed(dist, e2e_step, args.steps)
+        copy_step()
+    copy_ms = timed(dist, copy_step, args.steps)
 
     parity_ok, fer, iters = True, {}, {}
     oracle.build()
@@ -423,10 +450,18 @@ def measure_mixed(args, dist: Dist) -> dict:
         "e2e": {"value": dist.world * info_bits * args.steps / (e2e_ms * 1e-3) / 1e9, "unit": UNIT,
                 "h2d_bytes_per_step": int(sum(s.numel() * 8 for s in sym_host)),
                 "d2h_bytes_per_step": int(sum(sum(t.numel() * t.element_size() for t in o) for o in outs)),
-                "ms_per_step": e2e_ms / args.steps},
+                "ms_per_step": e2e_ms / args.steps,
+                "form": "MixedReceiver(host_io=True): symbols read from and results written to pinned host "
+                        "memory by the kernels each step (NVLink-C2C), graph replay",
+                "bit_identical_to_device": bool(host_same),
+                "with_copies": {"value": dist.world * info_bits * args.steps / (copy_ms * 1e-3) / 1e9,
+                                "ms_per_step": copy_ms / args.steps,
+                                "form": "copy_ in, graph replay, copy_ out (pinned host buffers)"}},
         "gpu_launches": (len(names) + 1) * args.steps,
-        "roofline": roofline(pk, alg_bytes, edge_updates, dec_ms, sm_count, clocks.get("sm_mhz") or pk["sm_max_mhz"],
-                             "ck mixed decoder (ldpc_mixed_kernel)"),
+        "roofline": dict(roofline(pk, alg_bytes, edge_updates, dec_ms, sm_count, clocks.get("sm_mhz") or pk["sm_max_mhz"],
+                                  "ck mixed decoder (ldpc_mixed_kernel)"),
+                         traffic=MIXED_DRAM_BYTES_PER_FRAME * sum(int(work[n].symbols.shape[0]) for n in names),
+                         traffic_source=MIXED_TRAFFIC_NOTE),
         "decode": {"fer": fer, "iterations_min_mean_max": iters},
         "parity": {"frames_checked": 16 * len(names), "bit_exact": bool(parity_ok)},
         "clocks": clocks,
@@ -444,7 +479,8 @@ def measure_single(args, dist: Dist, wname: str) -> dict:
     frames = args.frames if args.workload == wname else w["frames"]
     spec = W.CODES[w["code"]]
     code = ck.LDPCCode.quasi_cyclic(spec.base(), lifting=spec.z)
-    tuning.tune(code, device=dev.index)
+    if not tuning.apply_cached(code, code._plan(dev.index), dev.index):
+        tuning.tune(code, device=dev.index)
     const = ck.Constellation.qam(w["order"])
     method = ck.MinSum(max_iterations=w["max_it"])
     batch = W.coded_batch(spec, frames, w["order"], w["ebn0"], seed=SEED + dist.rank)
@@ -542,6 +578,40 @@ def measure_demapper(dist: Dist) -> dict:
     return {"workload": "2^22 symbols, 1024 frames x 4096, per-frame Es/N0 U[8,20] dB, one launch", "results": out}
 
 
+def measure_mpoint(dist: Dist) -> dict:
+    """The M-point demapper (constellations without per-axis factors) at
+    2^22 symbols: 16-PSK and 128-cross-QAM, the reference's non-separable
+    benchmark constellations (``benchmarks/bench_llr.py:38-51``, there at
+    2^18 symbols), and 8-QAM; max-log and exact; the L2 is flushed before
+    every launch (its inputs are smaller than L2)."""
+    import commkit_gb300 as ck
+
+    torch, dev = dist.torch, dist.dev
+    pk = peaks()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    out = {}
+    for name, c in (("psk16", ck.Constellation.psk(16)), ("qam128_cross", ck.Constellation.qam(128)),
+                    ("qam8", ck.Constellation.qam(8))):  # fmt: skip
+        n = 1 << 22
+        rng = np.random.default_rng(5)
+        x = c.points[rng.integers(0, c.order, n)] + 0.1 * (rng.standard_normal(n) + 1j * rng.standard_normal(n))
+        xd = torch.from_numpy(x.astype(np.complex64)).to(dev)
+        for method in ("maxlog", "exact"):
+            for _ in range(3):
+                ck.compute_llr(xd, noise_var=0.05, constellation=c, method=method)
+            times = []
+            for _ in range(10):
+                flush.zero_()
+                times.append(timed(dist, lambda c=c, method=method: ck.compute_llr(
+                    xd, noise_var=0.05, constellation=c, method=method), 1))  # fmt: skip
+            ms = float(np.median(times))
+            nbytes = n * (8 + 4 * c.bits_per_symbol)
+            out[f"{name}_{method}"] = {"us": ms * 1e3, "gsym_per_s": n / (ms * 1e-3) / 1e9,
+                                       "gbs": nbytes / (ms * 1e-3) / 1e9,
+                                       "frac": nbytes / (ms * 1e-3) / 1e9 / pk["hbm_gbs"]}  # fmt: skip
+    return {"workload": "M-point demapping, 2^22 symbols per call (public compute_llr, L2 flushed)", "results": out}
+
+
 def measure_dvbs2(dist: Dist, steps: int = 10, warmup: int = 3) -> dict:
     """The reference's own LDPC benchmark (``benchmarks/bench_coding.py:37-38,
     55-56,75-86``): 64 DVB-S2 normal-frame rate-1/2 codewords over QPSK at
@@ -601,21 +671,31 @@ def measure_served(args, dist: Dist) -> dict:
                              seed=7)  # fmt: skip
     t_build = time.perf_counter() - t_build
     codes = {n: ck.LDPCCode.quasi_cyclic(W.CODES[n].base(), lifting=W.CODES[n].z) for n in "ABC"}
+    slots = int(os.environ.get("CK_SERVE_SLOTS", "6"))
     server = Server(codes, ck.MinSum(max_iterations=WORKLOADS["served"]["max_it"]), hbm_budget=4 << 30,
-                    max_inflight=3, device=dev)  # fmt: skip
+                    max_inflight=slots, device=dev)  # fmt: skip
     k_of = {n: c.k for n, c in codes.items()}
 
     def info_bits(reqs):
         return sum(r.frames * k_of[r.code] for r in reqs)
 
     server.serve(poisson_requests(1e5, 0.002, pool, seed=1))  # warm-up
+    # Saturation: the sustained completion rate under overload.  A first
+    # backlog (everything arrived at once) gives a rough rate; then requests
+    # arrive at 3x that rate for 0.5 s, and the rate is what the server
+    # completes from the first arrival until the backlog has drained.
     backlog = poisson_requests(1e6, 4e-4, pool, seed=2)
     for r in backlog:
         r.arrival = 0.0
     t0 = time.perf_counter()
     server.serve(backlog)
+    rough = len(backlog) / (time.perf_counter() - t0)
+    over = poisson_requests(3.0 * rough, 0.5, pool, seed=3)
+    t0 = time.perf_counter()
+    server.serve(over)
     sat_s = time.perf_counter() - t0
-    sat_rate = len(backlog) / sat_s
+    sat_rate = len(over) / sat_s
+    backlog = over
     duration = float(os.environ.get("CK_SERVE_SECONDS", "1.5"))
     sweep = {}
     with Clocks(dev.index) as clk:
@@ -630,12 +710,15 @@ def measure_served(args, dist: Dist) -> dict:
                 "gbps": info_bits(done) / wall / 1e9, "p50_ms": float(np.percentile(lat, 50)),
                 "p99_ms": float(np.percentile(lat, 99)), "p999_ms": float(np.percentile(lat, 99.9)),
                 "max_ms": float(lat.max()),
+                "p99_ms_by_code": {c: float(np.percentile([r.latency * 1e3 for r in done if r.code == c], 99))
+                                   for c in "ABC" if any(r.code == c for r in done)},
             }  # fmt: skip
     return {
         "workload": WORKLOADS["served"]["desc"],
         "saturation": {"gbps": info_bits(backlog) / sat_s / 1e9, "requests_per_s": sat_rate,
-                       "requests": len(backlog), "frames": int(sum(r.frames for r in backlog))},
-        "latency_vs_load": sweep, "p99_ms_at_70pct": sweep["70%"]["p99_ms"],
+                       "requests": len(backlog), "frames": int(sum(r.frames for r in backlog)),
+                       "method": "overload at 3x a backlog estimate for 0.5 s, completed / wall until drained"},
+        "latency_vs_load": sweep, "p99_ms_at_70pct": sweep["70%"]["p99_ms"], "batch_slots": slots,
         "pool_build_s": t_build, "clocks": clk.summary(),
     }  # fmt: skip
 
@@ -648,6 +731,20 @@ def main() -> None:
     dist = Dist()
     if args.workload == "mixed":
         line = measure_mixed(args, dist)
+    elif args.workload == "demapper":
+        dm = measure_demapper(dist)
+        r = dm["results"]["qam16_maxlog"]
+        line = {"metric": "demapper HBM throughput", "value": r["gbs"], "unit": "GB/s", "n_gpus": 1, "steps": 10,
+                "warmup": 3, "ms_per_step": r["us"] / 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+                "config": {"workload": dm["workload"]}, "demapper": dm}  # fmt: skip
+    elif args.workload == "mpoint":
+        mp_ = measure_mpoint(dist)
+        r = mp_["results"]["qam128_cross_maxlog"]
+        line = {"metric": "M-point LLR throughput", "value": r["gsym_per_s"], "unit": "Gsymbols/s", "n_gpus": 1,
+                "steps": 10, "warmup": 3, "ms_per_step": r["us"] / 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+                "config": {"workload": mp_["workload"]}, "mpoint": mp_}  # fmt: skip
     elif args.workload == "dvbs2":
         dv = measure_dvbs2(dist, args.steps, args.warmup)
         ms = dv["min_sum"]["ms"]
@@ -671,7 +768,7 @@ def main() -> None:
                 "gpu_launches": 2 * args.steps, "roofline": s["roofline"], "demapper": s["demapper"],
                 "decode": s["decode"], "parity": s["parity"]}  # fmt: skip
     if dist.rank == 0:
-        if not args.no_cpu_baseline and args.workload not in ("served", "dvbs2"):
+        if not args.no_cpu_baseline and args.workload not in ("served", "dvbs2", "mpoint", "demapper"):
             sample, threads, desc = cpu_sample(args, 10.0)
             t, bits = oracle_step(sample, args.w["max_it"], threads, args.w.get("method", "maxlog"))
             line["cpu_baseline"] = {"value": bits / t / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
@@ -681,6 +778,7 @@ def main() -> None:
             for key, fn in (("3", lambda: measure_single(args, dist, "C")),
                             ("1", lambda: measure_single(args, dist, "A")),
                             ("2", lambda: measure_demapper(dist)),
+                            ("2_mpoint", lambda: measure_mpoint(dist)),
                             ("reference_ldpc_benchmark", lambda: measure_dvbs2(dist)),
                             ("5", lambda: measure_served(args, dist))):  # fmt: skip
                 try:

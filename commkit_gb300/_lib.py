@@ -45,6 +45,8 @@ EXPORTS = (
     "ck_map_awgn",
     "ck_count_errors",
     "ck_gmi_loss",
+    "ck_gather",
+    "ck_host_acquire",
     "ck_ldpc_schedule",
     "ck_ldpc_plan_create",
     "ck_ldpc_plan_destroy",
@@ -150,6 +152,8 @@ def _declare(lib: ctypes.CDLL) -> None:
                         ctypes.c_int),
         "ck_count_errors": ([p, p, p, p, i64, i32, i32, p, p, p, p], ctypes.c_int),
         "ck_gmi_loss": ([p, p, i64, i64, p, p], ctypes.c_int),
+        "ck_gather": ([p, i32, p], ctypes.c_int),
+        "ck_host_acquire": ([], None),
         "ck_ldpc_schedule": ([p, p, i64, i32, i32, p, p, p, ctypes.POINTER(i32)], ctypes.c_int),
         "ck_ldpc_plan_create": ([p, p, p, i32, i32, i32, ctypes.POINTER(p)], ctypes.c_int),
         "ck_ldpc_plan_destroy": ([p], ctypes.c_int),

@@ -41,6 +41,11 @@
 #include <string.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <set>
+#include <tuple>
+#include <utility>
 
 #include "ck_ldpc_kernel.cuh"
 
@@ -428,9 +433,15 @@ __device__ void mixed_frames(const MixedCode& K, unsigned char* smem, const int3
             int8_t* bdst = K.bits + static_cast<size_t>(f) * K.k_bits;
             for (int i = tid; i < K.k_bits; i += K.T) bdst[i] = a[i] < 0.0f ? 1 : 0;
         }
+        // The iteration count is written last, after a system-scope fence
+        // that follows the group's writes: a host that reads it from mapped
+        // memory (the request server polls frames as they finish) then also
+        // sees the frame's LLRs, bits and flag.
+        group_sync(bar, K.T);
         if (tid == 0) {
-            K.iters[f] = it;
             K.valid[f] = ok ? 1 : 0;
+            __threadfence_system();
+            K.iters[f] = it;
         }
         group_sync(bar, K.T);
     }
@@ -498,9 +509,43 @@ int device_limits(int dev, int* sms, int* smem_optin) {
 // Launch shape, shared-memory layout, grid and workspace of a decode of B
 // frames by `rule`; a pure function of the plan, its launch setting, the
 // rule and B.
+int resolve_shape(const ck_ldpc_plan* plan, int32_t rule, Resolved* r, int* per_sm_out, int* sms_out);
+
 int resolve(const ck_ldpc_plan* plan, int32_t rule, int64_t B, Resolved* r) {
     if (rule != CK_LDPC_MIN_SUM && rule != CK_LDPC_SUM_PRODUCT)
         return ck::fail(CK_ERR_INVALID_ARGUMENT, "unknown check rule %d", rule);
+    static_assert(sizeof(Resolved) <= sizeof(plan->shape_cache[0].resolved), "shape cache too small");
+    int per_sm = 0, sms = 0;
+    {
+        std::lock_guard<std::mutex> lock(plan->shape_mu);
+        auto& c = plan->shape_cache[rule];
+        if (c.valid && memcmp(&c.launch, &plan->launch, sizeof(ck_ldpc_launch)) == 0) {
+            memcpy(static_cast<void*>(r), c.resolved, sizeof(Resolved));
+            per_sm = c.per_sm;
+            sms = c.sms;
+        } else {
+            CK_TRY(resolve_shape(plan, rule, r, &per_sm, &sms));
+            memcpy(c.resolved, static_cast<const void*>(r), sizeof(Resolved));
+            c.launch = plan->launch;
+            c.per_sm = per_sm;
+            c.sms = sms;
+            c.valid = true;
+        }
+    }
+    const int32_t G = r->G;
+    const int64_t need = (B + G - 1) / G;
+    r->grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(need, int64_t(sms) * per_sm)));
+    const size_t slots = static_cast<size_t>(r->grid) * G;
+    r->r_ws_off = kHeaderBytes;
+    const size_t r_ws = slots * r->r_slot_bytes;
+    r->app_ws_off = kHeaderBytes + ((r_ws + 255) / 256) * 256;
+    const size_t app_ws = r->app_smem ? 0 : slots * static_cast<size_t>(r->app_stride) * 4;
+    r->ws_bytes = r->app_ws_off + app_ws;
+    return CK_OK;
+}
+
+// Everything of a decode's launch that does not depend on the frame count.
+int resolve_shape(const ck_ldpc_plan* plan, int32_t rule, Resolved* r, int* per_sm_out, int* sms_out) {
     const bool sp = rule == CK_LDPC_SUM_PRODUCT;
     int sms = 0, optin = 0;
     CK_TRY(device_limits(plan->device, &sms, &optin));
@@ -577,11 +622,10 @@ int resolve(const ck_ldpc_plan* plan, int32_t rule, int64_t B, Resolved* r) {
     KernelFn kernel = sp ? sum_product_kernel(plan->qc, plan->max_deg, app_smem, r_smem)
                          : min_sum_kernel(plan->qc, plan->max_deg, app_smem, r_smem);
     if (!kernel) return ck::fail(CK_ERR_UNSUPPORTED, "no decoder kernel for this code shape");
+    CK_TRY(ck::allow_max_smem(reinterpret_cast<const void*>(kernel), plan->device, optin));
     if (G == 0) {
         // The most resident frames per SM (registers, shared memory, threads),
         // the smaller block on a tie.
-        CK_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void*>(kernel),
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
         int best = 0;
         for (int32_t g = 1; g <= gmax; ++g) {
             int per_sm = 0;
@@ -614,9 +658,6 @@ int resolve(const ck_ldpc_plan* plan, int32_t rule, int64_t B, Resolved* r) {
     r->smem = tables + static_cast<uint32_t>(G) * group;
     r->app_stride = static_cast<int32_t>(app_bytes / 4);
 
-    CK_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void*>(r->kernel),
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(r->smem)));
     int per_sm = 0;
     CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &per_sm, reinterpret_cast<const void*>(r->kernel), T * G, r->smem));
@@ -625,15 +666,9 @@ int resolve(const ck_ldpc_plan* plan, int32_t rule, int64_t B, Resolved* r) {
                         "decoder block of %d threads and %u bytes of shared memory does not fit "
                         "an SM",
                         T * G, r->smem);
-    const int64_t need = (B + G - 1) / G;
-    r->grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(need, int64_t(sms) * per_sm)));
-    const size_t slots = static_cast<size_t>(r->grid) * G;
     r->r_slot_bytes = r_smem ? 0 : r_bytes_dev;
-    r->r_ws_off = kHeaderBytes;
-    const size_t r_ws = slots * r->r_slot_bytes;
-    r->app_ws_off = kHeaderBytes + ((r_ws + 255) / 256) * 256;
-    const size_t app_ws = app_smem ? 0 : slots * app_bytes;
-    r->ws_bytes = r->app_ws_off + app_ws;
+    *per_sm_out = per_sm;
+    *sms_out = sms;
     return CK_OK;
 }
 
@@ -954,11 +989,24 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
         return ck::fail(CK_ERR_UNSUPPORTED, "mixed launch of %d threads with rows above degree 16",
                         R->block_threads);
     KernelMixed kernel = R->wide ? ldpc_mixed_kernel<27> : ldpc_mixed_kernel<16>;
-    CK_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void*>(kernel),
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(R->smem)));
+    CK_TRY(ck::allow_max_smem(reinterpret_cast<const void*>(kernel), dev, optin));
     int per_sm = 0;
-    CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(kernel),
-                                                          R->block_threads, R->smem));
+    {
+        // Occupancy per (kernel, device, block shape), remembered: the
+        // request server launches a mixed batch per admission.
+        static std::mutex mu;
+        static std::map<std::tuple<const void*, int, int, uint32_t>, int> known;
+        const auto key = std::make_tuple(reinterpret_cast<const void*>(kernel), dev, R->block_threads, R->smem);
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = known.find(key);
+        if (it != known.end()) {
+            per_sm = it->second;
+        } else {
+            CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(kernel),
+                                                                  R->block_threads, R->smem));
+            known[key] = per_sm;
+        }
+    }
     if (per_sm < 1) return ck::fail(CK_ERR_UNSUPPORTED, "mixed block does not fit an SM");
     int64_t need = 0;
     for (int c = 0; c < n; ++c)
@@ -1040,4 +1088,19 @@ extern "C" int ck_ldpc_decode_mixed(const ck_ldpc_batch* batches, int32_t num_ba
         if (status == CK_OK) status = st;
     }
     return status;
+}
+
+int ck::allow_max_smem(const void* kernel, int device, int optin) {
+    static std::mutex mu;
+    static std::set<std::pair<const void*, int>> done;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done.count({kernel, device})) return CK_OK;
+    // The limit covers dynamic shared memory only: the opt-in maximum less
+    // the kernel's static shared variables.
+    cudaFuncAttributes attr;
+    CK_CUDA(cudaFuncGetAttributes(&attr, kernel));
+    const int dynamic = optin - static_cast<int>(attr.sharedSizeBytes);
+    CK_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dynamic));
+    done.insert({kernel, device});
+    return CK_OK;
 }

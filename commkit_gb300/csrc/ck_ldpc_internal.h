@@ -3,6 +3,7 @@
 
 #include <stdint.h>
 
+#include <mutex>
 #include <vector>
 
 #include "ck_common.cuh"
@@ -54,4 +55,23 @@ struct ck_ldpc_plan {
     int32_t* d_cols = nullptr;
     ck::FastDiv divZ{1, 1, 0};
     ck_ldpc_launch launch{0, 0, 0};
+    // The decoder's launch shape per check rule for the current launch
+    // setting (everything but the grid, which depends on the frame count),
+    // resolved on first use: later calls skip the occupancy queries.
+    struct ShapeCache {
+        bool valid = false;
+        ck_ldpc_launch launch{0, 0, 0};
+        int per_sm = 0, sms = 0;
+        alignas(16) unsigned char resolved[192];
+    };
+    mutable ShapeCache shape_cache[2];
+    mutable std::mutex shape_mu;
 };
+
+namespace ck {
+// Raises a kernel's dynamic shared-memory limit to the device's opt-in
+// maximum (less its static shared memory), once per kernel and device (a
+// limit set per call would let plans sharing the kernel lower it under one
+// another).
+int allow_max_smem(const void* kernel, int device, int optin);
+}  // namespace ck

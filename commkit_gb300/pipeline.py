@@ -1,12 +1,20 @@
 """Device-resident receiver pipelines: demap + decode with no per-step allocation.
 
 :class:`MixedReceiver` holds, per code, the symbol buffer, the per-frame
-``1/sigma^2``, the LLRs, the decoder outputs and one shared workspace on the
-device.  A step demaps every code's frames (``compute_llr_frames``) and
-decodes all of them in ONE launch of the mixed-code persistent kernel
-(``decode_mixed``).  Nothing is allocated or copied from the host inside a
-step, so :meth:`capture` records it once as a CUDA graph and :meth:`run`
-replays it: one graph launch per batch of mixed traffic.
+``1/sigma^2``, the LLRs, the decoder outputs and one shared workspace.  A
+step demaps every code's frames (``compute_llr_frames``) and decodes all of
+them in ONE launch of the mixed-code persistent kernel (``decode_mixed``).
+Nothing is allocated or copied inside a step, so :meth:`capture` records it
+once as a CUDA graph and :meth:`run` replays it: one graph launch per batch
+of mixed traffic.
+
+With ``host_io=True`` the symbol buffers and the outputs are pinned host
+memory instead (GB300's Grace memory is coherent with the GPU over
+NVLink-C2C, with one address on both sides): the demapper reads the
+received symbols where the host put them and the decoder writes each
+frame's results straight into host memory, so a step needs no copy in
+either direction.  The LLRs, the noise scales and the message state stay in
+HBM.
 """
 
 from __future__ import annotations
@@ -19,7 +27,7 @@ import numpy as np
 
 from . import _device, _lib
 from .coding import DecodeResult, LDPCCode, MinSum, decode_mixed
-from .mapping import Constellation, compute_llr_frames, inv_s2_frames
+from .mapping import Constellation, _axis_struct, _table_kind, compute_llr_frames, device_tables, inv_s2_frames
 
 
 @dataclass
@@ -36,7 +44,7 @@ class CodeSlot:
 class MixedReceiver:
     """Demap + mixed-code decode of fixed-size batches on one CUDA device."""
 
-    def __init__(self, slots: list[CodeSlot], device: Any = None):
+    def __init__(self, slots: list[CodeSlot], device: Any = None, host_io: bool = False):
         import torch
 
         if not slots or len(slots) > 4:
@@ -44,20 +52,22 @@ class MixedReceiver:
         self.torch = torch
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         self.slots = slots
+        self.host_io = bool(host_io)
+        io = {"pin_memory": True} if self.host_io else {"device": self.device}
         self.sym, self.s2, self.llr, self.outputs = [], [], [], []
         for s in slots:
             k = s.constellation.bits_per_symbol
             if s.code.n % k:
                 raise ValueError(f"n = {s.code.n} is not a multiple of {k} bits per symbol")
             S = s.code.n // k
-            self.sym.append(torch.zeros((s.frames, S), dtype=torch.complex64, device=self.device))
+            self.sym.append(torch.zeros((s.frames, S), dtype=torch.complex64, **io))
             self.s2.append(torch.ones((s.frames,), dtype=torch.float32, device=self.device))
             self.llr.append(torch.empty((s.frames, s.code.n), dtype=torch.float32, device=self.device))
             self.outputs.append((
-                torch.empty((s.frames, s.code.n), dtype=torch.float32, device=self.device),
-                torch.empty((s.frames, s.code.k), dtype=torch.int8, device=self.device),
-                torch.empty((s.frames,), dtype=torch.int32, device=self.device),
-                torch.empty((s.frames,), dtype=torch.uint8, device=self.device),
+                torch.empty((s.frames, s.code.n), dtype=torch.float32, **io),
+                torch.empty((s.frames, s.code.k), dtype=torch.int8, **io),
+                torch.empty((s.frames,), dtype=torch.int32, **io),
+                torch.empty((s.frames,), dtype=torch.uint8, **io),
             ))  # fmt: skip
         self.workspace = torch.empty(max(self._workspace_bytes(), 256), dtype=torch.uint8, device=self.device)
         self.graph = None
@@ -82,7 +92,11 @@ class MixedReceiver:
 
     def load(self, symbols: list, noise_var: list) -> None:
         """Stage one batch: per slot ``(frames, S)`` complex64 symbols (host
-        or device) and per-frame noise variances (host)."""
+        or device) and per-frame noise variances (host).  With ``host_io``
+        the symbols go into the pinned host buffers, after the device has
+        finished the steps queued before (which may still read them)."""
+        if self.host_io:
+            self.torch.cuda.current_stream(self.device).synchronize()
         for i, (x, nv) in enumerate(zip(symbols, noise_var, strict=True)):
             t = x if isinstance(x, self.torch.Tensor) else self.torch.from_numpy(np.ascontiguousarray(x))
             self.sym[i].copy_(t, non_blocking=True)
@@ -90,11 +104,41 @@ class MixedReceiver:
 
     def step(self) -> None:
         """Demap every slot and decode them all in one mixed launch (no allocation)."""
-        for i, s in enumerate(self.slots):
-            compute_llr_frames(self.sym[i], constellation=s.constellation, method=s.demap,
-                               inv_s2=self.s2[i], out=self.llr[i])  # fmt: skip
-        decode_mixed([(self.llr[i], s.code, s.method) for i, s in enumerate(self.slots)],
-                     workspace=self.workspace, outputs=self.outputs)  # fmt: skip
+        if not self.host_io:
+            for i, s in enumerate(self.slots):
+                compute_llr_frames(self.sym[i], constellation=s.constellation, method=s.demap,
+                                   inv_s2=self.s2[i], out=self.llr[i])  # fmt: skip
+            decode_mixed([(self.llr[i], s.code, s.method) for i, s in enumerate(self.slots)],
+                         workspace=self.workspace, outputs=self.outputs)  # fmt: skip
+            return
+        # Host I/O: the same kernels, given the pinned host addresses.
+        lib = _lib.lib()
+        like = _device.wrap(self.llr[0])
+        st = _device.stream_of(like)
+        with _device.on_device(like):
+            for i, s in enumerate(self.slots):
+                F, S = self.sym[i].shape
+                kind = _table_kind(s.constellation, s.demap)
+                tabs = device_tables(s.constellation, kind, like)
+                exact = 1 if s.demap == "exact" else 0
+                x, s2, out = self.sym[i].data_ptr(), self.s2[i].data_ptr(), self.llr[i].data_ptr()
+                if kind == "points":
+                    st_ = lib.ck_llr_points_frames(x, F * S, S, s2, tabs[0].data_ptr(), tabs[1].data_ptr(),
+                                                   tabs[2].data_ptr(), s.constellation.order,
+                                                   s.constellation.bits_per_symbol, exact, out, st)  # fmt: skip
+                else:
+                    half = len(tabs) // 2
+                    re, im = _axis_struct(tabs[:half], kind), _axis_struct(tabs[half:], kind)
+                    if kind == "maxlog":
+                        st_ = lib.ck_llr_separable_maxlog_frames(x, F * S, S, s2, ctypes.byref(re),
+                                                                 ctypes.byref(im), out, st)  # fmt: skip
+                    else:
+                        st_ = lib.ck_llr_separable_frames(x, F * S, S, s2, ctypes.byref(re), ctypes.byref(im),
+                                                          exact, out, st)  # fmt: skip
+                _lib.check(st_, "MixedReceiver demap")
+            arr = self._batches()
+            _lib.check(lib.ck_ldpc_decode_mixed(arr, len(self.slots), self.workspace.data_ptr(),
+                                                self.workspace.numel(), st), "MixedReceiver decode")  # fmt: skip
 
     def capture(self, warmup: int = 2) -> None:
         """Record :meth:`step` as a CUDA graph (after ``warmup`` eager steps)."""
@@ -117,6 +161,8 @@ class MixedReceiver:
             self.step()
 
     def results(self) -> list[DecodeResult]:
+        """Each slot's result of the last step (device tensors, or pinned host
+        tensors with ``host_io``; synchronize the stream before reading them)."""
         torch = self.torch
         return [DecodeResult(bits=o[1], llrs=o[0], valid=o[3].view(torch.bool), iterations=o[2], checked=True)
                 for o in self.outputs]  # fmt: skip

@@ -1,27 +1,37 @@
 """A continuous-batching request loop for demap + decode.
 
 Requests carry frames of one code on one constellation with one Es/N0.
-They arrive over time (:func:`poisson_requests` draws a seeded stream). The
-:class:`Server` keeps LLRs and check-message state on the device and admits
-requests whenever the device memory they need fits the HBM budget and a
-batch slot is free. Each batch takes everything admitted since the previous
-one, demaps it per (code, constellation) and decodes every code in ONE
-launch of the mixed-code persistent kernel. Each batch runs on its own
-CUDA stream, so a batch admitted while others are still on the GPU overlaps
-with them; when a batch completes, its memory returns to the budget. Per
-request the server records the latency from arrival to results in host
-memory.
+They arrive over time (:func:`poisson_requests` draws a seeded stream).
+The :class:`Server` keeps LLRs and check-message state on the device and
+admits requests whenever a batch slot is free; a slot's device memory is
+allocated once, so the HBM budget is ``slots x bytes per slot``.  Each
+batch takes the arrived requests that fit one slot, demaps them per (code,
+constellation) and decodes every code in ONE launch of the mixed-code
+persistent kernel, on the slot's own CUDA stream: batches admitted while
+others run overlap with them on the device.
+
+Zero-copy on GB300: the Grace host memory is coherent with the GPU over
+NVLink-C2C and pinned allocations have one address on both sides.  So a
+batch is assembled by one gather kernel that reads every request's pinned
+symbols (and the frames' noise scales) in place, and the decoder writes
+each frame's a-posteriori LLRs, bits, iterations and syndrome flag straight
+into a pinned output arena.  A batch costs one gather launch, one demap
+launch per (code, constellation), one decode launch and an event: no
+per-request copy call, no device-to-host copy, no allocation.
+
+The arena is a ring: request results (:attr:`Request.llrs` etc.) are views
+into it and stay valid until ``output_arena_bytes`` of later results have
+been written; copy them out to keep them longer.  Per request the server
+records the latency from arrival to results in host memory.
 
 The admission and batching policy (:class:`Admission`) is plain Python and
-is tested without a GPU.  Each batch slot holds preallocated device buffers
-and pinned staging, so a batch costs one host-to-device copy of its
-symbols, one of its inverse noise variances, a demap launch per (code,
-constellation), one decode launch and one device-to-host copy per output,
-all on the slot's stream, with no allocation.
+is tested without a GPU.
 """
 
 from __future__ import annotations
 
+import ctypes
+import gc
 import time
 from collections import deque
 from dataclasses import dataclass, field
@@ -29,11 +39,13 @@ from typing import Any
 
 import numpy as np
 
-import ctypes
-
 from . import _lib
 from .coding import LDPCCode, MinSum
-from .mapping import Constellation, inv_s2_frames
+from .mapping import Constellation
+
+# Largest piece of one request's symbols a gather block copies (so one big
+# request spreads over many blocks).
+_CHUNK = 1 << 20
 
 
 @dataclass
@@ -43,7 +55,7 @@ class Request:
     rid: int
     code: str
     order: int
-    symbols: Any  # (F, S) complex64, host (ideally pinned)
+    symbols: Any  # (F, S) complex64: a pinned host tensor (read in place) or a CUDA tensor
     noise_var: float
     arrival: float = 0.0  # seconds from the stream's start
     # filled by the server
@@ -101,10 +113,41 @@ class Admission:
         self.free += 1
 
 
+class OutputArena:
+    """A ring of pinned host memory the decoder writes results into.
+
+    ``alloc`` hands out 256-byte aligned regions in order, wrapping at the
+    end; a region still being written by a batch in flight is never handed
+    out again (``busy(lo, hi)`` reports such regions, and the caller waits
+    for them).
+    """
+
+    def __init__(self, nbytes: int):
+        import torch
+
+        self.buf = torch.empty(int(nbytes), dtype=torch.uint8, pin_memory=True)
+        self.np = self.buf.numpy()
+        self.np[:: 1 << 12] = 0  # touch every page once before serving
+        self.base = self.buf.data_ptr()
+        self.size = int(nbytes)
+        self.head = 0
+
+    def alloc(self, nbytes: int, busy) -> int:
+        n = (int(nbytes) + 255) // 256 * 256
+        if n > self.size:
+            raise MemoryError(f"a batch's results ({n} bytes) exceed the {self.size}-byte output arena")
+        if self.head + n > self.size:
+            self.head = 0
+        off = self.head
+        busy(off, off + n)  # waits for batches still writing there
+        self.head = off + n
+        return off
+
+
 class _Slot:
     """One batch slot: device buffers, pinned staging and a stream."""
 
-    def __init__(self, server: Server, caps: dict[str, int], sym_bytes: int):
+    def __init__(self, server: Server, caps: dict[str, int], sym_bytes: int, max_segments: int):
         torch = server.torch
         dev = server.device
         self.stream = torch.cuda.Stream(dev)
@@ -113,36 +156,39 @@ class _Slot:
         self.sym_dev = torch.empty(sym_bytes // 8, dtype=torch.complex64, device=dev)
         self.s2_dev = torch.empty(total, dtype=torch.float32, device=dev)
         self.s2_host = torch.empty(total, dtype=torch.float32, pin_memory=True)
-        self.llr, self.out_dev, self.out_host = {}, {}, {}
+        self.s2_np = self.s2_host.numpy()
+        self.segs = torch.empty(max_segments * 3, dtype=torch.int64, pin_memory=True)
+        self.segs_np = self.segs.numpy().reshape(max_segments, 3)
+        self.max_segments = max_segments
+        self.llr = {}
         for name, cap in caps.items():
-            code = server.codes[name]
-            self.llr[name] = torch.empty((cap, code.n), dtype=torch.float32, device=dev)
-            shapes = (((cap, code.n), torch.float32), ((cap, code.k), torch.int8), ((cap,), torch.int32),
-                      ((cap,), torch.uint8))  # fmt: skip
-            self.out_dev[name] = [torch.empty(sh, dtype=dt, device=dev) for sh, dt in shapes]
-        arr = server._batch_array({name: (cap, self) for name, cap in caps.items()})
+            self.llr[name] = torch.empty((cap, server.codes[name].n), dtype=torch.float32, device=dev)
+        arr = server._batch_array({name: cap for name, cap in caps.items()}, self, {})
         need = ctypes.c_size_t(0)
         _lib.check(_lib.lib().ck_ldpc_mixed_workspace_size(arr, len(caps), ctypes.byref(need)), "server slot")
         self.ws = torch.empty(max(int(need.value), 256), dtype=torch.uint8, device=dev)
         self.bytes = (self.sym_dev.numel() * 8 + self.s2_dev.numel() * 4 + self.ws.numel()
-                      + sum(t.numel() * t.element_size() for v in self.out_dev.values() for t in v)
                       + sum(t.numel() * 4 for t in self.llr.values()))  # fmt: skip
         self.event = torch.cuda.Event()
         self.batch: list = []
         self.layout: list = []
-        self.counts: dict[str, int] = {}
+        self.region: tuple[int, int] | None = None
+        self.out: dict = {}
+        self.waiting: list = []
 
 
 class Server:
     """Demap + decode server on one CUDA device (see the module docstring).
 
     ``frames_per_slot`` caps each code's frames in one batch; the slots'
-    device memory (``slots`` of them) must fit ``hbm_budget``.
+    device memory (``max_inflight`` of them) must fit ``hbm_budget``.
+    ``output_arena_bytes`` sizes the pinned result ring (by default two
+    full batches of every slot).
     """
 
     def __init__(self, codes: dict[str, LDPCCode], method: MinSum, *, hbm_budget: int = 4 << 30,
                  max_inflight: int = 3, device: Any = None, frames_per_slot: dict | None = None,
-                 orders=(4, 16, 64)):  # fmt: skip
+                 orders=(4, 16, 64), output_arena_bytes: int | None = None):  # fmt: skip
         import torch
 
         self.torch = torch
@@ -159,22 +205,32 @@ class Server:
             share = max(0, hbm_budget // max_inflight - ws) // len(codes)
             frames_per_slot = {}
             for name, code in codes.items():
-                per_frame = (code.n // kmin) * 8 + 4 + 8 * code.n + code.k + 8
+                per_frame = (code.n // kmin) * 8 + 4 + 4 * code.n
                 frames_per_slot[name] = max(1, int(share // per_frame))
         self.caps = {name: int(frames_per_slot[name]) for name in codes}
         sym_bytes = sum(cap * (codes[n].n // kmin) * 8 for n, cap in self.caps.items())
         self._sym_cap = sym_bytes // 8
+        out_per_slot = sum(cap * self._out_frame_bytes(n) for n, cap in self.caps.items()) + 256 * 4 * len(codes)
+        if output_arena_bytes is None:
+            output_arena_bytes = 2 * max_inflight * out_per_slot
+        max_segments = sum(self.caps.values()) + sym_bytes // _CHUNK + 2 * len(codes) * len(self.orders) + 8
         with torch.cuda.device(self.device):
             self._tables = {o: self._axis_structs(o) for o in self.orders}
-            self.slots = [_Slot(self, self.caps, sym_bytes) for _ in range(max_inflight)]
+            self.slots = [_Slot(self, self.caps, sym_bytes, max_segments) for _ in range(max_inflight)]
         used = sum(sl.bytes for sl in self.slots)
         if used > hbm_budget:
             raise MemoryError(f"{max_inflight} batch slots need {used} bytes, over the {hbm_budget}-byte budget")
         self.hbm_bytes = used
+        self.arena = OutputArena(output_arena_bytes)
         self.admission = Admission(slots=max_inflight)
         self._free = list(self.slots)
         self._busy: list[_Slot] = []
         self.completed: list[Request] = []
+        self._t0 = 0.0
+
+    def _out_frame_bytes(self, name: str) -> int:
+        code = self.codes[name]
+        return 4 * code.n + code.k + 4 + 1
 
     def _axis_structs(self, order: int):
         from . import _device
@@ -185,16 +241,19 @@ class Server:
         half = len(tabs) // 2
         return (_axis_struct(tabs[:half], "maxlog"), _axis_struct(tabs[half:], "maxlog"), tabs)
 
-    def _batch_array(self, counts: dict):
+    def _batch_array(self, counts: dict, slot: _Slot, out: dict):
+        """The mixed decode's per-code arguments; outputs at the host
+        addresses ``out[name] = (llr, bits, iters, valid)``, or in a scratch
+        layout when ``out`` is empty (workspace sizing only)."""
         arr = (_lib.Batch * len(counts))()
         m = self.method
-        for i, (name, (B, slot)) in enumerate(counts.items()):
+        for i, (name, B) in enumerate(counts.items()):
             code = self.codes[name]
-            o = slot.out_dev[name]
-            arr[i] = _lib.Batch(code._plan(self.device.index).handle, slot.llr[name].data_ptr(), o[0].data_ptr(), B,
-                                code.n, _lib.CK_LDPC_MIN_SUM, np.float32(m.scale), np.float32(m.offset),
-                                int(m.max_iterations), 1 if m.early_stop else 0, o[2].data_ptr(),
-                                o[3].data_ptr(), o[1].data_ptr(), code.k)  # fmt: skip
+            llr_o, bits_o, it_o, ok_o = out.get(name, (1, 1, 1, 1))
+            arr[i] = _lib.Batch(code._plan(self.device.index).handle, slot.llr[name].data_ptr(), llr_o, B, code.n,
+                                _lib.CK_LDPC_MIN_SUM, np.float32(m.scale), np.float32(m.offset),
+                                int(m.max_iterations), 1 if m.early_stop else 0, it_o, ok_o, bits_o,
+                                code.k)  # fmt: skip
         return arr
 
     def _fits(self, batch: list[Request], r: Request) -> bool:
@@ -202,17 +261,27 @@ class Server:
         syms = sum(q.frames * q.symbols.shape[1] for q in batch) + r.frames * r.symbols.shape[1]
         return frames <= self.caps[r.code] and syms <= self._sym_cap
 
-    def _launch(self, batch: list[Request], t0: float) -> None:
+    def _wait_region(self, lo: int, hi: int) -> None:
+        """Blocks until no batch in flight writes into arena bytes [lo, hi)."""
+        while True:
+            hit = [sl for sl in self._busy if sl.region and sl.region[0] < hi and lo < sl.region[1]]
+            if not hit:
+                return
+            self._poll(block_on=hit[0])
+
+    def _launch(self, batch: list[Request]) -> None:
         torch = self.torch
         slot = self._free.pop()
-        now = time.perf_counter() - t0
+        now = time.perf_counter() - self._t0
         slot.batch, slot.layout = batch, []
         groups: dict[tuple[str, int], list[Request]] = {}
         for r in batch:
             r.admitted = now
             groups.setdefault((r.code, r.order), []).append(r)
-        s2_np = slot.s2_host.numpy()
-        sym_off, s2_off, counts, demaps, copies = 0, 0, {}, [], []
+        segs = slot.segs_np
+        sym_base, s2_base = slot.sym_dev.data_ptr(), slot.s2_dev.data_ptr()
+        nseg, sym_off, s2_off = 0, 0, 0
+        counts, demaps = {}, []
         for name in self.codes:
             frame_off = 0
             for order in self.orders:
@@ -220,91 +289,140 @@ class Server:
                 if not group:
                     continue
                 S = group[0].symbols.shape[1]
-                g_frames = sum(r.frames for r in group)
-                g_sym = sym_off
+                g_sym, g_s2, g_frame = sym_off, s2_off, frame_off
                 for r in group:
-                    # Each request's (pinned) symbols go straight to the device.
-                    copies.append((sym_off, r.frames * S, r.symbols))
-                    s2_np[s2_off : s2_off + r.frames] = inv_s2_frames([r.noise_var])[0]
+                    src, nbytes = r.symbols.data_ptr(), r.frames * S * 8
+                    dst = sym_base + 8 * sym_off
+                    for c0 in range(0, nbytes, _CHUNK):
+                        segs[nseg] = (src + c0, dst + c0, min(_CHUNK, nbytes - c0))
+                        nseg += 1
+                    slot.s2_np[s2_off : s2_off + r.frames] = np.float32(1.0 / max(r.noise_var, 1e-20))
                     slot.layout.append((r, name, frame_off))
                     sym_off += r.frames * S
                     s2_off += r.frames
                     frame_off += r.frames
-                demaps.append((order, g_sym, S, g_frames, s2_off - g_frames, name, frame_off - g_frames))
+                demaps.append((order, g_sym, S, frame_off - g_frame, g_s2, name, g_frame))
             if frame_off:
                 counts[name] = frame_off
-        slot.counts = counts
+        segs[nseg] = (slot.s2_host.data_ptr(), s2_base, 4 * s2_off)
+        nseg += 1
+        # Results go straight into the arena: per code (llrs, bits, iterations, valid).
+        sizes = {n: B * self._out_frame_bytes(n) + 4 * 256 for n, B in counts.items()}
+        off = self.arena.alloc(sum(sizes.values()), self._wait_region)
+        slot.region = (off, off + sum(sizes.values()))
+        out, slot.out = {}, {}
+        a = self.arena.np
+        for name, B in counts.items():
+            code = self.codes[name]
+            parts, o = [], off
+            for nbytes in (4 * B * code.n, B * code.k, 4 * B, B):
+                parts.append(o)
+                o += (nbytes + 255) // 256 * 256
+            # Iteration counts start at -2: the decoder publishes a frame by
+            # writing its count (>= -1) last.
+            a[parts[2] : parts[2] + 4 * B].view(np.int32)[:] = -2
+            slot.out[name] = (B, parts, self._views(name, B, parts))
+            out[name] = tuple(self.arena.base + p for p in (parts[0], parts[1], parts[2], parts[3]))
+            off = o
+        slot.waiting = [(r, name, off_r) for r, name, off_r in slot.layout]
         lib = _lib.lib()
-        with torch.cuda.stream(slot.stream):
-            for off, n, src in copies:
-                if not isinstance(src, torch.Tensor):
-                    src = torch.from_numpy(np.ascontiguousarray(src))
-                slot.sym_dev[off : off + n].copy_(src.reshape(-1), non_blocking=True)
-            slot.s2_dev[:s2_off].copy_(slot.s2_host[:s2_off], non_blocking=True)
-            st = slot.stream.cuda_stream
-            for order, g_sym, S, g_frames, g_s2, name, f_off in demaps:
-                re, im, _ = self._tables[order]
-                x_ptr = slot.sym_dev.data_ptr() + 8 * g_sym
-                out_ptr = slot.llr[name].data_ptr() + 4 * f_off * self.codes[name].n
-                _lib.check(lib.ck_llr_separable_maxlog_frames(
-                    x_ptr, g_frames * S, S, slot.s2_dev.data_ptr() + 4 * g_s2, ctypes.byref(re), ctypes.byref(im),
-                    out_ptr, st), "server demap")  # fmt: skip
-            arr = self._batch_array({name: (B, slot) for name, B in counts.items()})
-            _lib.check(lib.ck_ldpc_decode_mixed(arr, len(counts), slot.ws.data_ptr(), slot.ws.numel(), st),
-                       "server decode")  # fmt: skip
-            # Results land in pinned buffers of this batch, which the requests
-            # then view (no host-side copies).
-            slot.out_host = {}
-            for name, B in counts.items():
-                hs = []
-                for d in slot.out_dev[name]:
-                    h = torch.empty((B, *d.shape[1:]), dtype=d.dtype, pin_memory=True)
-                    h.copy_(d[:B], non_blocking=True)
-                    hs.append(h)
-                slot.out_host[name] = hs
-            slot.event.record(slot.stream)
+        st = slot.stream.cuda_stream
+        _lib.check(lib.ck_gather(slot.segs.data_ptr(), nseg, st), "server gather")
+        for order, g_sym, S, g_frames, g_s2, name, f_off in demaps:
+            re, im, _ = self._tables[order]
+            _lib.check(lib.ck_llr_separable_maxlog_frames(
+                sym_base + 8 * g_sym, g_frames * S, S, s2_base + 4 * g_s2, ctypes.byref(re), ctypes.byref(im),
+                slot.llr[name].data_ptr() + 4 * f_off * self.codes[name].n, st), "server demap")  # fmt: skip
+        arr = self._batch_array(counts, slot, out)
+        _lib.check(lib.ck_ldpc_decode_mixed(arr, len(counts), slot.ws.data_ptr(), slot.ws.numel(), st),
+                   "server decode")  # fmt: skip
+        slot.event.record(slot.stream)
         self._busy.append(slot)
 
-    def _poll(self, t0: float, block: bool = False) -> None:
+    def _views(self, name: str, B: int, parts: list) -> tuple:
+        a, code = self.arena.np, self.codes[name]
+        return (a[parts[0] : parts[0] + 4 * B * code.n].view(np.float32).reshape(B, code.n),
+                a[parts[1] : parts[1] + B * code.k].view(np.int8).reshape(B, code.k),
+                a[parts[2] : parts[2] + 4 * B].view(np.int32), a[parts[3] : parts[3] + B])  # fmt: skip
+
+    def _deliver(self, slot: _Slot, r: Request, name: str, off: int, now: float) -> None:
+        llrs, bits, iters, valid = slot.out[name][2]
+        sl = slice(off, off + r.frames)
+        r.bits, r.llrs, r.iterations = bits[sl], llrs[sl], iters[sl]
+        r.valid = valid[sl].view(np.bool_)
+        r.done = now
+        self.completed.append(r)
+
+    def _poll(self, block: bool = False, block_on: _Slot | None = None) -> None:
+        """Delivers every request whose frames the decoder has published,
+        and frees the slots whose batch is complete."""
+        lib = _lib.lib()
         still = []
         for slot in self._busy:
-            if not slot.event.query():
-                if not block:
-                    still.append(slot)
-                    continue
+            finished = slot.event.query()
+            if not finished and (block or slot is block_on):
                 slot.event.synchronize()
-            now = time.perf_counter() - t0
-            for r, name, off in slot.layout:
-                llrs, bits, iters, valid = (t.numpy() for t in slot.out_host[name])
-                sl = slice(off, off + r.frames)
-                r.bits, r.llrs, r.iterations = bits[sl], llrs[sl], iters[sl]
-                r.valid = valid[sl].view(np.bool_)
-                r.done = now
-                self.completed.append(r)
-            slot.batch, slot.layout = [], []
-            self._free.append(slot)
-            self.admission.release()
+                finished = True
+            now = time.perf_counter() - self._t0
+            if finished:
+                for r, name, off in slot.waiting:
+                    self._deliver(slot, r, name, off, now)
+                slot.waiting = []
+                slot.batch, slot.layout, slot.region = [], [], None
+                self._free.append(slot)
+                self.admission.release()
+                continue
+            # Requests whose frames have all been published, before the batch ends.
+            left = []
+            for item in slot.waiting:
+                r, name, off = item
+                if int(slot.out[name][2][2][off : off + r.frames].min()) >= -1:
+                    lib.ck_host_acquire()
+                    self._deliver(slot, r, name, off, now)
+                else:
+                    left.append(item)
+            slot.waiting = left
+            still.append(slot)
         self._busy = still
 
     def serve(self, requests: list[Request]) -> list[Request]:
         """Run a request stream (arrival times in seconds from now) to completion."""
         pending = deque(sorted(requests, key=lambda r: r.arrival))
+        for r in pending:
+            if not r.symbols.is_contiguous():
+                r.symbols = r.symbols.contiguous()
+            if not r.symbols.is_cuda and not r.symbols.is_pinned():
+                # The gather reads payloads in place: they must be pinned (or on the device).
+                r.symbols = r.symbols.pin_memory()
         self.completed = []
-        t0 = time.perf_counter()
-        while pending or self.admission.pending or self._busy:
-            now = time.perf_counter() - t0
-            while pending and pending[0].arrival <= now:
-                self.admission.arrive(pending.popleft())
-            if self._busy:
-                self._poll(t0)
-            batch = self.admission.next_batch(self._fits)
-            if batch:
-                self._launch(batch, t0)
-            elif pending and not self.admission.pending and not self._busy:
-                wait = pending[0].arrival - (time.perf_counter() - t0)
-                if wait > 2e-4:
-                    time.sleep(wait - 1e-4)
-        self._poll(t0, block=True)
+        # The cyclic garbage collector would pause the loop for tens of
+        # milliseconds once many results are alive; requests create no cycles.
+        gc_on = gc.isenabled()
+        gc.disable()
+        try:
+            return self._serve(pending)
+        finally:
+            if gc_on:
+                gc.enable()
+
+    def _serve(self, pending: deque) -> list[Request]:
+        torch = self.torch
+        self._t0 = time.perf_counter()
+        with torch.cuda.device(self.device):
+            while pending or self.admission.pending or self._busy:
+                now = time.perf_counter() - self._t0
+                while pending and pending[0].arrival <= now:
+                    self.admission.arrive(pending.popleft())
+                if self._busy:
+                    self._poll()
+                batch = self.admission.next_batch(self._fits)
+                if batch:
+                    self._launch(batch)
+                elif pending and not self.admission.pending and not self._busy:
+                    wait = pending[0].arrival - (time.perf_counter() - self._t0)
+                    if wait > 2e-4:
+                        time.sleep(wait - 1e-4)
+            self._poll(block=True)
         return self.completed
 
 

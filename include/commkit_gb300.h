@@ -204,6 +204,31 @@ int ck_count_errors(const int8_t* info, const int8_t* decoded, const float* llr,
 int ck_gmi_loss(const float* llr, const int8_t* bits, int64_t rows, int64_t len, double* partial,
                 void* stream);
 
+/*
+ * One copy of a batch assembly: `bytes` from `src` to `dst`.  Both may be
+ * device memory or pinned host memory (the same address on host and device
+ * under unified addressing).
+ */
+typedef struct ck_segment {
+    const void* src;
+    void* dst;
+    int64_t bytes;
+} ck_segment;
+
+/*
+ * Copies n segments in one launch (no reference counterpart: the request
+ * server's batch assembly).  `segments` itself may sit in pinned host
+ * memory.  Segments must not overlap one another's destinations.
+ */
+int ck_gather(const ck_segment* segments, int32_t n, void* stream);
+
+/*
+ * Host acquire fence: call after reading a value the device published in
+ * mapped host memory (the mixed decoder writes each frame's iteration count
+ * last, after a system-scope fence) and before reading the data it guards.
+ */
+void ck_host_acquire(void);
+
 /* ---------------------------------------------------------------------- */
 /* Layered LDPC decoding                                                   */
 /* ---------------------------------------------------------------------- */

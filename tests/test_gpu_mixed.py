@@ -66,9 +66,11 @@ def test_mixed_single_code_and_empty_batch():
     np.testing.assert_array_equal(m1.bits.cpu().numpy(), p.bits.cpu().numpy())
 
 
-def test_receiver_graph_replay_matches_plain_calls():
-    """The device-resident mixed receiver, captured once as a CUDA graph and
-    replayed on a new batch, gives the plain calls' results."""
+@pytest.mark.parametrize("host_io", [False, True])
+def test_receiver_graph_replay_matches_plain_calls(host_io):
+    """The mixed receiver, captured once as a CUDA graph and replayed on a
+    new batch, gives the plain calls' results; with ``host_io`` its kernels
+    read the symbols from and write the results to pinned host memory."""
     import torch
 
     import commkit_gb300 as ck
@@ -80,12 +82,15 @@ def test_receiver_graph_replay_matches_plain_calls():
     names = list(work)
     codes = {n: ck.LDPCCode.quasi_cyclic(W.CODES[n].base(), lifting=W.CODES[n].z) for n in names}
     consts = {n: ck.Constellation.qam(W.MIXED_ORDERS[n]) for n in names}
-    rx = MixedReceiver([CodeSlot(codes[n], consts[n], work[n].symbols.shape[0], method) for n in names], dev)
+    rx = MixedReceiver([CodeSlot(codes[n], consts[n], work[n].symbols.shape[0], method) for n in names], dev,
+                       host_io=host_io)  # fmt: skip
+    assert rx.sym[0].is_cuda != host_io and rx.outputs[0][0].is_cuda != host_io
     rx.load([work[n].symbols for n in names], [work[n].noise_var for n in names])
     rx.capture()
     work2 = W.mixed_workload(total=600, seed=6)  # same shapes, new frames
     rx.load([work2[n].symbols for n in names], [work2[n].noise_var for n in names])
     rx.run()
+    torch.cuda.synchronize()
     for r, n in zip(rx.results(), names, strict=True):
         llr = ck.compute_llr_frames(torch.from_numpy(work2[n].symbols).to(dev), noise_var=work2[n].noise_var,
                                     constellation=consts[n])  # fmt: skip
