@@ -203,8 +203,8 @@ struct MinSumState {
           g2(g1 + p.r_stride),
           g3(g2 + p.r_stride) {}
 
-    __device__ __forceinline__ void zero(const Params& p, int tid) const {
-        for (int i = tid; i < p.m; i += p.T) {
+    __device__ __forceinline__ void zero(const Params& p, int first, int stride) const {
+        for (int i = first; i < p.m; i += stride) {
             if (R_SMEM) {
                 rs[i] = make_uint4(0u, 0u, 0u, 0u);
             } else {
@@ -263,6 +263,12 @@ struct MinSumPick {
 
 KernelFn min_sum_kernel(bool qc, int dmax, bool app_smem, bool r_smem) {
     return pick_shape<MinSumPick>(qc, dmax, app_smem, r_smem);
+}
+
+KernelFn min_sum_cluster_kernel(int dmax) {
+    if (dmax <= 8) return decode_cluster_kernel<MinSumState, 8>;
+    if (dmax <= 16) return decode_cluster_kernel<MinSumState, 16>;
+    return decode_cluster_kernel<MinSumState, 27>;
 }
 
 }  // namespace ldpc
@@ -496,7 +502,15 @@ struct Resolved {
     int grid;
     size_t r_slot_bytes;  // message state of one frame slot in device memory (0 in shared)
     size_t ws_bytes, r_ws_off, app_ws_off;
+    // CSR codes with the posterior in device memory: the cluster kernel, and
+    // the cluster size a decode uses (1: the plain kernel).
+    KernelFn cluster_kernel;
+    int cluster_per_sm;
+    int cluster;
+    int plain_grid;  // the plain kernel's grid for the same frames
 };
+
+constexpr int kMaxCluster = 8;  // the portable cluster size
 
 constexpr size_t kHeaderBytes = 256;
 
@@ -533,9 +547,44 @@ int resolve(const ck_ldpc_plan* plan, int32_t rule, int64_t B, Resolved* r) {
         }
     }
     const int32_t G = r->G;
+    r->cluster = 1;
+    size_t slots;
+    if (r->cluster_kernel && B * 2 <= int64_t(sms) * r->cluster_per_sm) {
+        // Fewer frames than the GPU holds: a cluster of C CTAs per frame, the
+        // largest C whose clusters can all be resident at once.
+        for (int c = kMaxCluster; c >= 2; c /= 2) {
+            if (B * c > int64_t(sms) * r->cluster_per_sm) continue;
+            cudaLaunchConfig_t cfg = {};
+            cudaLaunchAttribute attr;
+            attr.id = cudaLaunchAttributeClusterDimension;
+            attr.val.clusterDim.x = c;
+            attr.val.clusterDim.y = 1;
+            attr.val.clusterDim.z = 1;
+            cfg.gridDim = dim3(static_cast<unsigned>(B * c));
+            cfg.blockDim = dim3(static_cast<unsigned>(r->T));
+            cfg.attrs = &attr;
+            cfg.numAttrs = 1;
+            int clusters = 0;
+            if (cudaOccupancyMaxActiveClusters(&clusters, reinterpret_cast<const void*>(r->cluster_kernel), &cfg) !=
+                cudaSuccess) {
+                (void)cudaGetLastError();
+                continue;
+            }
+            if (clusters >= B) {
+                r->cluster = c;
+                break;
+            }
+        }
+    }
     const int64_t need = (B + G - 1) / G;
-    r->grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(need, int64_t(sms) * per_sm)));
-    const size_t slots = static_cast<size_t>(r->grid) * G;
+    r->plain_grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(need, int64_t(sms) * per_sm)));
+    if (r->cluster > 1) {
+        r->grid = static_cast<int>(B * r->cluster);
+        slots = static_cast<size_t>(B);  // one frame slot per cluster
+    } else {
+        r->grid = r->plain_grid;
+        slots = static_cast<size_t>(r->grid) * G;
+    }
     r->r_ws_off = kHeaderBytes;
     const size_t r_ws = slots * r->r_slot_bytes;
     r->app_ws_off = kHeaderBytes + ((r_ws + 255) / 256) * 256;
@@ -667,9 +716,43 @@ int resolve_shape(const ck_ldpc_plan* plan, int32_t rule, Resolved* r, int* per_
                         "an SM",
                         T * G, r->smem);
     r->r_slot_bytes = r_smem ? 0 : r_bytes_dev;
+    r->cluster_kernel = nullptr;
+    r->cluster_per_sm = 0;
+    r->cluster = 1;
+    if (!plan->qc && !app_smem && !r_smem) {
+        KernelFn ck = sp ? sum_product_cluster_kernel(plan->max_deg) : min_sum_cluster_kernel(plan->max_deg);
+        int cps = 0;
+        CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cps, reinterpret_cast<const void*>(ck), T, 0));
+        if (cps >= 1) {
+            r->cluster_kernel = ck;
+            r->cluster_per_sm = cps;
+        }
+    }
     *per_sm_out = per_sm;
     *sms_out = sms;
     return CK_OK;
+}
+
+// Launches a resolved decode: the plain kernel, or the cluster kernel with
+// its cluster size.
+int launch_decode(const Resolved& r, const Params& p, cudaStream_t s) {
+    if (r.cluster <= 1) {
+        r.kernel<<<r.grid, r.T * r.G, r.smem, s>>>(p);
+        return ck::cuda_check(cudaGetLastError(), "decoder launch");
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = static_cast<unsigned>(r.cluster);
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.gridDim = dim3(static_cast<unsigned>(r.grid));
+    cfg.blockDim = dim3(static_cast<unsigned>(r.T));
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    return ck::cuda_check(cudaLaunchKernelEx(&cfg, r.cluster_kernel, p), "cluster decoder launch");
 }
 
 int check_device(const ck_ldpc_plan* plan) {
@@ -803,10 +886,7 @@ extern "C" int ck_ldpc_decode(const ck_ldpc_plan* plan, const float* llr_in, flo
     int status = ck::cuda_check(cudaMemsetAsync(wsb, 0, kHeaderBytes, s), "cudaMemsetAsync");
     const Params p = make_params(plan, r, llr_in, llr_out, B, n_in, scale, offset, max_iterations,
                                  early_stop, iters, valid, bits, k_bits, wsb);
-    if (status == CK_OK) {
-        r.kernel<<<r.grid, r.T * r.G, r.smem, s>>>(p);
-        status = ck::cuda_check(cudaGetLastError(), "decoder launch");
-    }
+    if (status == CK_OK) status = launch_decode(r, p, s);
     if (owned) {
         const int st = ck::cuda_check(cudaFreeAsync(ws, s), "cudaFreeAsync");
         if (status == CK_OK) status = st;
@@ -846,6 +926,9 @@ int ck::ldpc_decode_in_scratch(const ck_ldpc_plan* plan, const float* llr_in, fl
     CK_TRY(check_device(plan));
     Resolved r;
     CK_TRY(resolve(plan, rule, B, &r));
+    // The static scratch serves the plain kernel's frame slots.
+    r.cluster = 1;
+    r.grid = r.plain_grid;
     // Bytes of device-memory state per frame slot (the header is shared).
     const size_t app_bytes = r.app_smem ? 0 : static_cast<size_t>(r.app_stride) * 4;
     const size_t per_slot = r.r_slot_bytes + app_bytes;
@@ -872,8 +955,7 @@ int ck::ldpc_decode_in_scratch(const ck_ldpc_plan* plan, const float* llr_in, fl
     CK_CUDA(cudaMemsetAsync(wsb, 0, kHeaderBytes, s));
     const Params p = make_params(plan, r, llr_in, llr_out, B, n_in, scale, offset, max_iterations,
                                  early_stop, iters, valid, bits, k_bits, wsb);
-    r.kernel<<<r.grid, r.T * r.G, r.smem, s>>>(p);
-    return ck::cuda_check(cudaGetLastError(), "decoder launch");
+    return launch_decode(r, p, s);
 }
 
 // ---------------------------------------------------------------------------

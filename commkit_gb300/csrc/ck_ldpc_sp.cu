@@ -39,8 +39,8 @@ struct SumProductState {
         : r(R_SMEM ? reinterpret_cast<float*>(gbase + p.r_off)
                    : reinterpret_cast<float*>(p.g_r) + static_cast<size_t>(slot) * p.r_stride) {}
 
-    __device__ __forceinline__ void zero(const Params& p, int tid) const {
-        for (int i = tid; i < p.E; i += p.T) r[i] = 0.0f;
+    __device__ __forceinline__ void zero(const Params& p, int first, int stride) const {
+        for (int i = first; i < p.E; i += stride) r[i] = 0.0f;
     }
     __device__ __forceinline__ float ld(uint32_t i) const { return R_SMEM ? r[i] : __ldcg(r + i); }
     __device__ __forceinline__ void st(uint32_t i, float v) const {
@@ -132,6 +132,12 @@ struct SumProductPick {
 
 KernelFn sum_product_kernel(bool qc, int dmax, bool app_smem, bool r_smem) {
     return pick_shape<sp::SumProductPick>(qc, dmax, app_smem, r_smem);
+}
+
+KernelFn sum_product_cluster_kernel(int dmax) {
+    if (dmax <= 8) return decode_cluster_kernel<sp::SumProductState, 8>;
+    if (dmax <= 16) return decode_cluster_kernel<sp::SumProductState, 16>;
+    return decode_cluster_kernel<sp::SumProductState, 27>;
 }
 
 }  // namespace ldpc

@@ -277,3 +277,36 @@ def test_dvbs2_normal_frames(torch_dev, ck):
     llr = ck.compute_llr(torch.from_numpy(sym).to(dev), noise_var=nv, constellation=c).reshape(64, n)
     got = _to_np(ck.decode(llr, code=code), 64)
     _assert_same(got, _oracle(code, llr.cpu().numpy(), max_iterations=50))
+
+
+@pytest.mark.parametrize("rule, early_stop", [("min_sum", True), ("min_sum", False), ("sum_product", True)])
+def test_cluster_decode_equals_plain(torch_dev, ck, rule, early_stop):
+    """DVB-S2 normal frames: a small batch runs on thread-block clusters (one
+    frame per cluster of CTAs, the posterior in device memory), a large one
+    on the plain persistent kernel; the same frames decode identically."""
+    from commkit_gb300.workloads import awgn, encode_accumulate, map_bits
+    from tests.conftest import GOLDEN
+
+    torch, dev = torch_dev
+    d = dict(np.load(GOLDEN / "dvbs2_normal.npz"))
+    m, N, n, k = (int(d[f"dvbs2n_{s}"]) for s in ("m", "N", "n", "k"))
+    code = ck.LDPCCode(d["dvbs2n_checks"], d["dvbs2n_variables"], m, N, N - n)
+    rng = np.random.default_rng(17)
+    frames = 400
+    info = rng.integers(0, 2, size=(frames, k), dtype=np.int8)
+    nv = 10.0 ** (-1.2 / 10.0)
+    sym = awgn(map_bits(encode_accumulate(d["dvbs2n_checks"], d["dvbs2n_variables"], m, k, info), 4), nv, rng)
+    llr = ck.compute_llr(torch.from_numpy(sym).to(dev), noise_var=nv, constellation=ck.Constellation.qam(4))
+    llr = llr.reshape(frames, n)
+    method = (ck.MinSum(max_iterations=15, early_stop=early_stop) if rule == "min_sum"
+              else ck.SumProduct(max_iterations=8, early_stop=early_stop))  # fmt: skip
+    big = _to_np(ck.decode(llr, code=code, method=method), frames)
+    for few in (3, 40):
+        small = _to_np(ck.decode(llr[:few].contiguous(), code=code, method=method), few)
+        for a, b, what in zip(small, big, ("bits", "llrs", "valid", "iterations"), strict=True):
+            np.testing.assert_array_equal(a, b[:few], err_msg=f"{what}, {few} frames")
+    if rule == "min_sum":
+        row_ptr, cols, _ = code._schedule
+        want = oracle.decode(llr[:3].cpu().numpy(), (row_ptr, cols, N), k=k, max_iterations=15,
+                             early_stop=early_stop)  # fmt: skip
+        _assert_same(_to_np(ck.decode(llr[:3].contiguous(), code=code, method=method), 3), want)
