@@ -72,7 +72,7 @@ WORKLOADS = {
     "served": dict(max_it=50,
                    desc="served stream: Poisson arrivals of 1-256 frames (log-uniform), codes A/B/C 50/35/15 "
                         "on QPSK/16-QAM/64-QAM, Es/N0 near each waterfall, MinSum 50 it, 4 GiB admission "
-                        "budget over 6 batch slots, load 10-100% of measured saturation"),
+                        "budget over 12 batch slots, load 10-100% of measured saturation"),
 }  # fmt: skip
 
 
@@ -671,7 +671,7 @@ def measure_served(args, dist: Dist) -> dict:
                              seed=7)  # fmt: skip
     t_build = time.perf_counter() - t_build
     codes = {n: ck.LDPCCode.quasi_cyclic(W.CODES[n].base(), lifting=W.CODES[n].z) for n in "ABC"}
-    slots = int(os.environ.get("CK_SERVE_SLOTS", "6"))
+    slots = int(os.environ.get("CK_SERVE_SLOTS", "12"))
     server = Server(codes, ck.MinSum(max_iterations=WORKLOADS["served"]["max_it"]), hbm_budget=4 << 30,
                     max_inflight=slots, device=dev)  # fmt: skip
     k_of = {n: c.k for n, c in codes.items()}

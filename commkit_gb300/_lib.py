@@ -111,6 +111,7 @@ class Batch(ctypes.Structure):
         ("valid", ctypes.c_void_p),
         ("bits", ctypes.c_void_p),
         ("k_bits", ctypes.c_int32),
+        ("order", ctypes.c_void_p),
     ]
 
 

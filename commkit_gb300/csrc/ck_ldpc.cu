@@ -301,6 +301,7 @@ struct MixedCode {
     uint8_t* valid;
     int8_t* bits;
     int32_t k_bits;
+    const int32_t* order;  // queue position -> frame, or null
     float scale, offset;
     int32_t max_iterations, early_stop;
     int32_t T, G, q_bstep, r_smem;
@@ -384,8 +385,9 @@ __device__ void mixed_frames(const MixedCode& K, unsigned char* smem, const int3
     for (;;) {
         if (tid == 0) *s_frame = atomicAdd(K.counter, 1u);
         group_sync(bar, K.T);
-        const uint32_t f = *s_frame;
-        if (f >= K.B) break;
+        const uint32_t pos = *s_frame;
+        if (pos >= K.B) break;
+        const uint32_t f = K.order ? static_cast<uint32_t>(__ldg(K.order + pos)) : pos;
         const float* src = K.llr_in + static_cast<size_t>(f) * K.n_in;
         for (int i = tid; i < K.n_in; i += K.T) a[i] = __fadd_rn(__ldcs(src + i), 0.0f);
         for (int i = K.n_in + tid; i < K.N; i += K.T) a[i] = 0.0f;
@@ -1043,6 +1045,7 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
         K.nnzb = plan->nnzb;
         K.llr_in = b.llr_in;
         K.llr_out = b.llr_out;
+        K.order = b.order;
         K.B = static_cast<uint32_t>(b.B);
         K.n_in = b.n_in;
         K.iters = b.iters;

@@ -8,6 +8,11 @@ Nothing is allocated or copied inside a step, so :meth:`capture` records it
 once as a CUDA graph and :meth:`run` replays it: one graph launch per batch
 of mixed traffic.
 
+The decoder takes each code's frames noisiest first (``lpt``, the
+longest-processing-time-first rule: low-SNR frames run the most
+iterations), so the persistent launch does not end on a tail of 50-iteration
+frames; results are the same in any order.
+
 With ``host_io=True`` the symbol buffers and the outputs are pinned host
 memory instead (GB300's Grace memory is coherent with the GPU over
 NVLink-C2C, with one address on both sides): the demapper reads the
@@ -44,7 +49,7 @@ class CodeSlot:
 class MixedReceiver:
     """Demap + mixed-code decode of fixed-size batches on one CUDA device."""
 
-    def __init__(self, slots: list[CodeSlot], device: Any = None, host_io: bool = False):
+    def __init__(self, slots: list[CodeSlot], device: Any = None, host_io: bool = False, lpt: bool = True):
         import torch
 
         if not slots or len(slots) > 4:
@@ -54,7 +59,8 @@ class MixedReceiver:
         self.slots = slots
         self.host_io = bool(host_io)
         io = {"pin_memory": True} if self.host_io else {"device": self.device}
-        self.sym, self.s2, self.llr, self.outputs = [], [], [], []
+        self.sym, self.s2, self.llr, self.outputs, self.order = [], [], [], [], []
+        self.lpt = bool(lpt)
         for s in slots:
             k = s.constellation.bits_per_symbol
             if s.code.n % k:
@@ -62,6 +68,7 @@ class MixedReceiver:
             S = s.code.n // k
             self.sym.append(torch.zeros((s.frames, S), dtype=torch.complex64, **io))
             self.s2.append(torch.ones((s.frames,), dtype=torch.float32, device=self.device))
+            self.order.append(torch.arange(s.frames, dtype=torch.int32, device=self.device))
             self.llr.append(torch.empty((s.frames, s.code.n), dtype=torch.float32, device=self.device))
             self.outputs.append((
                 torch.empty((s.frames, s.code.n), dtype=torch.float32, **io),
@@ -80,7 +87,8 @@ class MixedReceiver:
             arr[i] = _lib.Batch(plan.handle, self.llr[i].data_ptr(), out[0].data_ptr(), s.frames, s.code.n,
                                 _lib.CK_LDPC_MIN_SUM, np.float32(s.method.scale), np.float32(s.method.offset),
                                 int(s.method.max_iterations), 1 if s.method.early_stop else 0,
-                                out[2].data_ptr(), out[3].data_ptr(), out[1].data_ptr(), s.code.k)  # fmt: skip
+                                out[2].data_ptr(), out[3].data_ptr(), out[1].data_ptr(), s.code.k,
+                                self.order[i].data_ptr())  # fmt: skip
         return arr
 
     def _workspace_bytes(self) -> int:
@@ -100,7 +108,14 @@ class MixedReceiver:
         for i, (x, nv) in enumerate(zip(symbols, noise_var, strict=True)):
             t = x if isinstance(x, self.torch.Tensor) else self.torch.from_numpy(np.ascontiguousarray(x))
             self.sym[i].copy_(t, non_blocking=True)
-            self.s2[i].copy_(self.torch.from_numpy(inv_s2_frames(nv)), non_blocking=False)
+            s2 = inv_s2_frames(nv)
+            self.s2[i].copy_(self.torch.from_numpy(s2), non_blocking=False)
+            if self.lpt:
+                # Longest expected first: the noisiest frames (the smallest
+                # 1/sigma^2) tend to run the most iterations, so the decoder
+                # takes them first and the launch ends on short frames.
+                order = np.argsort(s2, kind="stable").astype(np.int32)
+                self.order[i].copy_(self.torch.from_numpy(order), non_blocking=False)
 
     def step(self) -> None:
         """Demap every slot and decode them all in one mixed launch (no allocation)."""

@@ -357,6 +357,10 @@ typedef struct ck_ldpc_batch {
     uint8_t* valid;       /* (B,) */
     int8_t* bits;         /* (B, k_bits) or NULL */
     int32_t k_bits;
+    /* (B,) device int32, a permutation of 0..B-1: the order in which the
+     * frames are taken from the queue (heaviest expected first shortens the
+     * launch's tail); NULL for 0..B-1.  Results stay at their frame's place. */
+    const int32_t* order;
 } ck_ldpc_batch;
 
 #define CK_LDPC_MAX_MIXED 4
