@@ -549,6 +549,42 @@ def measure_single(args, dist: Dist, wname: str) -> dict:
     }  # fmt: skip
 
 
+def llr_fp64(x: np.ndarray, constellation, inv_s2: np.ndarray, exact: bool) -> np.ndarray:
+    """The demapping formula evaluated in float64 from the kernel's float32
+    inputs (symbols, points, log prior, inv_s2): metric = -|y - x|^2 inv_s2 +
+    log P(x); LLR_j = log sum over points with bit j = 0 of e^metric minus
+    the same over bit j = 1 (max-log: the maxima), bits MSB first
+    (``commkit/mapping/_numba_llr.py:35-124``).  A checker for the error
+    statement beside each demapper result, not a path that produces LLRs."""
+    from commkit_gb300.mapping import host_tables
+
+    pts, logp, lab = host_tables(constellation, "points")
+    k = constellation.bits_per_symbol
+    d = x.astype(np.complex128)[:, None] - pts.astype(np.complex128)[None, :]
+    metric = -(d.real**2 + d.imag**2) * inv_s2.astype(np.float64)[:, None] + logp.astype(np.float64)[None, :]
+    out = np.empty((x.size, k), np.float64)
+    for j in range(k):
+        zero = ((lab >> (k - 1 - j)) & 1) == 0
+        half = []
+        for sel in (zero, ~zero):
+            mm = metric[:, sel]
+            peak = mm.max(axis=1)
+            half.append(peak + np.log(np.exp(mm - peak[:, None]).sum(axis=1)) if exact else peak)
+        out[:, j] = half[0] - half[1]
+    return out
+
+
+def llr_error_vs_fp64(llr: np.ndarray, ref: np.ndarray) -> dict:
+    """Largest absolute error, and largest relative error over entries with
+    |LLR| >= 0.01 (below that, cancellation makes a ratio meaningless)."""
+    err = np.abs(llr.astype(np.float64) - ref)
+    big = np.abs(ref) >= 1e-2
+    return {"max_abs": float(err.max()), "max_rel": float((err[big] / np.abs(ref[big])).max()) if big.any() else 0.0}
+
+
+FP64_SAMPLE = 1 << 16
+
+
 def measure_demapper(dist: Dist) -> dict:
     """Config 2: 2^22 symbols in 1024 frames of 4096, per-frame Es/N0 in
     [8, 20] dB, 16- and 64-QAM, max-log and exact, one batched launch."""
@@ -573,9 +609,15 @@ def measure_demapper(dist: Dist) -> dict:
                 fn()
             ms = timed(dist, fn, 10) / 10
             nbytes = rx.size * (8 + 4 * c.bits_per_symbol) + 1024 * 4
+            k = c.bits_per_symbol
+            got = res.reshape(-1, k)[:FP64_SAMPLE].cpu().numpy()
+            ref = llr_fp64(rx.reshape(-1)[:FP64_SAMPLE], c, np.repeat(inv_s2_frames(nv), 4096)[:FP64_SAMPLE],
+                           method == "exact")  # fmt: skip
             out[f"qam{order}_{method}"] = {"us": ms * 1e3, "gbs": nbytes / (ms * 1e-3) / 1e9,
-                                           "frac": nbytes / (ms * 1e-3) / 1e9 / pk["hbm_gbs"]}  # fmt: skip
-    return {"workload": "2^22 symbols, 1024 frames x 4096, per-frame Es/N0 U[8,20] dB, one launch", "results": out}
+                                           "frac": nbytes / (ms * 1e-3) / 1e9 / pk["hbm_gbs"],
+                                           "err_vs_fp64": llr_error_vs_fp64(got, ref)}  # fmt: skip
+    return {"workload": "2^22 symbols, 1024 frames x 4096, per-frame Es/N0 U[8,20] dB, one launch",
+            "fp64_sample_symbols": FP64_SAMPLE, "results": out}
 
 
 def measure_mpoint(dist: Dist) -> dict:
@@ -585,6 +627,7 @@ def measure_mpoint(dist: Dist) -> dict:
     2^18 symbols), and 8-QAM; max-log and exact; the L2 is flushed before
     every launch (its inputs are smaller than L2)."""
     import commkit_gb300 as ck
+    from commkit_gb300.mapping import inv_s2
 
     torch, dev = dist.torch, dist.dev
     pk = peaks()
@@ -606,10 +649,16 @@ def measure_mpoint(dist: Dist) -> dict:
                     xd, noise_var=0.05, constellation=c, method=method), 1))  # fmt: skip
             ms = float(np.median(times))
             nbytes = n * (8 + 4 * c.bits_per_symbol)
+            got = ck.compute_llr(xd[:FP64_SAMPLE], noise_var=0.05, constellation=c, method=method)
+            got = got.cpu().numpy().reshape(FP64_SAMPLE, -1)
+            ref = llr_fp64(x[:FP64_SAMPLE].astype(np.complex64), c,
+                           np.full(FP64_SAMPLE, inv_s2(0.05), np.float32), method == "exact")  # fmt: skip
             out[f"{name}_{method}"] = {"us": ms * 1e3, "gsym_per_s": n / (ms * 1e-3) / 1e9,
                                        "gbs": nbytes / (ms * 1e-3) / 1e9,
-                                       "frac": nbytes / (ms * 1e-3) / 1e9 / pk["hbm_gbs"]}  # fmt: skip
-    return {"workload": "M-point demapping, 2^22 symbols per call (public compute_llr, L2 flushed)", "results": out}
+                                       "frac": nbytes / (ms * 1e-3) / 1e9 / pk["hbm_gbs"],
+                                       "err_vs_fp64": llr_error_vs_fp64(got, ref)}  # fmt: skip
+    return {"workload": "M-point demapping, 2^22 symbols per call (public compute_llr, L2 flushed)",
+            "fp64_sample_symbols": FP64_SAMPLE, "results": out}
 
 
 def measure_dvbs2(dist: Dist, steps: int = 10, warmup: int = 3) -> dict:

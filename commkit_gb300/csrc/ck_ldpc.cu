@@ -81,7 +81,7 @@ __device__ __forceinline__ void min_sum_row(float* __restrict__ a, const int deg
             negs |= (qe < 0.0f ? 1u : 0u) << e;
             const float mag = fabsf(qe);
             if (mag < min1) idx = static_cast<uint32_t>(e);
-            min2 = fminf(min2, fmaxf(min1, mag));
+            min2 = fminf(min2, fmax_nan(min1, mag));
             min1 = fminf(min1, mag);
         }
     }
@@ -103,7 +103,12 @@ __device__ __forceinline__ void min_sum_row(float* __restrict__ a, const int deg
 
 // The same update for a circulant row of exactly D edges, shaped for the
 // ALU pipe, which bounds this kernel: fully unrolled, columns computed once
-// and kept in registers, and
+// and kept in registers,
+//  * min1/min2 taken over pairs of edges: with lo/hi the pair's smaller and
+//    larger magnitude, min2 = min(min2, hi, max(min1, lo)) and min1 =
+//    min(min1, lo), five operations per pair instead of six (three-input
+//    min), and half as long a dependency chain; a NaN magnitude (only from
+//    infinite input LLRs) drops out of both, as in the reference,
 //  * the sign bits of Q taken from the float sign (no -0 ever reaches the
 //    posterior: frames are loaded as x + 0, and from such values Q = APP - R
 //    and APP = Q + R_new cannot produce -0 either, so "sign bit set" is
@@ -139,9 +144,22 @@ __device__ __forceinline__ void qc_row_fixed(const int2* __restrict__ gblk, cons
         const float qe = __fsub_rn(ld_shared_f32(ce), r_old);
         q[e] = qe;
         negs = __funnelshift_l(__float_as_uint(qe), negs, 1);
-        const float mag = fabsf(qe);
-        min2 = fminf(min2, fmaxf(min1, mag));
-        min1 = fminf(min1, mag);
+        if (e & 1) {
+            const float x = fabsf(q[e - 1]), y = fabsf(qe);
+            const float hi = fmax_nan(x, y);
+            if (e == 1) {
+                min1 = fmin3(x, y, CUDART_INF_F);
+                min2 = fminf(hi, CUDART_INF_F);
+            } else {
+                const float lo = fminf(x, y);
+                min2 = fmin3(min2, hi, fmax_nan(min1, lo));
+                min1 = fminf(min1, lo);
+            }
+        } else if (e == D - 1) {
+            const float mag = fabsf(qe);
+            min2 = fminf(min2, fmax_nan(min1, mag));
+            min1 = fminf(min1, mag);
+        }
     }
     const float n1 = fmaxf(__fsub_rn(__fmul_rn(scale, min1), offset), 0.0f);
     const float n2 = fmaxf(__fsub_rn(__fmul_rn(scale, min2), offset), 0.0f);
@@ -187,42 +205,42 @@ __device__ __forceinline__ void qc_row(const int2* __restrict__ gblk, const int 
 
 // Min-sum check-message state of a frame slot: per row (min1', min2', one
 // word of signs and argmin).  In shared memory one 16-byte record per row
-// (one vector access); in device memory three arrays of 4 bytes, so the
-// resident frames' state (code C: 304 frames x 17664 rows x 12 B = 64 MB)
-// stays in L2.
+// (one vector access); in device memory 12 bytes, an array of (min1',
+// min2') pairs and one of words (two accesses), so the resident frames'
+// state (code C: 304 frames x 17664 rows x 12 B = 64 MB) stays in L2.  (A
+// 16-byte record there measured 17 % slower on code C: 86 MB of state
+// leaves too little of L2 to the rest.)
 template <bool R_SMEM>
 struct MinSumState {
     uint4* rs;
-    uint32_t* g1;
-    uint32_t* g2;
+    uint2* g12;
     uint32_t* g3;
 
     __device__ __forceinline__ MinSumState(const Params& p, unsigned char* gbase, uint32_t slot)
         : rs(reinterpret_cast<uint4*>(gbase + p.r_off)),
-          g1(p.g_r + static_cast<size_t>(slot) * 3 * p.r_stride),
-          g2(g1 + p.r_stride),
-          g3(g2 + p.r_stride) {}
+          g12(reinterpret_cast<uint2*>(p.g_r + static_cast<size_t>(slot) * 3 * p.r_stride)),
+          g3(p.g_r + static_cast<size_t>(slot) * 3 * p.r_stride + 2 * p.r_stride) {}
 
     __device__ __forceinline__ void zero(const Params& p, int first, int stride) const {
         for (int i = first; i < p.m; i += stride) {
             if (R_SMEM) {
                 rs[i] = make_uint4(0u, 0u, 0u, 0u);
             } else {
-                g1[i] = 0u;
-                g2[i] = 0u;
+                g12[i] = make_uint2(0u, 0u);
                 g3[i] = 0u;
             }
         }
     }
     __device__ __forceinline__ uint4 load(uint32_t row) const {
-        return R_SMEM ? rs[row] : make_uint4(__ldcg(g1 + row), __ldcg(g2 + row), __ldcg(g3 + row), 0u);
+        if (R_SMEM) return rs[row];
+        const uint2 m = __ldcg(g12 + row);
+        return make_uint4(m.x, m.y, __ldcg(g3 + row), 0u);
     }
     __device__ __forceinline__ void store(uint32_t row, float m1, float m2, uint32_t w) const {
         if (R_SMEM) {
             rs[row] = make_uint4(__float_as_uint(m1), __float_as_uint(m2), w, 0u);
         } else {
-            __stcg(g1 + row, __float_as_uint(m1));
-            __stcg(g2 + row, __float_as_uint(m2));
+            __stcg(g12 + row, make_uint2(__float_as_uint(m1), __float_as_uint(m2)));
             __stcg(g3 + row, w);
         }
     }
@@ -349,11 +367,10 @@ __device__ void mixed_frames(const MixedCode& K, unsigned char* smem, const int3
     unsigned char* gbase = smem + K.tables_bytes + static_cast<uint32_t>(g) * K.group_bytes;
     volatile uint32_t* s_frame = reinterpret_cast<volatile uint32_t*>(gbase + 8);
     float* a = reinterpret_cast<float*>(gbase + K.app_off);
-    uint4* rs = reinterpret_cast<uint4*>(gbase + K.r_off);
     const uint32_t slot = blockIdx.x * static_cast<uint32_t>(K.G) + static_cast<uint32_t>(g);
-    uint32_t* g1 = K.g_r + static_cast<size_t>(slot) * 3 * K.r_stride;
-    uint32_t* g2 = g1 + K.r_stride;
-    uint32_t* g3 = g2 + K.r_stride;
+    uint4* rs = reinterpret_cast<uint4*>(gbase + K.r_off);
+    uint2* g12 = reinterpret_cast<uint2*>(K.g_r + static_cast<size_t>(slot) * 3 * K.r_stride);
+    uint32_t* g3 = K.g_r + static_cast<size_t>(slot) * 3 * K.r_stride + 2 * K.r_stride;
     int2* gblk = reinterpret_cast<int2*>(gbase + K.gblk_off);
     const uint32_t a_addr = ck::smem_addr(a);
     for (int i = tid; i < K.nnzb; i += K.T)
@@ -395,8 +412,7 @@ __device__ void mixed_frames(const MixedCode& K, unsigned char* smem, const int3
             if (R_SMEM) {
                 rs[i] = make_uint4(0u, 0u, 0u, 0u);
             } else {
-                g1[i] = 0u;
-                g2[i] = 0u;
+                g12[i] = make_uint2(0u, 0u);
                 g3[i] = 0u;
             }
         }
@@ -413,9 +429,13 @@ __device__ void mixed_frames(const MixedCode& K, unsigned char* smem, const int3
                         if (r >= K.Z) continue;
                         const uint32_t row = static_cast<uint32_t>(b) * static_cast<uint32_t>(K.Z) +
                                              static_cast<uint32_t>(r);
-                        const uint4 st = R_SMEM ? rs[row]
-                                                : make_uint4(__ldcg(g1 + row), __ldcg(g2 + row),
-                                                             __ldcg(g3 + row), 0u);
+                        uint4 st;
+                        if (R_SMEM) {
+                            st = rs[row];
+                        } else {
+                            const uint2 mm = __ldcg(g12 + row);
+                            st = make_uint4(mm.x, mm.y, __ldcg(g3 + row), 0u);
+                        }
                         float m1 = __uint_as_float(st.x), m2 = __uint_as_float(st.y);
                         uint32_t w = st.z;
                         qc_row<DMAX>(gblk + e0, deg, r4 + 4u * static_cast<uint32_t>(r - qr0), Z4, m1,
@@ -423,8 +443,7 @@ __device__ void mixed_frames(const MixedCode& K, unsigned char* smem, const int3
                         if (R_SMEM) {
                             rs[row] = make_uint4(__float_as_uint(m1), __float_as_uint(m2), w, 0u);
                         } else {
-                            __stcg(g1 + row, __float_as_uint(m1));
-                            __stcg(g2 + row, __float_as_uint(m2));
+                            __stcg(g12 + row, make_uint2(__float_as_uint(m1), __float_as_uint(m2)));
                             __stcg(g3 + row, w);
                         }
                     }
@@ -1030,7 +1049,11 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
                                 : 2 * (ctrl + gblk + app + rsm) <= budget;
         const uint32_t group = ctrl + gblk + app + (r_smem ? rsm : 0);
         gmax = std::min<int32_t>(gmax, static_cast<int32_t>(budget / group));
-        int32_t G = plan->launch.frames_per_block > 0 ? std::min(plan->launch.frames_per_block, gmax) : gmax;
+        // As many groups as the block's threads and shared memory hold: a
+        // plain launch's tuned frames per block (one block of G groups among
+        // several per SM) says nothing about a mixed block, which is alone
+        // on its SM.
+        const int32_t G = gmax;
         if (G < 1) return ck::fail(CK_ERR_UNSUPPORTED, "batch %d: a frame does not fit a block", c);
         MixedCode& K = R->p.code[c];
         K.layer = plan->d_layer;

@@ -66,6 +66,23 @@ __device__ __forceinline__ float flip_sign(float v, uint32_t bit) {
     return __uint_as_float(__float_as_uint(v) ^ (bit << 31));
 }
 
+// Minimum of three floats, a NaN input counting as absent (min.f32 with
+// three inputs, sm_100 and later).
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// Maximum that returns NaN when either input is NaN.  In the min1/min2
+// updates it keeps an edge whose |Q| is NaN out of min2 as well as min1, as
+// the reference's `mag < min1` / `mag < min2` tests do.
+__device__ __forceinline__ float fmax_nan(float a, float b) {
+    float d;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(d) : "f"(a), "f"(b));
+    return d;
+}
+
 // Shared-memory load and store at a 32-bit shared address (volatile: their
 // order against each other and the barriers stays as written).
 __device__ __forceinline__ float ld_shared_f32(uint32_t addr) {

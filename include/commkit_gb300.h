@@ -282,7 +282,9 @@ int ck_ldpc_plan_get_info(const ck_ldpc_plan* plan, ck_ldpc_plan_info* info);
  * check-to-variable messages live; 0 lets the plan choose.  Every shape
  * gives the same results bit for bit; it only changes speed.  The
  * autotuner sets it per code.  Sum-product decodes use only the threads
- * per frame and choose their own frames per block and placement.
+ * per frame and choose their own frames per block and placement; mixed
+ * launches use the threads per frame and the placement, and fill their
+ * block with as many frames as fit.
  */
 typedef struct ck_ldpc_launch {
     int32_t threads_per_frame;

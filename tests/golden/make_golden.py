@@ -35,7 +35,9 @@ Every output here is the reference's own result on seeded inputs:
   reference's ``MinSum()`` decode of two QPSK frames at Es/N0 1.5 dB
   (``--only=dvbs2``);
 * ``gmi_golden.npz``: the reference's ``gmi`` / ``ngmi`` of seeded 16-QAM,
-  8-PSK and shaped 64-QAM LLRs (``--only=gmi``).
+  8-PSK and shaped 64-QAM LLRs (``--only=gmi``);
+* ``ldpc_nonfinite.npz``: min-sum on LLRs with infinities and a NaN,
+  DVB-S2 short 1/2 and PON (``--only=nonfinite``).
 
 Large outputs are stored as SHA-256 digests of their bytes (negative zeros
 folded to +0) plus their first frame; inputs drawn from ``default_rng``
@@ -430,6 +432,38 @@ def sp_case(ref: str, which: str, tag: str, mean: float, seed: int, frames: int,
     return out
 
 
+def nonfinite_case(ref: str, which: str) -> dict:
+    """Min-sum through the reference on LLRs holding infinities and a NaN:
+    3 frames of ``m + 1.5 N(0,1)`` (``default_rng(5)``, the all-zero word; m
+    = 1.8 for DVB-S2, 3.0 for PON)
+    with 1 % of the entries set to +inf (frame 0: it still converges), to
+    +-inf (frame 1) or to +inf plus one NaN (frame 2); 12 iterations at
+    most, with and without early stop.  A NaN Q (from the NaN input, or
+    inf - inf inside the decoder) is skipped by the reference's min1/min2
+    comparisons."""
+    _import_reference(ref)
+    from commkit.coding import LDPCCode, MinSum, decode
+
+    code = LDPCCode.dvbs2("1/2", frame="short") if which == "dvbs2s" else LDPCCode.pon()
+    rng = np.random.default_rng(5)
+    mean = 1.8 if which == "dvbs2s" else 3.0
+    llrs = (mean + 1.5 * rng.standard_normal((3, code.n))).astype(np.float32)
+    hit = rng.random(llrs.shape) < 0.01
+    sign = np.where(rng.random(llrs.shape) < 0.5, -1.0, 1.0)
+    sign[[0, 2]] = 1.0
+    llrs[hit] = (sign * np.inf)[hit].astype(np.float32)
+    llrs[2, code.n - 5] = np.nan  # a parity variable: late in its rows, after min1 is set
+    out = {f"nf_{which}_llrs": llrs}
+    for es in (False, True):
+        method = MinSum(max_iterations=12, early_stop=es)
+        res = decode(llrs.reshape(-1), code=code, method=method)
+        out[f"nf_{which}_es{int(es)}_post"] = np.asarray(res.llrs, np.float32).reshape(3, -1)
+        out[f"nf_{which}_es{int(es)}_bits"] = np.packbits(np.asarray(res.bits, np.uint8).reshape(3, -1), axis=1)
+        out[f"nf_{which}_es{int(es)}_valid"] = np.asarray(res.valid, bool)
+        out[f"nf_{which}_es{int(es)}_iters"] = np.asarray(res.iterations, np.int32)
+    return out
+
+
 # (tag, code, mean, seed, frames, iterations): the reference's own GPU-vs-CPU
 # case (tests/coding/test_ldpc_kernel.py:37-45), the circulant path (PON),
 # and both codes at an SNR where some frames stop early.
@@ -466,6 +500,14 @@ def main(ref: str, only: str | None = None) -> None:
             res = pool.submit(mpoint_golden, ref).result()
         np.savez_compressed(HERE / "llr_mpoint_golden.npz", **res)
         print(f"M-point fixtures written in {time.time() - t0:.0f} s")
+        return
+    if only == "nonfinite":
+        import multiprocessing as mp
+
+        with ProcessPoolExecutor(max_workers=2, mp_context=mp.get_context("spawn")) as pool:
+            parts = [f.result() for f in [pool.submit(nonfinite_case, ref, w) for w in ("dvbs2s", "pon")]]
+        np.savez_compressed(HERE / "ldpc_nonfinite.npz", **parts[0], **parts[1])
+        print(f"non-finite fixtures written in {time.time() - t0:.0f} s")
         return
     if only == "sp":
         import multiprocessing as mp

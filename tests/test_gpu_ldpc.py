@@ -71,6 +71,29 @@ def test_reference_kat(golden_ldpc, torch_dev, ck, which, early_stop):
     assert info["quasi_cyclic"] == (1 if which == "pon" else 0)
 
 
+@pytest.mark.parametrize("which", ["dvbs2s", "pon"])
+@pytest.mark.parametrize("early_stop", [False, True])
+def test_nonfinite_llrs(golden_ldpc, torch_dev, ck, which, early_stop):
+    """LLRs with +-inf and a NaN against the reference's decode
+    (``ldpc_nonfinite.npz``): a NaN |Q| stays out of min1 and min2 on both
+    paths, so every finite result matches bit for bit and NaN sits where
+    the reference has NaN."""
+    from tests.conftest import GOLDEN
+
+    torch, dev = torch_dev
+    g, nf = golden_ldpc, np.load(GOLDEN / "ldpc_nonfinite.npz")
+    m, N, n = (int(g[f"{which}_{s}"]) for s in ("m", "N", "n"))
+    code = ck.LDPCCode(g[f"{which}_checks"], g[f"{which}_variables"], m, N, N - n)
+    res = ck.decode(torch.from_numpy(nf[f"nf_{which}_llrs"]).to(dev), code=code,
+                    method=ck.MinSum(max_iterations=12, early_stop=early_stop))  # fmt: skip
+    bits, post, valid, iters = _to_np(res, 3)
+    p = f"nf_{which}_es{int(early_stop)}"
+    np.testing.assert_array_equal(iters, nf[p + "_iters"])
+    np.testing.assert_array_equal(valid, nf[p + "_valid"])
+    np.testing.assert_array_equal(np.packbits(bits.astype(np.uint8), axis=1), nf[p + "_bits"])
+    np.testing.assert_array_equal(post, nf[p + "_post"])
+
+
 @pytest.mark.parametrize("name", ["A", "B"])
 def test_golden_codes(golden_ldpc, torch_dev, ck, name):
     torch, dev = torch_dev

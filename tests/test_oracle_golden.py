@@ -149,6 +149,26 @@ def test_reference_kat(golden_ldpc, which, early_stop):
     _check_case(g, f"{which}_es{int(early_stop)}", bits, post, valid, iters)
 
 
+@pytest.mark.parametrize("which", ["dvbs2s", "pon"])
+@pytest.mark.parametrize("early_stop", [False, True])
+def test_nonfinite_llrs(golden_ldpc, which, early_stop):
+    """LLRs holding +-inf and a NaN (``ldpc_nonfinite.npz``): the oracle
+    skips NaN magnitudes in min1/min2 as the reference does; posteriors
+    equal the reference's, NaN where it has NaN."""
+    from tests.conftest import GOLDEN
+
+    g, nf = golden_ldpc, np.load(GOLDEN / "ldpc_nonfinite.npz")
+    m, N, k = (int(g[f"{which}_{s}"]) for s in ("m", "N", "k"))
+    row_ptr, cols, _ = oracle.schedule(g[f"{which}_checks"], g[f"{which}_variables"], m, N)
+    bits, post, valid, iters = oracle.decode(nf[f"nf_{which}_llrs"], (row_ptr, cols, N), k=k, max_iterations=12,
+                                             early_stop=early_stop)  # fmt: skip
+    p = f"nf_{which}_es{int(early_stop)}"
+    np.testing.assert_array_equal(iters, nf[p + "_iters"])
+    np.testing.assert_array_equal(valid, nf[p + "_valid"])
+    np.testing.assert_array_equal(np.packbits(bits.astype(np.uint8), axis=1), nf[p + "_bits"])
+    np.testing.assert_array_equal(post, nf[p + "_post"])
+
+
 def test_oracle_threads_do_not_change_results(golden_ldpc):
     g = golden_ldpc
     llrs = kat_llrs(int(g["pon_n"]))
