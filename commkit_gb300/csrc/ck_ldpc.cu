@@ -181,27 +181,39 @@ __device__ __forceinline__ void qc_row_fixed(const int2* __restrict__ gblk, cons
     w = (signs & 0x07ffffffu) | (idx << 27);
 }
 
-// Degree dispatch of a circulant row (warp-uniform): D = 2..DMAX unrolled.
+// Degree dispatch of a circulant row (warp-uniform): D = 2..DMAX unrolled,
+// with no case above DMAX (a switch over 2..16 rather than 2..27 for the
+// DMAX = 16 kernels).
+#define CK_ROW_CASE(D) \
+    case D:            \
+        qc_row_fixed<D>(gblk, r4, Z4, m1, m2, w, scale, offset); \
+        break;
 template <int DMAX>
 __device__ __forceinline__ void qc_row(const int2* __restrict__ gblk, const int deg,
                                        const uint32_t r4, const uint32_t Z4, float& m1, float& m2,
                                        uint32_t& w, const float scale, const float offset) {
-    switch (deg) {
-#define CK_ROW_CASE(D) \
-    case D:            \
-        if (D <= DMAX) qc_row_fixed<(D <= DMAX ? D : 2)>(gblk, r4, Z4, m1, m2, w, scale, offset); \
-        break;
-        CK_ROW_CASE(2) CK_ROW_CASE(3) CK_ROW_CASE(4) CK_ROW_CASE(5) CK_ROW_CASE(6)
-        CK_ROW_CASE(7) CK_ROW_CASE(8) CK_ROW_CASE(9) CK_ROW_CASE(10) CK_ROW_CASE(11)
-        CK_ROW_CASE(12) CK_ROW_CASE(13) CK_ROW_CASE(14) CK_ROW_CASE(15) CK_ROW_CASE(16)
-        CK_ROW_CASE(17) CK_ROW_CASE(18) CK_ROW_CASE(19) CK_ROW_CASE(20) CK_ROW_CASE(21)
-        CK_ROW_CASE(22) CK_ROW_CASE(23) CK_ROW_CASE(24) CK_ROW_CASE(25) CK_ROW_CASE(26)
-        CK_ROW_CASE(27)
-#undef CK_ROW_CASE
-        default:
-            break;
+    if constexpr (DMAX <= 16) {
+        switch (deg) {
+            CK_ROW_CASE(2) CK_ROW_CASE(3) CK_ROW_CASE(4) CK_ROW_CASE(5) CK_ROW_CASE(6)
+            CK_ROW_CASE(7) CK_ROW_CASE(8) CK_ROW_CASE(9) CK_ROW_CASE(10) CK_ROW_CASE(11)
+            CK_ROW_CASE(12) CK_ROW_CASE(13) CK_ROW_CASE(14) CK_ROW_CASE(15) CK_ROW_CASE(16)
+            default:
+                break;
+        }
+    } else {
+        switch (deg) {
+            CK_ROW_CASE(2) CK_ROW_CASE(3) CK_ROW_CASE(4) CK_ROW_CASE(5) CK_ROW_CASE(6)
+            CK_ROW_CASE(7) CK_ROW_CASE(8) CK_ROW_CASE(9) CK_ROW_CASE(10) CK_ROW_CASE(11)
+            CK_ROW_CASE(12) CK_ROW_CASE(13) CK_ROW_CASE(14) CK_ROW_CASE(15) CK_ROW_CASE(16)
+            CK_ROW_CASE(17) CK_ROW_CASE(18) CK_ROW_CASE(19) CK_ROW_CASE(20) CK_ROW_CASE(21)
+            CK_ROW_CASE(22) CK_ROW_CASE(23) CK_ROW_CASE(24) CK_ROW_CASE(25) CK_ROW_CASE(26)
+            CK_ROW_CASE(27)
+            default:
+                break;
+        }
     }
 }
+#undef CK_ROW_CASE
 
 // Min-sum check-message state of a frame slot: per row (min1', min2', one
 // word of signs and argmin).  In shared memory one 16-byte record per row
@@ -270,17 +282,17 @@ namespace ck {
 namespace ldpc {
 
 struct MinSumPick {
-    template <bool QC, int DMAX>
+    template <bool QC, int DMAX, bool ONE_ROW>
     static KernelFn get(bool app_smem, bool r_smem) {
-        if (app_smem && r_smem) return decode_kernel<MinSumState, QC, DMAX, true, true>;
-        if (app_smem) return decode_kernel<MinSumState, QC, DMAX, true, false>;
-        if constexpr (!QC) return decode_kernel<MinSumState, QC, DMAX, false, false>;
+        if (app_smem && r_smem) return decode_kernel<MinSumState, QC, DMAX, true, true, ONE_ROW>;
+        if (app_smem) return decode_kernel<MinSumState, QC, DMAX, true, false, ONE_ROW>;
+        if constexpr (!QC) return decode_kernel<MinSumState, QC, DMAX, false, false, false>;
         return nullptr;
     }
 };
 
-KernelFn min_sum_kernel(bool qc, int dmax, bool app_smem, bool r_smem) {
-    return pick_shape<MinSumPick>(qc, dmax, app_smem, r_smem);
+KernelFn min_sum_kernel(bool qc, int dmax, bool app_smem, bool r_smem, bool one_row) {
+    return pick_shape<MinSumPick>(qc, dmax, app_smem, r_smem, one_row);
 }
 
 KernelFn min_sum_cluster_kernel(int dmax) {
@@ -356,8 +368,9 @@ __device__ int mixed_pick(const MixedParams& p, int prefer) {
     return best;
 }
 
-// Decodes frames of code K with group g until K's queue is empty.
-template <int DMAX, bool R_SMEM>
+// Decodes frames of code K with group g until K's queue is empty (ONE_ROW:
+// K.T >= K.Zp, one row per visited base row, as in decode_kernel).
+template <int DMAX, bool R_SMEM, bool ONE_ROW>
 __device__ void mixed_frames(const MixedCode& K, unsigned char* smem, const int32_t* s_layer,
                              const int32_t* s_eptr, const int2* s_blk, const int g,
                              const int tid) {
@@ -420,31 +433,39 @@ __device__ void mixed_frames(const MixedCode& K, unsigned char* smem, const int3
         int32_t it = 0;
         bool ok = K.early_stop && syndrome_ok();
         while (!ok && it < K.max_iterations) {
+            // One check row: row r of base row b (circulants e0 .. e0 + deg).
+            auto do_row = [&](int32_t b, int32_t e0, int deg, int32_t r) {
+                const uint32_t row = static_cast<uint32_t>(b) * static_cast<uint32_t>(K.Z) +
+                                     static_cast<uint32_t>(r);
+                uint4 st;
+                if (R_SMEM) {
+                    st = rs[row];
+                } else {
+                    const uint2 mm = __ldcg(g12 + row);
+                    st = make_uint4(mm.x, mm.y, __ldcg(g3 + row), 0u);
+                }
+                float m1 = __uint_as_float(st.x), m2 = __uint_as_float(st.y);
+                uint32_t w = st.z;
+                qc_row<DMAX>(gblk + e0, deg, r4 + 4u * static_cast<uint32_t>(r - qr0), Z4, m1, m2, w,
+                             K.scale, K.offset);
+                if (R_SMEM) {
+                    rs[row] = make_uint4(__float_as_uint(m1), __float_as_uint(m2), w, 0u);
+                } else {
+                    __stcg(g12 + row, make_uint2(__float_as_uint(m1), __float_as_uint(m2)));
+                    __stcg(g3 + row, w);
+                }
+            };
             for (int32_t l = 0; l < K.L; ++l) {
                 const int32_t b1 = s_layer[l + 1];
-                for (int32_t b = s_layer[l] + qb0; b < b1; b += K.q_bstep) {
-                    const int32_t e0 = s_eptr[b];
-                    const int deg = s_eptr[b + 1] - e0;
-                    for (int32_t r = qr0; r - qr0 < K.Zp; r += K.T) {
-                        if (r >= K.Z) continue;
-                        const uint32_t row = static_cast<uint32_t>(b) * static_cast<uint32_t>(K.Z) +
-                                             static_cast<uint32_t>(r);
-                        uint4 st;
-                        if (R_SMEM) {
-                            st = rs[row];
+                if (!ONE_ROW || qr0 < K.Z) {
+                    for (int32_t b = s_layer[l] + qb0; b < b1; b += K.q_bstep) {
+                        const int32_t e0 = s_eptr[b];
+                        const int deg = s_eptr[b + 1] - e0;
+                        if (ONE_ROW) {
+                            do_row(b, e0, deg, qr0);
                         } else {
-                            const uint2 mm = __ldcg(g12 + row);
-                            st = make_uint4(mm.x, mm.y, __ldcg(g3 + row), 0u);
-                        }
-                        float m1 = __uint_as_float(st.x), m2 = __uint_as_float(st.y);
-                        uint32_t w = st.z;
-                        qc_row<DMAX>(gblk + e0, deg, r4 + 4u * static_cast<uint32_t>(r - qr0), Z4, m1,
-                                     m2, w, K.scale, K.offset);
-                        if (R_SMEM) {
-                            rs[row] = make_uint4(__float_as_uint(m1), __float_as_uint(m2), w, 0u);
-                        } else {
-                            __stcg(g12 + row, make_uint2(__float_as_uint(m1), __float_as_uint(m2)));
-                            __stcg(g3 + row, w);
+                            for (int32_t r = qr0; r - qr0 < K.Zp; r += K.T)
+                                if (r < K.Z) do_row(b, e0, deg, r);
                         }
                     }
                 }
@@ -499,10 +520,15 @@ __global__ void __launch_bounds__(kMixedThreads) ldpc_mixed_kernel(const __grid_
         const int g = threadIdx.x / K.T;
         if (g < K.G) {
             const int tid = threadIdx.x - g * K.T;
-            if (K.r_smem)
-                mixed_frames<DMAX, true>(K, smem, s_layer, s_eptr, s_blk, g, tid);
+            const bool one_row = K.T >= K.Zp;
+            if (K.r_smem && one_row)
+                mixed_frames<DMAX, true, true>(K, smem, s_layer, s_eptr, s_blk, g, tid);
+            else if (K.r_smem)
+                mixed_frames<DMAX, true, false>(K, smem, s_layer, s_eptr, s_blk, g, tid);
+            else if (one_row)
+                mixed_frames<DMAX, false, true>(K, smem, s_layer, s_eptr, s_blk, g, tid);
             else
-                mixed_frames<DMAX, false>(K, smem, s_layer, s_eptr, s_blk, g, tid);
+                mixed_frames<DMAX, false, false>(K, smem, s_layer, s_eptr, s_blk, g, tid);
         }
         __syncthreads();
         if (threadIdx.x == 0) s_code = mixed_pick(p, -1);
@@ -689,8 +715,9 @@ int resolve_shape(const ck_ldpc_plan* plan, int32_t rule, Resolved* r, int* per_
     if (gmax < 1)
         return ck::fail(CK_ERR_UNSUPPORTED, "a frame needs %u bytes of shared memory, %u available",
                         group, budget);
-    KernelFn kernel = sp ? sum_product_kernel(plan->qc, plan->max_deg, app_smem, r_smem)
-                         : min_sum_kernel(plan->qc, plan->max_deg, app_smem, r_smem);
+    const bool one_row = plan->qc && T >= Zp;
+    KernelFn kernel = sp ? sum_product_kernel(plan->qc, plan->max_deg, app_smem, r_smem, one_row)
+                         : min_sum_kernel(plan->qc, plan->max_deg, app_smem, r_smem, one_row);
     if (!kernel) return ck::fail(CK_ERR_UNSUPPORTED, "no decoder kernel for this code shape");
     CK_TRY(ck::allow_max_smem(reinterpret_cast<const void*>(kernel), plan->device, optin));
     if (G == 0) {

@@ -119,19 +119,19 @@ struct SumProductState {
 };
 
 struct SumProductPick {
-    template <bool QC, int DMAX>
+    template <bool QC, int DMAX, bool ONE_ROW>
     static KernelFn get(bool app_smem, bool r_smem) {
-        if (app_smem && r_smem) return decode_kernel<SumProductState, QC, DMAX, true, true>;
-        if (app_smem) return decode_kernel<SumProductState, QC, DMAX, true, false>;
-        if constexpr (!QC) return decode_kernel<SumProductState, QC, DMAX, false, false>;
+        if (app_smem && r_smem) return decode_kernel<SumProductState, QC, DMAX, true, true, ONE_ROW>;
+        if (app_smem) return decode_kernel<SumProductState, QC, DMAX, true, false, ONE_ROW>;
+        if constexpr (!QC) return decode_kernel<SumProductState, QC, DMAX, false, false, false>;
         return nullptr;
     }
 };
 
 }  // namespace sp
 
-KernelFn sum_product_kernel(bool qc, int dmax, bool app_smem, bool r_smem) {
-    return pick_shape<sp::SumProductPick>(qc, dmax, app_smem, r_smem);
+KernelFn sum_product_kernel(bool qc, int dmax, bool app_smem, bool r_smem, bool one_row) {
+    return pick_shape<sp::SumProductPick>(qc, dmax, app_smem, r_smem, one_row);
 }
 
 KernelFn sum_product_cluster_kernel(int dmax) {
