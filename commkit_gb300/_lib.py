@@ -28,6 +28,9 @@ CK_LDPC_SUM_PRODUCT = 1
 CK_LDPC_PLACE_AUTO = 0
 CK_LDPC_PLACE_SHARED = 1
 CK_LDPC_PLACE_GLOBAL = 2
+CK_LDPC_SPECIALISE_AUTO = 0
+CK_LDPC_SPECIALISE_OFF = 1
+CK_LDPC_SPECIALISE_ON = 2
 
 # Every symbol the header declares; tests check the library exports them.
 EXPORTS = (
@@ -53,6 +56,9 @@ EXPORTS = (
     "ck_ldpc_plan_get_info",
     "ck_ldpc_plan_set_launch",
     "ck_ldpc_plan_get_launch",
+    "ck_ldpc_plan_set_specialise",
+    "ck_ldpc_plan_get_specialise",
+    "ck_ldpc_specialised_source",
     "ck_ldpc_workspace_size",
     "ck_ldpc_decode",
     "ck_ldpc_workspace_status",
@@ -161,6 +167,10 @@ def _declare(lib: ctypes.CDLL) -> None:
         "ck_ldpc_plan_get_info": ([p, ctypes.POINTER(PlanInfo)], ctypes.c_int),
         "ck_ldpc_plan_set_launch": ([p, ctypes.POINTER(Launch)], ctypes.c_int),
         "ck_ldpc_plan_get_launch": ([p, ctypes.POINTER(Launch)], ctypes.c_int),
+        "ck_ldpc_plan_set_specialise": ([p, i32], ctypes.c_int),
+        "ck_ldpc_plan_get_specialise": ([p, ctypes.POINTER(i32), ctypes.POINTER(i32)], ctypes.c_int),
+        "ck_ldpc_specialised_source": ([p, p, p, i32, i32, i32, i32, ctypes.c_char_p, ctypes.c_size_t,
+                                        ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
         "ck_ldpc_workspace_size": ([p, i64, i32, size_p], ctypes.c_int),
         "ck_ldpc_decode": (
             [p, p, p, i64, i32, i32, f32, f32, i32, i32, p, p, p, i32, p, ctypes.c_size_t, p],

@@ -40,8 +40,34 @@ def nvcc() -> str:
     return found
 
 
+# Kernel headers the code-specialised decoders are compiled from at run time
+# (NVRTC): embedded in the library as strings.
+JIT_HEADERS = ("ck_device.cuh", "ck_ldpc_kernel.cuh", "ck_ldpc_minsum.cuh", "ck_ldpc_mixed.cuh")
+JIT_SOURCE = BUILD / "ck_jit_headers.cpp"
+
+
+def _jit_headers() -> Path:
+    """Writes the embedded-header source if a header changed since."""
+    deps = [SRC / h for h in JIT_HEADERS]
+    if _stale(JIT_SOURCE, deps):
+        parts = ["// Written by commkit_gb300/build.py: NVRTC sources of the kernel headers.",
+                 f"extern const int ck_jit_header_count = {len(JIT_HEADERS)};",
+                 "extern const char* const ck_jit_header_names[] = {" + ", ".join(f'"{h}"' for h in JIT_HEADERS) + "};",
+                 "extern const char* const ck_jit_header_sources[] = {"]  # fmt: skip
+        for d in deps:
+            text = d.read_text()
+            if ')ckjit"' in text:
+                raise RuntimeError(f"{d.name} holds the raw-string delimiter")
+            parts.append('R"ckjit(' + text + ')ckjit",')
+        parts.append("};")
+        tmp = JIT_SOURCE.with_suffix(f".{os.getpid()}.tmp")
+        tmp.write_text("\n".join(parts) + "\n")
+        os.replace(tmp, JIT_SOURCE)
+    return JIT_SOURCE
+
+
 def _sources() -> list[Path]:
-    return sorted([*SRC.glob("*.cu"), *SRC.glob("*.cpp")])
+    return sorted([*SRC.glob("*.cu"), *SRC.glob("*.cpp")]) + [_jit_headers()]
 
 
 def _headers() -> list[Path]:
@@ -82,7 +108,7 @@ def build(verbose: bool = False) -> Path:
         # The shared CUDA runtime (soname libcudart.so.13): a process that has
         # loaded torch's copy reuses it, so both see one current device.
         cmd = [nvcc(), *ARCH, "-shared", "-cudart", "shared", "-Xlinker", "-rpath=/usr/local/cuda/lib64",
-               "-o", str(tmp), *map(str, objs)]  # fmt: skip
+               "-o", str(tmp), *map(str, objs), "-ldl"]  # fmt: skip
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")

@@ -334,6 +334,20 @@ class _Plan:
         _lib.check(_lib.lib().ck_ldpc_plan_get_launch(self.handle, ctypes.byref(cfg)), "get_launch")
         return cfg.threads_per_frame, cfg.frames_per_block, cfg.placement
 
+    def set_specialise(self, mode: int) -> None:
+        """``_lib.CK_LDPC_SPECIALISE_{AUTO,OFF,ON}``: whether min-sum decodes
+        of this circulant code run its code-specialised kernel."""
+        _lib.check(_lib.lib().ck_ldpc_plan_set_specialise(self.handle, int(mode)), "set_specialise")
+
+    def specialisation(self) -> tuple[int, int, str]:
+        """(mode, state, reason): state 1 compiled, 0 not yet, -1 unavailable
+        (reason says why)."""
+        mode, state = ctypes.c_int32(), ctypes.c_int32()
+        lib = _lib.lib()
+        _lib.check(lib.ck_ldpc_plan_get_specialise(self.handle, ctypes.byref(mode), ctypes.byref(state)),
+                   "get_specialise")  # fmt: skip
+        return mode.value, state.value, (_lib.last_error() if state.value < 0 else "")
+
     def workspace_size(self, frames: int, rule: int = _lib.CK_LDPC_MIN_SUM) -> int:
         size = ctypes.c_size_t(0)
         st = _lib.lib().ck_ldpc_workspace_size(self.handle, int(frames), int(rule), ctypes.byref(size))

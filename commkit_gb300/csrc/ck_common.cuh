@@ -1,11 +1,12 @@
 // Internal helpers shared by the commkit-gb300 CUDA sources: error
-// reporting, fast division by a run-time constant, and the inline-PTX
-// wrappers (named barriers, mbarriers, bulk copies) the kernels use.
+// reporting on the host, and (from ck_device.cuh) fast division by a
+// run-time constant and the inline-PTX wrappers the kernels use.
 #pragma once
 
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "ck_device.cuh"
 #include "commkit_gb300.h"
 
 namespace ck {
@@ -24,127 +25,5 @@ void clear_error();
     } while (0)
 
 #define CK_CUDA(expr) CK_TRY(::ck::cuda_check((expr), #expr))
-
-// q = n / d for 0 <= n < 2^31 and a run-time divisor 1 <= d < 2^31, by a
-// multiply-high and a shift (the round-up method of Granlund and
-// Montgomery, "Division by invariant integers using multiplication", 1994).
-struct FastDiv {
-    uint32_t d;
-    uint32_t mul;
-    uint32_t shift;
-
-    static FastDiv make(uint32_t d) {
-        FastDiv f{d, 0u, 0u};
-        uint32_t l = 0;
-        while ((1ull << l) < d) ++l;
-        f.shift = l;
-        // mul = floor(2^32 (2^l - d) / d) + 1
-        f.mul = static_cast<uint32_t>(((1ull << 32) * ((1ull << l) - d)) / d + 1ull);
-        return f;
-    }
-
-    __host__ __device__ __forceinline__ uint32_t div(uint32_t n) const {
-#ifdef __CUDA_ARCH__
-        const uint32_t hi = __umulhi(n, mul);
-#else
-        const uint32_t hi = static_cast<uint32_t>((static_cast<uint64_t>(n) * mul) >> 32);
-#endif
-        // hi <= n < 2^31, so the sum does not overflow.
-        return (hi + n) >> shift;
-    }
-};
-
-// Iterations a bounded device-side wait spins before it gives up (each
-// try_wait itself suspends for a while, so this is seconds).
-constexpr uint32_t kWaitLimit = 1u << 24;
-
-// Status bits a kernel leaves in its workspace header.
-constexpr uint32_t kStatusTimeout = 1u;
-
-#ifdef __CUDACC__
-
-__device__ __forceinline__ uint32_t smem_addr(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-// Barrier over the `count` threads of one frame group: a named barrier
-// (ids 1..15; 0 is __syncthreads), or the warp when the group is one warp.
-__device__ __forceinline__ void group_sync(int id, int count) {
-    if (count == 32) {
-        __syncwarp();
-    } else {
-        asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
-    }
-}
-
-// OR of `pred` over the group, in every thread of the group.
-__device__ __forceinline__ int group_any(int pred, int id, int count) {
-    if (count == 32) return __any_sync(0xffffffffu, pred);
-    int out;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.s32 p, %1, 0;\n\t"
-        "bar.red.or.pred p, %2, %3, p;\n\t"
-        "selp.s32 %0, 1, 0, p;\n\t}"
-        : "=r"(out)
-        : "r"(pred), "r"(id), "r"(count)
-        : "memory");
-    return out;
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
-                 : "memory");
-}
-
-__device__ __forceinline__ void fence_mbar_init() {
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-// Orders this thread's generic-proxy shared-memory accesses before later
-// async-proxy (bulk copy) accesses.
-__device__ __forceinline__ void fence_proxy_async_smem() {
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile(
-        "mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(
-            smem_addr(bar)),
-        "r"(bytes)
-        : "memory");
-}
-
-// Waits (bounded) for the phase with parity `phase` of `bar` to complete.
-// Returns false if it gave up after kWaitLimit polls.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
-    const uint32_t addr = smem_addr(bar);
-    for (uint32_t i = 0; i < kWaitLimit; ++i) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(addr), "r"(phase)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
-// Bulk copy (TMA, non-tensor) of `bytes` from global to this CTA's shared
-// memory, completing on `bar`.  Both addresses 16-byte aligned; bytes a
-// multiple of 16.
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
-                                         uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
-        "[%3];" ::"r"(smem_addr(dst)),
-        "l"(src), "r"(bytes), "r"(smem_addr(bar))
-        : "memory");
-}
-
-#endif  // __CUDACC__
 
 }  // namespace ck

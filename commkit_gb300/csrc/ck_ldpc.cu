@@ -47,236 +47,16 @@
 #include <tuple>
 #include <utility>
 
+#include "ck_ldpc_cluster.cuh"
 #include "ck_ldpc_kernel.cuh"
+#include "ck_ldpc_minsum.cuh"
+#include "ck_ldpc_mixed.cuh"
 
 
 using namespace ck::ldpc;
 
-namespace {
+static_assert(kMaxMixed == CK_LDPC_MAX_MIXED, "mixed-launch code count");
 
-// One check row, min-sum: reads the row's compressed state (m1, m2, w),
-// updates the posterior `a` of its deg variables (columns from col_of) and
-// writes the new state back.  Two passes as the reference's min_sum_row
-// (commkit/_cuda/src/ldpc.cu:45-72), with Q kept in registers between them
-// (columns are recomputed in the second pass rather than held).
-template <int DMAX, class ColOf>
-__device__ __forceinline__ void min_sum_row(float* __restrict__ a, const int deg,
-                                            const ColOf& col_of, float& m1, float& m2,
-                                            uint32_t& w, const float scale,
-                                            const float offset) {
-    const uint32_t oidx = w >> 27;
-    const uint32_t osign = w;
-    const float om1 = m1, om2 = m2;
-    float q[DMAX];
-    float min1 = CUDART_INF_F, min2 = CUDART_INF_F;
-    uint32_t idx = 31u;  // no edge; matches the reference's -1 when every |Q| is inf
-    uint32_t negs = 0u;
-#pragma unroll
-    for (int e = 0; e < DMAX; ++e) {
-        if (e < deg) {
-            const float r_old =
-                flip_sign(static_cast<uint32_t>(e) == oidx ? om2 : om1, (osign >> e) & 1u);
-            const float qe = __fsub_rn(a[col_of(e)], r_old);
-            q[e] = qe;
-            negs |= (qe < 0.0f ? 1u : 0u) << e;
-            const float mag = fabsf(qe);
-            if (mag < min1) idx = static_cast<uint32_t>(e);
-            min2 = fminf(min2, fmax_nan(min1, mag));
-            min1 = fminf(min1, mag);
-        }
-    }
-    const float n1 = fmaxf(__fsub_rn(__fmul_rn(scale, min1), offset), 0.0f);
-    const float n2 = fmaxf(__fsub_rn(__fmul_rn(scale, min2), offset), 0.0f);
-    // Sign of edge e's new message: the parity of all signs times its own.
-    const uint32_t signs = negs ^ ((__popc(negs) & 1u) ? 0xffffffffu : 0u);
-#pragma unroll
-    for (int e = 0; e < DMAX; ++e) {
-        if (e < deg) {
-            const float rn = flip_sign(static_cast<uint32_t>(e) == idx ? n2 : n1, (signs >> e) & 1u);
-            a[col_of(e)] = __fadd_rn(q[e], rn);
-        }
-    }
-    m1 = n1;
-    m2 = n2;
-    w = (signs & 0x07ffffffu) | (idx << 27);
-}
-
-// The same update for a circulant row of exactly D edges, shaped for the
-// ALU pipe, which bounds this kernel: fully unrolled, columns computed once
-// and kept in registers,
-//  * min1/min2 taken over pairs of edges: with lo/hi the pair's smaller and
-//    larger magnitude, min2 = min(min2, hi, max(min1, lo)) and min1 =
-//    min(min1, lo), five operations per pair instead of six (three-input
-//    min), and half as long a dependency chain; a NaN magnitude (only from
-//    infinite input LLRs) drops out of both, as in the reference,
-//  * the sign bits of Q taken from the float sign (no -0 ever reaches the
-//    posterior: frames are loaded as x + 0, and from such values Q = APP - R
-//    and APP = Q + R_new cannot produce -0 either, so "sign bit set" is
-//    "Q < 0"), one funnel shift per edge;
-//  * the new signs applied with one multiply by the parity sign (exact) and
-//    one bitwise or;
-//  * no running argmin: an edge takes min2' when |Q| equals min1 (a tie
-//    means min2 == min1, so every tied edge gets the same value), and the
-//    stored argmin is the first such edge, found in the second pass.
-// The compressed state keeps the sign of edge e at bit D - 1 - e here.
-template <int D>
-__device__ __forceinline__ void qc_row_fixed(const int2* __restrict__ gblk, const uint32_t r4,
-                                             const uint32_t Z4, float& m1, float& m2, uint32_t& w,
-                                             const float scale, const float offset) {
-    const uint32_t oidx = w >> 27;
-    const uint32_t osign = w;
-    const float om1 = m1, om2 = m2;
-    float q[D];
-    uint32_t c[D];
-    float min1 = CUDART_INF_F, min2 = CUDART_INF_F;
-    uint32_t negs = 0u;
-#pragma unroll
-    for (int e = 0; e < D; ++e) {
-        // gblk[e] = (shared address of the circulant's row-0 column, address
-        // of the block's end): row r's column, wrapped once at the end.
-        const int2 b = gblk[e];
-        uint32_t ce = r4 + static_cast<uint32_t>(b.x);
-        ce = ce >= static_cast<uint32_t>(b.y) ? ce - Z4 : ce;
-        c[e] = ce;
-        const float mag_old = static_cast<uint32_t>(e) == oidx ? om2 : om1;
-        const float r_old = __uint_as_float(__float_as_uint(mag_old) ^
-                                            ((osign << (32 - D + e)) & 0x80000000u));
-        const float qe = __fsub_rn(ld_shared_f32(ce), r_old);
-        q[e] = qe;
-        negs = __funnelshift_l(__float_as_uint(qe), negs, 1);
-        if (e & 1) {
-            const float x = fabsf(q[e - 1]), y = fabsf(qe);
-            const float hi = fmax_nan(x, y);
-            if (e == 1) {
-                min1 = fmin3(x, y, CUDART_INF_F);
-                min2 = fminf(hi, CUDART_INF_F);
-            } else {
-                const float lo = fminf(x, y);
-                min2 = fmin3(min2, hi, fmax_nan(min1, lo));
-                min1 = fminf(min1, lo);
-            }
-        } else if (e == D - 1) {
-            const float mag = fabsf(qe);
-            min2 = fminf(min2, fmax_nan(min1, mag));
-            min1 = fminf(min1, mag);
-        }
-    }
-    const float n1 = fmaxf(__fsub_rn(__fmul_rn(scale, min1), offset), 0.0f);
-    const float n2 = fmaxf(__fsub_rn(__fmul_rn(scale, min2), offset), 0.0f);
-    const bool odd = __popc(negs) & 1u;
-    const float psign = odd ? -1.0f : 1.0f;
-    uint32_t idx = 31u;
-#pragma unroll
-    for (int e = D - 1; e >= 0; --e) {
-        const bool at_min = fabsf(q[e]) == min1;
-        if (at_min) idx = static_cast<uint32_t>(e);
-        const float mag = at_min ? n2 : n1;
-        const float t = __fmul_rn(q[e], psign);
-        const float rn = __uint_as_float(__float_as_uint(mag) | (__float_as_uint(t) & 0x80000000u));
-        st_shared_f32(c[e], __fadd_rn(q[e], rn));
-    }
-    const uint32_t signs = negs ^ (odd ? ((1u << D) - 1u) : 0u);
-    m1 = n1;
-    m2 = n2;
-    w = (signs & 0x07ffffffu) | (idx << 27);
-}
-
-// Degree dispatch of a circulant row (warp-uniform): D = 2..DMAX unrolled,
-// with no case above DMAX (a switch over 2..16 rather than 2..27 for the
-// DMAX = 16 kernels).
-#define CK_ROW_CASE(D) \
-    case D:            \
-        qc_row_fixed<D>(gblk, r4, Z4, m1, m2, w, scale, offset); \
-        break;
-template <int DMAX>
-__device__ __forceinline__ void qc_row(const int2* __restrict__ gblk, const int deg,
-                                       const uint32_t r4, const uint32_t Z4, float& m1, float& m2,
-                                       uint32_t& w, const float scale, const float offset) {
-    if constexpr (DMAX <= 16) {
-        switch (deg) {
-            CK_ROW_CASE(2) CK_ROW_CASE(3) CK_ROW_CASE(4) CK_ROW_CASE(5) CK_ROW_CASE(6)
-            CK_ROW_CASE(7) CK_ROW_CASE(8) CK_ROW_CASE(9) CK_ROW_CASE(10) CK_ROW_CASE(11)
-            CK_ROW_CASE(12) CK_ROW_CASE(13) CK_ROW_CASE(14) CK_ROW_CASE(15) CK_ROW_CASE(16)
-            default:
-                break;
-        }
-    } else {
-        switch (deg) {
-            CK_ROW_CASE(2) CK_ROW_CASE(3) CK_ROW_CASE(4) CK_ROW_CASE(5) CK_ROW_CASE(6)
-            CK_ROW_CASE(7) CK_ROW_CASE(8) CK_ROW_CASE(9) CK_ROW_CASE(10) CK_ROW_CASE(11)
-            CK_ROW_CASE(12) CK_ROW_CASE(13) CK_ROW_CASE(14) CK_ROW_CASE(15) CK_ROW_CASE(16)
-            CK_ROW_CASE(17) CK_ROW_CASE(18) CK_ROW_CASE(19) CK_ROW_CASE(20) CK_ROW_CASE(21)
-            CK_ROW_CASE(22) CK_ROW_CASE(23) CK_ROW_CASE(24) CK_ROW_CASE(25) CK_ROW_CASE(26)
-            CK_ROW_CASE(27)
-            default:
-                break;
-        }
-    }
-}
-#undef CK_ROW_CASE
-
-// Min-sum check-message state of a frame slot: per row (min1', min2', one
-// word of signs and argmin).  In shared memory one 16-byte record per row
-// (one vector access); in device memory 12 bytes, an array of (min1',
-// min2') pairs and one of words (two accesses), so the resident frames'
-// state (code C: 304 frames x 17664 rows x 12 B = 64 MB) stays in L2.  (A
-// 16-byte record there measured 17 % slower on code C: 86 MB of state
-// leaves too little of L2 to the rest.)
-template <bool R_SMEM>
-struct MinSumState {
-    uint4* rs;
-    uint2* g12;
-    uint32_t* g3;
-
-    __device__ __forceinline__ MinSumState(const Params& p, unsigned char* gbase, uint32_t slot)
-        : rs(reinterpret_cast<uint4*>(gbase + p.r_off)),
-          g12(reinterpret_cast<uint2*>(p.g_r + static_cast<size_t>(slot) * 3 * p.r_stride)),
-          g3(p.g_r + static_cast<size_t>(slot) * 3 * p.r_stride + 2 * p.r_stride) {}
-
-    __device__ __forceinline__ void zero(const Params& p, int first, int stride) const {
-        for (int i = first; i < p.m; i += stride) {
-            if (R_SMEM) {
-                rs[i] = make_uint4(0u, 0u, 0u, 0u);
-            } else {
-                g12[i] = make_uint2(0u, 0u);
-                g3[i] = 0u;
-            }
-        }
-    }
-    __device__ __forceinline__ uint4 load(uint32_t row) const {
-        if (R_SMEM) return rs[row];
-        const uint2 m = __ldcg(g12 + row);
-        return make_uint4(m.x, m.y, __ldcg(g3 + row), 0u);
-    }
-    __device__ __forceinline__ void store(uint32_t row, float m1, float m2, uint32_t w) const {
-        if (R_SMEM) {
-            rs[row] = make_uint4(__float_as_uint(m1), __float_as_uint(m2), w, 0u);
-        } else {
-            __stcg(g12 + row, make_uint2(__float_as_uint(m1), __float_as_uint(m2)));
-            __stcg(g3 + row, w);
-        }
-    }
-    template <int DMAX>
-    __device__ __forceinline__ void qc_row(const Params& p, const int2* gblk, int deg, uint32_t row,
-                                           int32_t, int32_t, uint32_t r4, uint32_t Z4) const {
-        const uint4 s = load(row);
-        float m1 = __uint_as_float(s.x), m2 = __uint_as_float(s.y);
-        uint32_t w = s.z;
-        ::qc_row<DMAX>(gblk, deg, r4, Z4, m1, m2, w, p.scale, p.offset);
-        store(row, m1, m2, w);
-    }
-    template <int DMAX, class ColOf>
-    __device__ __forceinline__ void csr_row(const Params& p, float* a, uint32_t row, int deg, int32_t,
-                                            const ColOf& col_of) const {
-        const uint4 s = load(row);
-        float m1 = __uint_as_float(s.x), m2 = __uint_as_float(s.y);
-        uint32_t w = s.z;
-        min_sum_row<DMAX>(a, deg, col_of, m1, m2, w, p.scale, p.offset);
-        store(row, m1, m2, w);
-    }
-};
-
-}  // namespace
 
 namespace ck {
 namespace ldpc {
@@ -306,242 +86,11 @@ KernelFn min_sum_cluster_kernel(int dmax) {
 
 namespace {
 
-// ---------------------------------------------------------------------------
-// Mixed-code persistent kernel: frames of several quasi-cyclic codes in one
-// launch.  Every block can host any code's frame groups (its shared memory
-// and threads are sized for the largest); it starts on a code chosen in
-// proportion to the work and, once that code's queue is empty, switches to
-// the code with the most work left.  The frame loop is the plain kernel's:
-// same rows, same order, same bits.
-// ---------------------------------------------------------------------------
-
-constexpr int kMaxMixed = CK_LDPC_MAX_MIXED;
-constexpr int kMixedThreads = 768;
-
-struct MixedCode {
-    const int32_t* layer;
-    const int32_t* eptr;
-    const int2* blk;
-    int32_t N, m, L, Z, Zp, mb, nnzb;
-    const float* llr_in;
-    float* llr_out;
-    uint32_t B;
-    int32_t n_in;
-    int32_t* iters;
-    uint8_t* valid;
-    int8_t* bits;
-    int32_t k_bits;
-    const int32_t* order;  // queue position -> frame, or null
-    float scale, offset;
-    int32_t max_iterations, early_stop;
-    int32_t T, G, q_bstep, r_smem;
-    uint32_t tables_bytes, group_bytes, gblk_off, app_off, r_off, r_stride;
-    uint32_t* g_r;
-    uint32_t* counter;
-    float weight;  // edges per frame
-};
-
-struct MixedParams {
-    MixedCode code[kMaxMixed];
-    int32_t num_codes;
-    int32_t start_block[kMaxMixed + 1];  // blocks [start_block[c], start_block[c+1]) begin on c
-};
-
-// The code this block should work on next: `prefer` while its queue has
-// frames, else the one with the most edges left; -1 when all are drained.
-__device__ int mixed_pick(const MixedParams& p, int prefer) {
-    if (prefer >= 0) {
-        const uint32_t taken = *reinterpret_cast<volatile uint32_t*>(p.code[prefer].counter);
-        if (taken < p.code[prefer].B) return prefer;
-    }
-    int best = -1;
-    float most = 0.0f;
-    for (int c = 0; c < p.num_codes; ++c) {
-        const uint32_t taken = *reinterpret_cast<volatile uint32_t*>(p.code[c].counter);
-        if (taken >= p.code[c].B) continue;
-        const float left = static_cast<float>(p.code[c].B - taken) * p.code[c].weight;
-        if (best < 0 || left > most) {
-            best = c;
-            most = left;
-        }
-    }
-    return best;
-}
-
-// Decodes frames of code K with group g until K's queue is empty (ONE_ROW:
-// K.T >= K.Zp, one row per visited base row, as in decode_kernel).
-template <int DMAX, bool R_SMEM, bool ONE_ROW>
-__device__ void mixed_frames(const MixedCode& K, unsigned char* smem, const int32_t* s_layer,
-                             const int32_t* s_eptr, const int2* s_blk, const int g,
-                             const int tid) {
-    using ck::group_any;
-    using ck::group_sync;
-    const int bar = g + 1;
-    unsigned char* gbase = smem + K.tables_bytes + static_cast<uint32_t>(g) * K.group_bytes;
-    volatile uint32_t* s_frame = reinterpret_cast<volatile uint32_t*>(gbase + 8);
-    float* a = reinterpret_cast<float*>(gbase + K.app_off);
-    const uint32_t slot = blockIdx.x * static_cast<uint32_t>(K.G) + static_cast<uint32_t>(g);
-    uint4* rs = reinterpret_cast<uint4*>(gbase + K.r_off);
-    uint2* g12 = reinterpret_cast<uint2*>(K.g_r + static_cast<size_t>(slot) * 3 * K.r_stride);
-    uint32_t* g3 = K.g_r + static_cast<size_t>(slot) * 3 * K.r_stride + 2 * K.r_stride;
-    int2* gblk = reinterpret_cast<int2*>(gbase + K.gblk_off);
-    const uint32_t a_addr = ck::smem_addr(a);
-    for (int i = tid; i < K.nnzb; i += K.T)
-        gblk[i] = make_int2(static_cast<int>(a_addr + 4u * static_cast<uint32_t>(s_blk[i].x)),
-                            static_cast<int>(a_addr + 4u * static_cast<uint32_t>(s_blk[i].y)));
-    const int32_t qr0 = K.T >= K.Zp ? tid % K.Zp : tid;
-    const int32_t qb0 = K.T >= K.Zp ? tid / K.Zp : 0;
-    const uint32_t r4 = 4u * static_cast<uint32_t>(qr0);
-    const uint32_t Z4 = 4u * static_cast<uint32_t>(K.Z);
-
-    auto syndrome_ok = [&]() -> bool {
-        const int32_t rounds = (K.mb + K.q_bstep - 1) / K.q_bstep;
-        for (int32_t k = 0; k < rounds; ++k) {
-            const int32_t b = k * K.q_bstep + qb0;
-            for (int32_t r = qr0; r - qr0 < K.Zp; r += K.T) {
-                uint32_t parity = 0;
-                if (b < K.mb && r < K.Z) {
-                    const int32_t e0 = s_eptr[b];
-                    const int deg = s_eptr[b + 1] - e0;
-                    const QcCols col_of{s_blk + e0, r, K.Z};
-                    for (int e = 0; e < deg; ++e) parity ^= a[col_of(e)] < 0.0f ? 1u : 0u;
-                }
-                if (group_any(static_cast<int>(parity), bar, K.T)) return false;
-            }
-        }
-        return true;
-    };
-
-    for (;;) {
-        if (tid == 0) *s_frame = atomicAdd(K.counter, 1u);
-        group_sync(bar, K.T);
-        const uint32_t pos = *s_frame;
-        if (pos >= K.B) break;
-        const uint32_t f = K.order ? static_cast<uint32_t>(__ldg(K.order + pos)) : pos;
-        const float* src = K.llr_in + static_cast<size_t>(f) * K.n_in;
-        for (int i = tid; i < K.n_in; i += K.T) a[i] = __fadd_rn(__ldcs(src + i), 0.0f);
-        for (int i = K.n_in + tid; i < K.N; i += K.T) a[i] = 0.0f;
-        for (int i = tid; i < K.m; i += K.T) {
-            if (R_SMEM) {
-                rs[i] = make_uint4(0u, 0u, 0u, 0u);
-            } else {
-                g12[i] = make_uint2(0u, 0u);
-                g3[i] = 0u;
-            }
-        }
-        group_sync(bar, K.T);
-        int32_t it = 0;
-        bool ok = K.early_stop && syndrome_ok();
-        while (!ok && it < K.max_iterations) {
-            // One check row: row r of base row b (circulants e0 .. e0 + deg).
-            auto do_row = [&](int32_t b, int32_t e0, int deg, int32_t r) {
-                const uint32_t row = static_cast<uint32_t>(b) * static_cast<uint32_t>(K.Z) +
-                                     static_cast<uint32_t>(r);
-                uint4 st;
-                if (R_SMEM) {
-                    st = rs[row];
-                } else {
-                    const uint2 mm = __ldcg(g12 + row);
-                    st = make_uint4(mm.x, mm.y, __ldcg(g3 + row), 0u);
-                }
-                float m1 = __uint_as_float(st.x), m2 = __uint_as_float(st.y);
-                uint32_t w = st.z;
-                qc_row<DMAX>(gblk + e0, deg, r4 + 4u * static_cast<uint32_t>(r - qr0), Z4, m1, m2, w,
-                             K.scale, K.offset);
-                if (R_SMEM) {
-                    rs[row] = make_uint4(__float_as_uint(m1), __float_as_uint(m2), w, 0u);
-                } else {
-                    __stcg(g12 + row, make_uint2(__float_as_uint(m1), __float_as_uint(m2)));
-                    __stcg(g3 + row, w);
-                }
-            };
-            for (int32_t l = 0; l < K.L; ++l) {
-                const int32_t b1 = s_layer[l + 1];
-                if (!ONE_ROW || qr0 < K.Z) {
-                    for (int32_t b = s_layer[l] + qb0; b < b1; b += K.q_bstep) {
-                        const int32_t e0 = s_eptr[b];
-                        const int deg = s_eptr[b + 1] - e0;
-                        if (ONE_ROW) {
-                            do_row(b, e0, deg, qr0);
-                        } else {
-                            for (int32_t r = qr0; r - qr0 < K.Zp; r += K.T)
-                                if (r < K.Z) do_row(b, e0, deg, r);
-                        }
-                    }
-                }
-                group_sync(bar, K.T);
-            }
-            ++it;
-            if (K.early_stop) ok = syndrome_ok();
-        }
-        if (!K.early_stop) ok = syndrome_ok();
-        float* dst = K.llr_out + static_cast<size_t>(f) * K.n_in;
-        for (int i = tid; i < K.n_in; i += K.T) __stcs(dst + i, a[i]);
-        if (K.bits) {
-            int8_t* bdst = K.bits + static_cast<size_t>(f) * K.k_bits;
-            for (int i = tid; i < K.k_bits; i += K.T) bdst[i] = a[i] < 0.0f ? 1 : 0;
-        }
-        // The iteration count is written last, after a system-scope fence
-        // that follows the group's writes: a host that reads it from mapped
-        // memory (the request server polls frames as they finish) then also
-        // sees the frame's LLRs, bits and flag.
-        group_sync(bar, K.T);
-        if (tid == 0) {
-            K.valid[f] = ok ? 1 : 0;
-            __threadfence_system();
-            K.iters[f] = it;
-        }
-        group_sync(bar, K.T);
-    }
-}
-
-template <int DMAX>
-__global__ void __launch_bounds__(kMixedThreads) ldpc_mixed_kernel(const __grid_constant__ MixedParams p) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ int s_code;
-    if (threadIdx.x == 0) {
-        int c = 0;
-        while (c + 1 < p.num_codes && static_cast<int32_t>(blockIdx.x) >= p.start_block[c + 1]) ++c;
-        s_code = mixed_pick(p, c);
-    }
-    __syncthreads();
-    for (;;) {
-        const int c = s_code;
-        if (c < 0) break;
-        const MixedCode& K = p.code[c];
-        int32_t* s_layer = reinterpret_cast<int32_t*>(smem);
-        int32_t* s_eptr = s_layer + (K.L + 1);
-        int2* s_blk = reinterpret_cast<int2*>(
-            smem + ((static_cast<uint32_t>(K.L + 1 + K.mb + 1) * 4 + 7) & ~7u));
-        for (int i = threadIdx.x; i <= K.L; i += blockDim.x) s_layer[i] = K.layer[i];
-        for (int i = threadIdx.x; i <= K.mb; i += blockDim.x) s_eptr[i] = K.eptr[i];
-        for (int i = threadIdx.x; i < K.nnzb; i += blockDim.x) s_blk[i] = K.blk[i];
-        __syncthreads();
-        const int g = threadIdx.x / K.T;
-        if (g < K.G) {
-            const int tid = threadIdx.x - g * K.T;
-            const bool one_row = K.T >= K.Zp;
-            if (K.r_smem && one_row)
-                mixed_frames<DMAX, true, true>(K, smem, s_layer, s_eptr, s_blk, g, tid);
-            else if (K.r_smem)
-                mixed_frames<DMAX, true, false>(K, smem, s_layer, s_eptr, s_blk, g, tid);
-            else if (one_row)
-                mixed_frames<DMAX, false, true>(K, smem, s_layer, s_eptr, s_blk, g, tid);
-            else
-                mixed_frames<DMAX, false, false>(K, smem, s_layer, s_eptr, s_blk, g, tid);
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) s_code = mixed_pick(p, -1);
-        __syncthreads();
-    }
-}
-
-using KernelMixed = void (*)(MixedParams);
 
 uint32_t align_up(uint32_t v, uint32_t a) { return (v + a - 1) / a * a; }
 
 struct Resolved {
-    KernelFn kernel;
+    const void* kernel;  // a __global__ function, or a code-specialised kernel handle
     int32_t T, G;
     bool app_smem, r_smem;
     uint32_t tables_bytes, group_bytes, gblk_off, app_off, r_off, r_stride, smem;
@@ -580,7 +129,8 @@ int resolve(const ck_ldpc_plan* plan, int32_t rule, int64_t B, Resolved* r) {
     {
         std::lock_guard<std::mutex> lock(plan->shape_mu);
         auto& c = plan->shape_cache[rule];
-        if (c.valid && memcmp(&c.launch, &plan->launch, sizeof(ck_ldpc_launch)) == 0) {
+        if (c.valid && memcmp(&c.launch, &plan->launch, sizeof(ck_ldpc_launch)) == 0 &&
+            c.jit_mode == plan->jit_mode) {
             memcpy(static_cast<void*>(r), c.resolved, sizeof(Resolved));
             per_sm = c.per_sm;
             sms = c.sms;
@@ -588,6 +138,7 @@ int resolve(const ck_ldpc_plan* plan, int32_t rule, int64_t B, Resolved* r) {
             CK_TRY(resolve_shape(plan, rule, r, &per_sm, &sms));
             memcpy(c.resolved, static_cast<const void*>(r), sizeof(Resolved));
             c.launch = plan->launch;
+            c.jit_mode = plan->jit_mode;
             c.per_sm = per_sm;
             c.sms = sms;
             c.valid = true;
@@ -716,18 +267,24 @@ int resolve_shape(const ck_ldpc_plan* plan, int32_t rule, Resolved* r, int* per_
         return ck::fail(CK_ERR_UNSUPPORTED, "a frame needs %u bytes of shared memory, %u available",
                         group, budget);
     const bool one_row = plan->qc && T >= Zp;
-    KernelFn kernel = sp ? sum_product_kernel(plan->qc, plan->max_deg, app_smem, r_smem, one_row)
-                         : min_sum_kernel(plan->qc, plan->max_deg, app_smem, r_smem, one_row);
-    if (!kernel) return ck::fail(CK_ERR_UNSUPPORTED, "no decoder kernel for this code shape");
-    CK_TRY(ck::allow_max_smem(reinterpret_cast<const void*>(kernel), plan->device, optin));
+    const KernelFn table = sp ? sum_product_kernel(plan->qc, plan->max_deg, app_smem, r_smem, one_row)
+                              : min_sum_kernel(plan->qc, plan->max_deg, app_smem, r_smem, one_row);
+    if (!table) return ck::fail(CK_ERR_UNSUPPORTED, "no decoder kernel for this code shape");
+    const void* kernel = reinterpret_cast<const void*>(table);
+    if (!sp && plan->qc && T == Zp && app_smem) {
+        // The code-specialised kernel, where the plan has one.
+        const void* special = nullptr;
+        CK_TRY(specialised_kernel(plan, plan->max_deg <= 16 ? 16 : 27, r_smem, &special));
+        if (special) kernel = special;
+    }
+    CK_TRY(ck::allow_max_smem(kernel, plan->device, optin));
     if (G == 0) {
         // The most resident frames per SM (registers, shared memory, threads),
         // the smaller block on a tie.
         int best = 0;
         for (int32_t g = 1; g <= gmax; ++g) {
             int per_sm = 0;
-            CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &per_sm, reinterpret_cast<const void*>(kernel), T * g, tables + g * group));
+            CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, T * g, tables + g * group));
             if (per_sm * g > best) {
                 best = per_sm * g;
                 G = g;
@@ -756,8 +313,7 @@ int resolve_shape(const ck_ldpc_plan* plan, int32_t rule, Resolved* r, int* per_
     r->app_stride = static_cast<int32_t>(app_bytes / 4);
 
     int per_sm = 0;
-    CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, reinterpret_cast<const void*>(r->kernel), T * G, r->smem));
+    CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, r->kernel, T * G, r->smem));
     if (per_sm < 1)
         return ck::fail(CK_ERR_UNSUPPORTED,
                         "decoder block of %d threads and %u bytes of shared memory does not fit "
@@ -785,8 +341,10 @@ int resolve_shape(const ck_ldpc_plan* plan, int32_t rule, Resolved* r, int* per_
 // its cluster size.
 int launch_decode(const Resolved& r, const Params& p, cudaStream_t s) {
     if (r.cluster <= 1) {
-        r.kernel<<<r.grid, r.T * r.G, r.smem, s>>>(p);
-        return ck::cuda_check(cudaGetLastError(), "decoder launch");
+        void* args[] = {const_cast<Params*>(&p)};
+        return ck::cuda_check(cudaLaunchKernel(r.kernel, dim3(static_cast<unsigned>(r.grid)),
+                                               dim3(static_cast<unsigned>(r.T * r.G)), args, r.smem, s),
+                              "decoder launch");
     }
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr;
@@ -1014,6 +572,7 @@ namespace {
 
 struct MixedResolved {
     MixedParams p;
+    const void* kernel;  // the table-driven kernel or a code-specialised one
     int block_threads;
     uint32_t smem;
     int grid;
@@ -1021,6 +580,25 @@ struct MixedResolved {
     size_t r_off[kMaxMixed];
     bool wide;  // some code has rows above degree 16
 };
+
+// Occupancy per (kernel, device, block shape), remembered: the request
+// server launches a mixed batch per admission.  forget_kernel drops a
+// kernel's entries.
+std::mutex g_occ_mu;
+std::map<std::tuple<const void*, int, int, uint32_t>, int> g_occ;
+
+int mixed_occupancy(const void* kernel, int dev, int threads, uint32_t smem, int* per_sm) {
+    const auto key = std::make_tuple(kernel, dev, threads, smem);
+    std::lock_guard<std::mutex> lock(g_occ_mu);
+    auto it = g_occ.find(key);
+    if (it != g_occ.end()) {
+        *per_sm = it->second;
+        return CK_OK;
+    }
+    CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, kernel, threads, smem));
+    g_occ[key] = *per_sm;
+    return CK_OK;
+}
 
 int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
     if (!batches || n < 1 || n > kMaxMixed)
@@ -1123,25 +701,23 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
     if (R->wide && R->block_threads > 512)
         return ck::fail(CK_ERR_UNSUPPORTED, "mixed launch of %d threads with rows above degree 16",
                         R->block_threads);
-    KernelMixed kernel = R->wide ? ldpc_mixed_kernel<27> : ldpc_mixed_kernel<16>;
-    CK_TRY(ck::allow_max_smem(reinterpret_cast<const void*>(kernel), dev, optin));
-    int per_sm = 0;
+    const void* kernel = reinterpret_cast<const void*>(R->wide ? ldpc_mixed_kernel<27> : ldpc_mixed_kernel<16>);
     {
-        // Occupancy per (kernel, device, block shape), remembered: the
-        // request server launches a mixed batch per admission.
-        static std::mutex mu;
-        static std::map<std::tuple<const void*, int, int, uint32_t>, int> known;
-        const auto key = std::make_tuple(reinterpret_cast<const void*>(kernel), dev, R->block_threads, R->smem);
-        std::lock_guard<std::mutex> lock(mu);
-        auto it = known.find(key);
-        if (it != known.end()) {
-            per_sm = it->second;
-        } else {
-            CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(kernel),
-                                                                  R->block_threads, R->smem));
-            known[key] = per_sm;
+        // The code-specialised mixed kernel, where the plans have one.
+        const ck_ldpc_plan* plans[kMaxMixed];
+        int32_t threads[kMaxMixed];
+        for (int c = 0; c < n; ++c) {
+            plans[c] = batches[c].plan;
+            threads[c] = R->p.code[c].T;
         }
+        const void* special = nullptr;
+        CK_TRY(ck::ldpc::mixed_specialised_kernel(plans, threads, n, R->wide ? 27 : 16, &special));
+        if (special) kernel = special;
     }
+    R->kernel = kernel;
+    CK_TRY(ck::allow_max_smem(kernel, dev, optin));
+    int per_sm = 0;
+    CK_TRY(mixed_occupancy(kernel, dev, R->block_threads, R->smem, &per_sm));
     if (per_sm < 1) return ck::fail(CK_ERR_UNSUPPORTED, "mixed block does not fit an SM");
     int64_t need = 0;
     for (int c = 0; c < n; ++c)
@@ -1214,9 +790,10 @@ extern "C" int ck_ldpc_decode_mixed(const ck_ldpc_batch* batches, int32_t num_ba
     }
     int status = ck::cuda_check(cudaMemsetAsync(wsb, 0, kHeaderBytes, s), "cudaMemsetAsync");
     if (status == CK_OK) {
-        KernelMixed kernel = R.wide ? ldpc_mixed_kernel<27> : ldpc_mixed_kernel<16>;
-        kernel<<<R.grid, R.block_threads, R.smem, s>>>(R.p);
-        status = ck::cuda_check(cudaGetLastError(), "mixed decoder launch");
+        void* args[] = {&R.p};
+        status = ck::cuda_check(cudaLaunchKernel(R.kernel, dim3(static_cast<unsigned>(R.grid)),
+                                                 dim3(static_cast<unsigned>(R.block_threads)), args, R.smem, s),
+                                "mixed decoder launch");
     }
     if (owned) {
         const int st = ck::cuda_check(cudaFreeAsync(ws, s), "cudaFreeAsync");
@@ -1225,10 +802,25 @@ extern "C" int ck_ldpc_decode_mixed(const ck_ldpc_batch* batches, int32_t num_ba
     return status;
 }
 
+namespace {
+std::mutex g_smem_mu;
+std::set<std::pair<const void*, int>> g_smem_done;  // (kernel, device) pairs already raised
+}  // namespace
+
+void ck::forget_kernel(const void* kernel) {
+    {
+        std::lock_guard<std::mutex> lock(g_smem_mu);
+        for (auto it = g_smem_done.begin(); it != g_smem_done.end();)
+            it = it->first == kernel ? g_smem_done.erase(it) : std::next(it);
+    }
+    std::lock_guard<std::mutex> lock(g_occ_mu);
+    for (auto it = g_occ.begin(); it != g_occ.end();)
+        it = std::get<0>(it->first) == kernel ? g_occ.erase(it) : std::next(it);
+}
+
 int ck::allow_max_smem(const void* kernel, int device, int optin) {
-    static std::mutex mu;
-    static std::set<std::pair<const void*, int>> done;
-    std::lock_guard<std::mutex> lock(mu);
+    std::lock_guard<std::mutex> lock(g_smem_mu);
+    auto& done = g_smem_done;
     if (done.count({kernel, device})) return CK_OK;
     // The limit covers dynamic shared memory only: the opt-in maximum less
     // the kernel's static shared variables.

@@ -4,6 +4,7 @@
 #include <stdint.h>
 
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "ck_common.cuh"
@@ -16,8 +17,6 @@ constexpr int32_t kMaxRowDegree = 27;
 // Circulant tables held in shared memory.
 constexpr int32_t kMaxBaseRows = 1024;
 constexpr int32_t kMaxBlocks = 2048;
-// Frame groups of more than one warp synchronize on named barriers 1..15.
-constexpr int32_t kMaxNamedGroups = 15;
 
 }  // namespace ck
 
@@ -61,11 +60,25 @@ struct ck_ldpc_plan {
     struct ShapeCache {
         bool valid = false;
         ck_ldpc_launch launch{0, 0, 0};
+        int32_t jit_mode = 0;
         int per_sm = 0, sms = 0;
         alignas(16) unsigned char resolved[192];
     };
     mutable ShapeCache shape_cache[2];
     mutable std::mutex shape_mu;
+    // Code-specialised min-sum kernels (ck_ldpc_jit.cu), compiled on first
+    // use: one per message-state placement.
+    struct Jit {
+        bool tried = false;
+        int dmax = 0;
+        cudaLibrary_t lib = nullptr;
+        const void* kernel[2] = {nullptr, nullptr};
+        std::string why;  // why there are none
+    };
+    uint64_t id = 0;  // unique in the process, never reused
+    int32_t jit_mode = CK_LDPC_SPECIALISE_AUTO;
+    mutable Jit jit;
+    mutable std::mutex jit_mu;
 };
 
 namespace ck {
@@ -74,4 +87,26 @@ namespace ck {
 // limit set per call would let plans sharing the kernel lower it under one
 // another).
 int allow_max_smem(const void* kernel, int device, int optin);
+// Drops a kernel from allow_max_smem's record before its module is unloaded
+// (a kernel loaded later may get the same handle).
+void forget_kernel(const void* kernel);
+namespace ldpc {
+// The plan's code-specialised min-sum kernel for a row-degree bound and a
+// message-state placement (compiled on first use), or nullptr in *out when
+// the plan has none (specialisation off, NVRTC missing or the compilation
+// failed); an error only when the plan requires specialisation.
+int specialised_kernel(const ck_ldpc_plan* plan, int dmax, bool r_smem, const void** out);
+// The NVRTC source of a circulant plan's specialised kernels.
+std::string specialised_source(const ck_ldpc_plan& plan, int dmax);
+// The NVRTC source of the specialised mixed kernel of n plans.
+std::string mixed_source(const ck_ldpc_plan* const* plans, const bool* special, int n, int dmax);
+// The code-specialised mixed kernel for these plans with threads per frame
+// T[c] (codes with T[c] == Z rounded up to whole warps run their programs,
+// the others the table loop), compiled on first use; nullptr in *out when
+// there is none.
+int mixed_specialised_kernel(const ck_ldpc_plan* const* plans, const int32_t* T, int n, int dmax,
+                             const void** out);
+// Unloads the specialised kernels that use `plan` (before it is freed).
+void forget_plan_kernels(const ck_ldpc_plan* plan);
+}  // namespace ldpc
 }  // namespace ck

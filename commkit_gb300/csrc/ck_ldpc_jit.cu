@@ -1,0 +1,344 @@
+// Code-specialised min-sum decoders for circulant codes, generated from a
+// plan and compiled at run time with NVRTC.
+//
+// The table-driven kernel reads, for every check row, its base row's
+// degree (a switch over the unrolled row bodies), its circulants' block
+// columns and shifts (shared-memory loads) and its row index.  A
+// specialised kernel has all of them as constants: every layer of one
+// iteration is straight-line code, each row's columns are an add and a
+// conditional subtract of constants, its message state an access at a
+// constant offset.  The frame loop around it (queue, staging, syndrome
+// test, outputs) and the row arithmetic are the same code as the table
+// kernel's (decode_body and qc_row_cols, compiled from the same headers),
+// so results are bit-identical; on code C (46 x 68 base, Z = 384) the
+// specialised iteration ran 1.22x faster in a side-by-side timing.
+//
+// Applies to min-sum decodes of circulant codes launched with one frame
+// group thread per row slot (threads per frame == Z rounded up to whole
+// warps).  NVRTC is loaded with dlopen; where it is missing, or a
+// compilation fails, decodes keep the table-driven kernel unless the plan
+// requires specialisation.
+#include <dlfcn.h>
+#include <stdlib.h>
+
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "ck_ldpc_internal.h"
+#include "ck_ldpc_kernel.cuh"
+#include "ck_ldpc_mixed.cuh"
+
+// The NVRTC sources of the kernel headers (written by the build).
+extern const int ck_jit_header_count;
+extern const char* const ck_jit_header_names[];
+extern const char* const ck_jit_header_sources[];
+
+namespace ck {
+namespace ldpc {
+namespace {
+
+struct Nvrtc {
+    using Create = int (*)(void**, const char*, const char*, int, const char* const*, const char* const*);
+    using Compile = int (*)(void*, int, const char* const*);
+    using Size = int (*)(void*, size_t*);
+    using Get = int (*)(void*, char*);
+    using Destroy = int (*)(void**);
+    Create create = nullptr;
+    Compile compile = nullptr;
+    Size log_size = nullptr, cubin_size = nullptr;
+    Get log = nullptr, cubin = nullptr;
+    Destroy destroy = nullptr;
+    std::string why;  // why it is unavailable
+};
+
+const Nvrtc& nvrtc() {
+    static const Nvrtc n = [] {
+        Nvrtc r;
+        void* h = nullptr;
+        std::string tried;
+        std::string paths[] = {"libnvrtc.so.13", "libnvrtc.so", "", "/usr/local/cuda/lib64/libnvrtc.so.13"};
+        if (const char* home = getenv("CUDA_HOME")) paths[2] = std::string(home) + "/lib64/libnvrtc.so.13";
+        for (const std::string& p : paths) {
+            if (p.empty()) continue;
+            h = dlopen(p.c_str(), RTLD_NOW | RTLD_LOCAL);
+            if (h) break;
+            tried += (tried.empty() ? "" : ", ") + p;
+        }
+        if (!h) {
+            r.why = "NVRTC not found (tried " + tried + ")";
+            return r;
+        }
+        r.create = reinterpret_cast<Nvrtc::Create>(dlsym(h, "nvrtcCreateProgram"));
+        r.compile = reinterpret_cast<Nvrtc::Compile>(dlsym(h, "nvrtcCompileProgram"));
+        r.log_size = reinterpret_cast<Nvrtc::Size>(dlsym(h, "nvrtcGetProgramLogSize"));
+        r.log = reinterpret_cast<Nvrtc::Get>(dlsym(h, "nvrtcGetProgramLog"));
+        r.cubin_size = reinterpret_cast<Nvrtc::Size>(dlsym(h, "nvrtcGetCUBINSize"));
+        r.cubin = reinterpret_cast<Nvrtc::Get>(dlsym(h, "nvrtcGetCUBIN"));
+        r.destroy = reinterpret_cast<Nvrtc::Destroy>(dlsym(h, "nvrtcDestroyProgram"));
+        if (!r.create || !r.compile || !r.log_size || !r.log || !r.cubin_size || !r.cubin || !r.destroy) {
+            r.why = "NVRTC lacks an entry point";
+            r.create = nullptr;
+        }
+        return r;
+    }();
+    return n;
+}
+
+void add(std::string& s, const char* fmt, long long a = 0, long long b = 0, long long c = 0) {
+    char buf[256];
+    snprintf(buf, sizeof(buf), fmt, a, b, c);
+    s += buf;
+}
+
+// The program of one circulant code, as struct `name`: every layer's base
+// rows, each as its columns (row qr0 of circulant (j, shift) is column j Z +
+// (qr0 + shift) mod Z) and its state row b Z + qr0, then the group barrier.
+std::string program_struct(const ck_ldpc_plan& plan, const char* name) {
+    const int32_t Z = plan.Z, Zp = (Z + 31) / 32 * 32;
+    std::string s;
+    s += "struct ";
+    s += name;
+    s += " {\n";
+    s += "    static constexpr bool kSpecialised = true;\n";
+    s += "    template <class St>\n";
+    s += "    __device__ __forceinline__ static void iteration(const St& st, const uint32_t base4_in, const uint32_t qr0_in,\n";
+    s += "                                                     const float scale, const float offset, const int bar,\n";
+    s += "                                                     const int T) {\n";
+    // Opaque copies of the thread's offsets, taken anew each iteration: the
+    // columns and state addresses derived from them are then computed where
+    // they are used instead of being hoisted out of the iteration loop and
+    // held (or spilled) across it.
+    s += "        uint32_t base4, qr0;\n";
+    s += "        asm volatile(\"mov.b32 %0, %1;\" : \"=r\"(base4) : \"r\"(base4_in));\n";
+    s += "        asm volatile(\"mov.b32 %0, %1;\" : \"=r\"(qr0) : \"r\"(qr0_in));\n";
+    for (int32_t l = 0; l < plan.L; ++l) {
+        add(s, "        // layer %lld\n", l);
+        if (Zp != Z) add(s, "        if (qr0 < %lldu) {\n", Z);
+        for (int32_t b = plan.h_layer[l]; b < plan.h_layer[l + 1]; ++b) {
+            const int32_t e0 = plan.h_eptr[b], deg = plan.h_eptr[b + 1] - e0;
+            add(s, "        {\n            uint32_t c[%lld];\n", deg);
+            for (int32_t e = 0; e < deg; ++e) {
+                const int32_t first = plan.h_blk[2 * (e0 + e)];    // j Z + shift
+                const int32_t end = plan.h_blk[2 * (e0 + e) + 1];  // (j + 1) Z
+                add(s, "            c[%lld] = base4 + %lldu;", e, 4ll * first);
+                if (end - first < Z) add(s, " if (qr0 >= %lldu) c[%lld] -= ", end - first, e);
+                if (end - first < Z) add(s, "%lldu;", 4ll * Z);
+                s += "\n";
+            }
+            add(s, "            st.template row_cols<%lld>(c, %lldu + qr0, scale, offset);\n        }\n", deg,
+                static_cast<long long>(b) * Z);
+        }
+        if (Zp != Z) s += "        }\n";
+        s += "        ck::group_sync(bar, T);\n";
+    }
+    s += "    }\n};\n";
+    return s;
+}
+
+// The plain decoder of one code: one kernel per message-state placement
+// (device memory, shared memory).
+std::string program_source(const ck_ldpc_plan& plan, int dmax) {
+    std::string s = "#include \"ck_ldpc_minsum.cuh\"\nusing namespace ck::ldpc;\nnamespace {\n";
+    s += program_struct(plan, "CodeProgram");
+    s += "}  // namespace\n";
+    for (int r = 0; r < 2; ++r) {
+        add(s, "extern \"C\" __global__ void __launch_bounds__(%lld) ck_ldpc_code_r%lld(const __grid_constant__ Params p) {\n",
+            max_block_threads(true, dmax), r);
+        add(s, "    decode_body<MinSumState, true, %lld, true, ", dmax);
+        s += r ? "true" : "false";
+        s += ", true, CodeProgram>(p);\n}\n";
+    }
+    return s;
+}
+
+// The mixed decoder of n codes; code c runs its program when special[c].
+std::string mixed_program_source(const ck_ldpc_plan* const* plans, const bool* special, int n, int dmax) {
+    std::string s = "#include \"ck_ldpc_mixed.cuh\"\nusing namespace ck::ldpc;\nnamespace {\n";
+    for (int c = 0; c < n; ++c)
+        if (special[c]) s += program_struct(*plans[c], ("CodeProgram" + std::to_string(c)).c_str());
+    s += "struct CodeDispatch {\n";
+    s += "    template <int DMAX>\n";
+    s += "    __device__ __forceinline__ static void run(int c, const MixedCode& K, unsigned char* smem,\n";
+    s += "                                               const int32_t* s_layer, const int32_t* s_eptr,\n";
+    s += "                                               const int2* s_blk, int g, int tid) {\n";
+    s += "        switch (c) {\n";
+    for (int c = 0; c < n; ++c) {
+        add(s, "            case %lld:\n", c);
+        if (special[c]) {
+            const std::string prog = "CodeProgram" + std::to_string(c);
+            s += "                if (K.r_smem)\n";
+            s += "                    mixed_frames<DMAX, true, true, " + prog + ">(K, smem, s_layer, s_eptr, s_blk, g, tid);\n";
+            s += "                else\n";
+            s += "                    mixed_frames<DMAX, false, true, " + prog + ">(K, smem, s_layer, s_eptr, s_blk, g, tid);\n";
+        } else {
+            s += "                TableDispatch::run<DMAX>(c, K, smem, s_layer, s_eptr, s_blk, g, tid);\n";
+        }
+        s += "                break;\n";
+    }
+    s += "            default:\n                break;\n        }\n    }\n};\n}  // namespace\n";
+    add(s, "extern \"C\" __global__ void __launch_bounds__(kMixedThreads) ck_ldpc_mixed_code(const __grid_constant__ MixedParams p) {\n    mixed_body<%lld, CodeDispatch>(p);\n}\n", dmax);
+    return s;
+}
+
+// Compiles `src` and loads `names` from it; returns false with `why` set
+// when that fails.
+bool compile_load(const std::string& src, int device, const char* const* names, int count, cudaLibrary_t* lib,
+                  const void** kernels, std::string* why) {
+    const Nvrtc& nv = nvrtc();
+    if (!nv.create) {
+        *why = nv.why;
+        return false;
+    }
+    void* prog = nullptr;
+    if (nv.create(&prog, src.c_str(), "ck_ldpc_code.cu", ck_jit_header_count, ck_jit_header_sources,
+                  ck_jit_header_names) != 0) {
+        *why = "nvrtcCreateProgram failed";
+        return false;
+    }
+    int major = 0, minor = 0;
+    (void)cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device);
+    (void)cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device);
+    const std::string arch = "-arch=sm_" + std::to_string(major * 10 + minor) + "a";
+    const char* opts[] = {arch.c_str(), "-std=c++17", "-fmad=false"};
+    bool ok = false;
+    if (nv.compile(prog, 3, opts) != 0) {
+        size_t n = 0;
+        nv.log_size(prog, &n);
+        std::string log(n, '\0');
+        if (n) nv.log(prog, &log[0]);
+        *why = "NVRTC compilation failed: " + log.substr(0, 2000);
+    } else {
+        size_t n = 0;
+        nv.cubin_size(prog, &n);
+        std::string cubin(n, '\0');
+        nv.cubin(prog, &cubin[0]);
+        cudaError_t ce = cudaLibraryLoadData(lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+        for (int i = 0; i < count && ce == cudaSuccess; ++i) {
+            cudaKernel_t k = nullptr;
+            ce = cudaLibraryGetKernel(&k, *lib, names[i]);
+            kernels[i] = reinterpret_cast<const void*>(k);
+        }
+        if (ce != cudaSuccess) {
+            (void)cudaGetLastError();
+            if (*lib) (void)cudaLibraryUnload(*lib);
+            *lib = nullptr;
+            *why = std::string("loading the specialised kernels failed: ") + cudaGetErrorString(ce);
+        } else {
+            ok = true;
+        }
+    }
+    nv.destroy(&prog);
+    return ok;
+}
+
+int effective_mode(int32_t mode) {
+    if (mode == CK_LDPC_SPECIALISE_AUTO) {
+        const char* env = getenv("COMMKIT_GB300_SPECIALISE");
+        if (env && env[0] == '0') return CK_LDPC_SPECIALISE_OFF;
+    }
+    return mode;
+}
+
+// Mixed kernels compiled so far, by (degree bound, plan ids and whether each
+// code is specialised).
+struct MixedJit {
+    cudaLibrary_t lib = nullptr;
+    const void* kernel = nullptr;
+    std::string why;
+};
+std::mutex g_mixed_mu;
+std::map<std::vector<uint64_t>, MixedJit> g_mixed;
+
+}  // namespace
+
+std::string specialised_source(const ck_ldpc_plan& plan, int dmax) { return program_source(plan, dmax); }
+
+std::string mixed_source(const ck_ldpc_plan* const* plans, const bool* special, int n, int dmax) {
+    return mixed_program_source(plans, special, n, dmax);
+}
+
+int specialised_kernel(const ck_ldpc_plan* plan, int dmax, bool r_smem, const void** out) {
+    *out = nullptr;
+    const int mode = effective_mode(plan->jit_mode);
+    if (mode == CK_LDPC_SPECIALISE_OFF) return CK_OK;
+    std::lock_guard<std::mutex> lock(plan->jit_mu);
+    ck_ldpc_plan::Jit& j = plan->jit;
+    if (!j.tried) {  // a plan's degree bound never changes, so one compilation serves it
+        j.tried = true;
+        j.dmax = dmax;
+        static const char* const names[] = {"ck_ldpc_code_r0", "ck_ldpc_code_r1"};
+        if (!compile_load(program_source(*plan, dmax), plan->device, names, 2, &j.lib, j.kernel, &j.why))
+            j.lib = nullptr;
+    }
+    if (!j.lib) {
+        if (mode == CK_LDPC_SPECIALISE_ON)
+            return ck::fail(CK_ERR_UNSUPPORTED, "code-specialised decoder unavailable: %s", j.why.c_str());
+        return CK_OK;
+    }
+    *out = j.kernel[r_smem ? 1 : 0];
+    return CK_OK;
+}
+
+int mixed_specialised_kernel(const ck_ldpc_plan* const* plans, const int32_t* T, int n, int dmax,
+                             const void** out) {
+    *out = nullptr;
+    bool special[8] = {};
+    bool any = false, required = false;
+    std::vector<uint64_t> key{static_cast<uint64_t>(dmax)};
+    for (int c = 0; c < n; ++c) {
+        const int mode = effective_mode(plans[c]->jit_mode);
+        if (mode == CK_LDPC_SPECIALISE_OFF) return CK_OK;  // any code opting out keeps the table kernel
+        required |= mode == CK_LDPC_SPECIALISE_ON;
+        special[c] = T[c] == (plans[c]->Z + 31) / 32 * 32;
+        any |= special[c];
+        key.push_back(plans[c]->id);
+        key.push_back(special[c] ? 1u : 0u);
+    }
+    if (!any) return CK_OK;
+    std::lock_guard<std::mutex> lock(g_mixed_mu);
+    auto it = g_mixed.find(key);
+    if (it == g_mixed.end()) {
+        MixedJit mj;
+        static const char* const names[] = {"ck_ldpc_mixed_code"};
+        const void* k = nullptr;
+        const int dev = plans[0]->device;
+        if (compile_load(mixed_program_source(plans, special, n, dmax), dev, names, 1, &mj.lib, &k, &mj.why))
+            mj.kernel = k;
+        it = g_mixed.emplace(key, std::move(mj)).first;
+    }
+    if (!it->second.kernel) {
+        if (required)
+            return ck::fail(CK_ERR_UNSUPPORTED, "code-specialised mixed decoder unavailable: %s",
+                            it->second.why.c_str());
+        return CK_OK;
+    }
+    *out = it->second.kernel;
+    return CK_OK;
+}
+
+void forget_plan_kernels(const ck_ldpc_plan* plan) {
+    std::lock_guard<std::mutex> lock(g_mixed_mu);
+    for (auto it = g_mixed.begin(); it != g_mixed.end();) {
+        bool uses = false;
+        for (size_t i = 1; i + 1 < it->first.size(); i += 2) uses |= it->first[i] == plan->id;
+        if (!uses) {
+            ++it;
+            continue;
+        }
+        if (it->second.lib) {
+            ck::forget_kernel(it->second.kernel);
+            (void)cudaLibraryUnload(it->second.lib);
+        }
+        it = g_mixed.erase(it);
+    }
+    if (plan->jit.lib) {
+        ck::forget_kernel(plan->jit.kernel[0]);
+        ck::forget_kernel(plan->jit.kernel[1]);
+        (void)cudaLibraryUnload(plan->jit.lib);
+    }
+}
+
+}  // namespace ldpc
+}  // namespace ck

@@ -1,0 +1,266 @@
+// The min-sum check rule of the layered decoder: the row updates (CSR and
+// circulant) and the compressed check-message state, for decode_kernel
+// (ck_ldpc_kernel.cuh), the mixed-code kernel and the code-specialised
+// kernels compiled at run time (ck_ldpc_jit.cu).  Compiles under NVRTC.
+#pragma once
+
+#include "ck_ldpc_kernel.cuh"
+
+namespace ck {
+namespace ldpc {
+
+
+// One check row, min-sum: reads the row's compressed state (m1, m2, w),
+// updates the posterior `a` of its deg variables (columns from col_of) and
+// writes the new state back.  Two passes as the reference's min_sum_row
+// (commkit/_cuda/src/ldpc.cu:45-72), with Q kept in registers between them
+// (columns are recomputed in the second pass rather than held).
+template <int DMAX, class ColOf>
+__device__ __forceinline__ void min_sum_row(float* __restrict__ a, const int deg,
+                                            const ColOf& col_of, float& m1, float& m2,
+                                            uint32_t& w, const float scale,
+                                            const float offset) {
+    const uint32_t oidx = w >> 27;
+    const uint32_t osign = w;
+    const float om1 = m1, om2 = m2;
+    float q[DMAX];
+    float min1 = ck::inf_f(), min2 = ck::inf_f();
+    uint32_t idx = 31u;  // no edge; matches the reference's -1 when every |Q| is inf
+    uint32_t negs = 0u;
+#pragma unroll
+    for (int e = 0; e < DMAX; ++e) {
+        if (e < deg) {
+            const float r_old =
+                flip_sign(static_cast<uint32_t>(e) == oidx ? om2 : om1, (osign >> e) & 1u);
+            const float qe = __fsub_rn(a[col_of(e)], r_old);
+            q[e] = qe;
+            negs |= (qe < 0.0f ? 1u : 0u) << e;
+            const float mag = fabsf(qe);
+            if (mag < min1) idx = static_cast<uint32_t>(e);
+            min2 = fminf(min2, fmax_nan(min1, mag));
+            min1 = fminf(min1, mag);
+        }
+    }
+    const float n1 = fmaxf(__fsub_rn(__fmul_rn(scale, min1), offset), 0.0f);
+    const float n2 = fmaxf(__fsub_rn(__fmul_rn(scale, min2), offset), 0.0f);
+    // Sign of edge e's new message: the parity of all signs times its own.
+    const uint32_t signs = negs ^ ((__popc(negs) & 1u) ? 0xffffffffu : 0u);
+#pragma unroll
+    for (int e = 0; e < DMAX; ++e) {
+        if (e < deg) {
+            const float rn = flip_sign(static_cast<uint32_t>(e) == idx ? n2 : n1, (signs >> e) & 1u);
+            a[col_of(e)] = __fadd_rn(q[e], rn);
+        }
+    }
+    m1 = n1;
+    m2 = n2;
+    w = (signs & 0x07ffffffu) | (idx << 27);
+}
+
+// The same update for a circulant row of exactly D edges, shaped for the
+// ALU pipe, which bounds this kernel: fully unrolled, columns computed once
+// and kept in registers,
+//  * min1/min2 taken over pairs of edges: with lo/hi the pair's smaller and
+//    larger magnitude, min2 = min(min2, hi, max(min1, lo)) and min1 =
+//    min(min1, lo), five operations per pair instead of six (three-input
+//    min), and half as long a dependency chain; a NaN magnitude (only from
+//    infinite input LLRs) drops out of both, as in the reference,
+//  * the sign bits of Q taken from the float sign (no -0 ever reaches the
+//    posterior: frames are loaded as x + 0, and from such values Q = APP - R
+//    and APP = Q + R_new cannot produce -0 either, so "sign bit set" is
+//    "Q < 0"), one funnel shift per edge;
+//  * the new signs applied with one multiply by the parity sign (exact) and
+//    one bitwise or;
+//  * no running argmin: an edge takes min2' when |Q| equals min1 (a tie
+//    means min2 == min1, so every tied edge gets the same value), and the
+//    stored argmin is the first such edge, found in the second pass.
+// The compressed state keeps the sign of edge e at bit D - 1 - e here.
+// The row's columns come as shared-memory addresses c[0..D).
+template <int D>
+__device__ __forceinline__ void qc_row_cols(const uint32_t (&c)[D], float& m1, float& m2, uint32_t& w,
+                                            const float scale, const float offset) {
+    const uint32_t oidx = w >> 27;
+    const uint32_t osign = w;
+    const float om1 = m1, om2 = m2;
+    float q[D];
+    float min1 = ck::inf_f(), min2 = ck::inf_f();
+    uint32_t negs = 0u;
+#pragma unroll
+    for (int e = 0; e < D; ++e) {
+        const uint32_t ce = c[e];
+        const float mag_old = static_cast<uint32_t>(e) == oidx ? om2 : om1;
+        const float r_old = __uint_as_float(__float_as_uint(mag_old) ^
+                                            ((osign << (32 - D + e)) & 0x80000000u));
+        const float qe = __fsub_rn(ld_shared_f32(ce), r_old);
+        q[e] = qe;
+        negs = __funnelshift_l(__float_as_uint(qe), negs, 1);
+        if (e & 1) {
+            const float x = fabsf(q[e - 1]), y = fabsf(qe);
+            const float hi = fmax_nan(x, y);
+            if (e == 1) {
+                min1 = fmin3(x, y, ck::inf_f());
+                min2 = fminf(hi, ck::inf_f());
+            } else {
+                const float lo = fminf(x, y);
+                min2 = fmin3(min2, hi, fmax_nan(min1, lo));
+                min1 = fminf(min1, lo);
+            }
+        } else if (e == D - 1) {
+            const float mag = fabsf(qe);
+            min2 = fminf(min2, fmax_nan(min1, mag));
+            min1 = fminf(min1, mag);
+        }
+    }
+    const float n1 = fmaxf(__fsub_rn(__fmul_rn(scale, min1), offset), 0.0f);
+    const float n2 = fmaxf(__fsub_rn(__fmul_rn(scale, min2), offset), 0.0f);
+    const bool odd = __popc(negs) & 1u;
+    const float psign = odd ? -1.0f : 1.0f;
+    uint32_t idx = 31u;
+#pragma unroll
+    for (int e = D - 1; e >= 0; --e) {
+        const bool at_min = fabsf(q[e]) == min1;
+        if (at_min) idx = static_cast<uint32_t>(e);
+        const float mag = at_min ? n2 : n1;
+        const float t = __fmul_rn(q[e], psign);
+        const float rn = __uint_as_float(__float_as_uint(mag) | (__float_as_uint(t) & 0x80000000u));
+        st_shared_f32(c[e], __fadd_rn(q[e], rn));
+    }
+    const uint32_t signs = negs ^ (odd ? ((1u << D) - 1u) : 0u);
+    m1 = n1;
+    m2 = n2;
+    w = (signs & 0x07ffffffu) | (idx << 27);
+}
+
+// Row r of a circulant base row: gblk[e] = (shared address of circulant
+// e's row-0 column, address of its block's end), r4 = 4 r, Z4 = 4 Z; row
+// r's column is r4 + gblk[e].x, wrapped back by Z4 once it reaches the end.
+template <int D>
+__device__ __forceinline__ void qc_row_fixed(const int2* __restrict__ gblk, const uint32_t r4,
+                                             const uint32_t Z4, float& m1, float& m2, uint32_t& w,
+                                             const float scale, const float offset) {
+    uint32_t c[D];
+#pragma unroll
+    for (int e = 0; e < D; ++e) {
+        const int2 b = gblk[e];
+        const uint32_t ce = r4 + static_cast<uint32_t>(b.x);
+        c[e] = ce >= static_cast<uint32_t>(b.y) ? ce - Z4 : ce;
+    }
+    qc_row_cols<D>(c, m1, m2, w, scale, offset);
+}
+
+// Degree dispatch of a circulant row (warp-uniform): D = 2..DMAX unrolled,
+// with no case above DMAX (a switch over 2..16 rather than 2..27 for the
+// DMAX = 16 kernels).
+#define CK_ROW_CASE(D) \
+    case D:            \
+        qc_row_fixed<D>(gblk, r4, Z4, m1, m2, w, scale, offset); \
+        break;
+template <int DMAX>
+__device__ __forceinline__ void qc_row(const int2* __restrict__ gblk, const int deg,
+                                       const uint32_t r4, const uint32_t Z4, float& m1, float& m2,
+                                       uint32_t& w, const float scale, const float offset) {
+    if constexpr (DMAX <= 16) {
+        switch (deg) {
+            CK_ROW_CASE(2) CK_ROW_CASE(3) CK_ROW_CASE(4) CK_ROW_CASE(5) CK_ROW_CASE(6)
+            CK_ROW_CASE(7) CK_ROW_CASE(8) CK_ROW_CASE(9) CK_ROW_CASE(10) CK_ROW_CASE(11)
+            CK_ROW_CASE(12) CK_ROW_CASE(13) CK_ROW_CASE(14) CK_ROW_CASE(15) CK_ROW_CASE(16)
+            default:
+                break;
+        }
+    } else {
+        switch (deg) {
+            CK_ROW_CASE(2) CK_ROW_CASE(3) CK_ROW_CASE(4) CK_ROW_CASE(5) CK_ROW_CASE(6)
+            CK_ROW_CASE(7) CK_ROW_CASE(8) CK_ROW_CASE(9) CK_ROW_CASE(10) CK_ROW_CASE(11)
+            CK_ROW_CASE(12) CK_ROW_CASE(13) CK_ROW_CASE(14) CK_ROW_CASE(15) CK_ROW_CASE(16)
+            CK_ROW_CASE(17) CK_ROW_CASE(18) CK_ROW_CASE(19) CK_ROW_CASE(20) CK_ROW_CASE(21)
+            CK_ROW_CASE(22) CK_ROW_CASE(23) CK_ROW_CASE(24) CK_ROW_CASE(25) CK_ROW_CASE(26)
+            CK_ROW_CASE(27)
+            default:
+                break;
+        }
+    }
+}
+#undef CK_ROW_CASE
+
+// Min-sum check-message state of a frame slot: per row (min1', min2', one
+// word of signs and argmin).  In shared memory one 16-byte record per row
+// (one vector access); in device memory 12 bytes, an array of (min1',
+// min2') pairs and one of words (two accesses), so the resident frames'
+// state (code C: 304 frames x 17664 rows x 12 B = 64 MB) stays in L2.  (A
+// 16-byte record there measured 17 % slower on code C: 86 MB of state
+// leaves too little of L2 to the rest.)
+template <bool R_SMEM>
+struct MinSumState {
+    uint4* rs;
+    uint2* g12;
+    uint32_t* g3;
+
+    __device__ __forceinline__ MinSumState(const Params& p, unsigned char* gbase, uint32_t slot)
+        : MinSumState(reinterpret_cast<uint4*>(gbase + p.r_off), p.g_r, slot, p.r_stride) {}
+    // rs: the group's records in shared memory; g_r: the device-memory
+    // state slots (3 r_stride words each), slot: this group's.
+    __device__ __forceinline__ MinSumState(uint4* rs_, uint32_t* g_r, uint32_t slot, uint32_t r_stride)
+        : rs(rs_),
+          g12(reinterpret_cast<uint2*>(g_r + static_cast<size_t>(slot) * 3 * r_stride)),
+          g3(g_r + static_cast<size_t>(slot) * 3 * r_stride + 2 * r_stride) {}
+
+    __device__ __forceinline__ void zero(const Params& p, int first, int stride) const {
+        zero_rows(p.m, first, stride);
+    }
+    __device__ __forceinline__ void zero_rows(int32_t m, int first, int stride) const {
+        for (int i = first; i < m; i += stride) {
+            if (R_SMEM) {
+                rs[i] = make_uint4(0u, 0u, 0u, 0u);
+            } else {
+                g12[i] = make_uint2(0u, 0u);
+                g3[i] = 0u;
+            }
+        }
+    }
+    __device__ __forceinline__ uint4 load(uint32_t row) const {
+        if (R_SMEM) return rs[row];
+        const uint2 m = __ldcg(g12 + row);
+        return make_uint4(m.x, m.y, __ldcg(g3 + row), 0u);
+    }
+    __device__ __forceinline__ void store(uint32_t row, float m1, float m2, uint32_t w) const {
+        if (R_SMEM) {
+            rs[row] = make_uint4(__float_as_uint(m1), __float_as_uint(m2), w, 0u);
+        } else {
+            __stcg(g12 + row, make_uint2(__float_as_uint(m1), __float_as_uint(m2)));
+            __stcg(g3 + row, w);
+        }
+    }
+    template <int DMAX>
+    __device__ __forceinline__ void qc_row(const Params& p, const int2* gblk, int deg, uint32_t row,
+                                           int32_t, int32_t, uint32_t r4, uint32_t Z4) const {
+        const uint4 s = load(row);
+        float m1 = __uint_as_float(s.x), m2 = __uint_as_float(s.y);
+        uint32_t w = s.z;
+        ck::ldpc::qc_row<DMAX>(gblk, deg, r4, Z4, m1, m2, w, p.scale, p.offset);
+        store(row, m1, m2, w);
+    }
+    // One circulant row with its columns computed by the caller (the
+    // code-specialised programs).
+    template <int D>
+    __device__ __forceinline__ void row_cols(const uint32_t (&c)[D], uint32_t row, float scale,
+                                             float offset) const {
+        const uint4 s = load(row);
+        float m1 = __uint_as_float(s.x), m2 = __uint_as_float(s.y);
+        uint32_t w = s.z;
+        qc_row_cols<D>(c, m1, m2, w, scale, offset);
+        store(row, m1, m2, w);
+    }
+    template <int DMAX, class ColOf>
+    __device__ __forceinline__ void csr_row(const Params& p, float* a, uint32_t row, int deg, int32_t,
+                                            const ColOf& col_of) const {
+        const uint4 s = load(row);
+        float m1 = __uint_as_float(s.x), m2 = __uint_as_float(s.y);
+        uint32_t w = s.z;
+        min_sum_row<DMAX>(a, deg, col_of, m1, m2, w, p.scale, p.offset);
+        store(row, m1, m2, w);
+    }
+};
+
+
+}  // namespace ldpc
+}  // namespace ck

@@ -1,0 +1,244 @@
+// The mixed-code persistent decoder (min-sum, circulant codes): frames of
+// several codes in one launch.  Also an NVRTC source: code-specialised
+// mixed kernels (ck_ldpc_jit.cu) instantiate mixed_body with a dispatch to
+// each code's generated program.
+#pragma once
+
+#include "ck_ldpc_minsum.cuh"
+
+namespace ck {
+namespace ldpc {
+
+// ---------------------------------------------------------------------------
+// Mixed-code persistent kernel: frames of several quasi-cyclic codes in one
+// launch.  Every block can host any code's frame groups (its shared memory
+// and threads are sized for the largest); it starts on a code chosen in
+// proportion to the work and, once that code's queue is empty, switches to
+// the code with the most work left.  The frame loop is the plain kernel's:
+// same rows, same order, same bits.
+// ---------------------------------------------------------------------------
+
+constexpr int kMaxMixed = 4;  // CK_LDPC_MAX_MIXED
+constexpr int kMixedThreads = 768;
+
+struct MixedCode {
+    const int32_t* layer;
+    const int32_t* eptr;
+    const int2* blk;
+    int32_t N, m, L, Z, Zp, mb, nnzb;
+    const float* llr_in;
+    float* llr_out;
+    uint32_t B;
+    int32_t n_in;
+    int32_t* iters;
+    uint8_t* valid;
+    int8_t* bits;
+    int32_t k_bits;
+    const int32_t* order;  // queue position -> frame, or null
+    float scale, offset;
+    int32_t max_iterations, early_stop;
+    int32_t T, G, q_bstep, r_smem;
+    uint32_t tables_bytes, group_bytes, gblk_off, app_off, r_off, r_stride;
+    uint32_t* g_r;
+    uint32_t* counter;
+    float weight;  // edges per frame
+};
+
+struct MixedParams {
+    MixedCode code[kMaxMixed];
+    int32_t num_codes;
+    int32_t start_block[kMaxMixed + 1];  // blocks [start_block[c], start_block[c+1]) begin on c
+};
+
+// The code this block should work on next: `prefer` while its queue has
+// frames, else the one with the most edges left; -1 when all are drained.
+__device__ inline int mixed_pick(const MixedParams& p, int prefer) {
+    if (prefer >= 0) {
+        const uint32_t taken = *reinterpret_cast<volatile uint32_t*>(p.code[prefer].counter);
+        if (taken < p.code[prefer].B) return prefer;
+    }
+    int best = -1;
+    float most = 0.0f;
+    for (int c = 0; c < p.num_codes; ++c) {
+        const uint32_t taken = *reinterpret_cast<volatile uint32_t*>(p.code[c].counter);
+        if (taken >= p.code[c].B) continue;
+        const float left = static_cast<float>(p.code[c].B - taken) * p.code[c].weight;
+        if (best < 0 || left > most) {
+            best = c;
+            most = left;
+        }
+    }
+    return best;
+}
+
+// Decodes frames of code K with group g until K's queue is empty (ONE_ROW:
+// K.T >= K.Zp, one row per visited base row, as in decode_body; Prog: the
+// table-driven layer loop or the code's specialised program).
+template <int DMAX, bool R_SMEM, bool ONE_ROW, class Prog>
+__device__ __forceinline__ void mixed_frames(const MixedCode& K, unsigned char* smem, const int32_t* s_layer,
+                             const int32_t* s_eptr, const int2* s_blk, const int g,
+                             const int tid) {
+    using ck::group_any;
+    using ck::group_sync;
+    const int bar = g + 1;
+    unsigned char* gbase = smem + K.tables_bytes + static_cast<uint32_t>(g) * K.group_bytes;
+    volatile uint32_t* s_frame = reinterpret_cast<volatile uint32_t*>(gbase + 8);
+    float* a = reinterpret_cast<float*>(gbase + K.app_off);
+    const uint32_t slot = blockIdx.x * static_cast<uint32_t>(K.G) + static_cast<uint32_t>(g);
+    const MinSumState<R_SMEM> st(reinterpret_cast<uint4*>(gbase + K.r_off), K.g_r, slot, K.r_stride);
+    int2* gblk = reinterpret_cast<int2*>(gbase + K.gblk_off);
+    const uint32_t a_addr = ck::smem_addr(a);
+    for (int i = tid; i < K.nnzb; i += K.T)
+        gblk[i] = make_int2(static_cast<int>(a_addr + 4u * static_cast<uint32_t>(s_blk[i].x)),
+                            static_cast<int>(a_addr + 4u * static_cast<uint32_t>(s_blk[i].y)));
+    const int32_t qr0 = K.T >= K.Zp ? tid % K.Zp : tid;
+    const int32_t qb0 = K.T >= K.Zp ? tid / K.Zp : 0;
+    const uint32_t r4 = 4u * static_cast<uint32_t>(qr0);
+    const uint32_t Z4 = 4u * static_cast<uint32_t>(K.Z);
+
+    auto syndrome_ok = [&]() -> bool {
+        const int32_t rounds = (K.mb + K.q_bstep - 1) / K.q_bstep;
+        for (int32_t k = 0; k < rounds; ++k) {
+            const int32_t b = k * K.q_bstep + qb0;
+            for (int32_t r = qr0; r - qr0 < K.Zp; r += K.T) {
+                uint32_t parity = 0;
+                if (b < K.mb && r < K.Z) {
+                    const int32_t e0 = s_eptr[b];
+                    const int deg = s_eptr[b + 1] - e0;
+                    const QcCols col_of{s_blk + e0, r, K.Z};
+                    for (int e = 0; e < deg; ++e) parity ^= a[col_of(e)] < 0.0f ? 1u : 0u;
+                }
+                if (group_any(static_cast<int>(parity), bar, K.T)) return false;
+            }
+        }
+        return true;
+    };
+
+    for (;;) {
+        if (tid == 0) *s_frame = atomicAdd(K.counter, 1u);
+        group_sync(bar, K.T);
+        const uint32_t pos = *s_frame;
+        if (pos >= K.B) break;
+        const uint32_t f = K.order ? static_cast<uint32_t>(__ldg(K.order + pos)) : pos;
+        const float* src = K.llr_in + static_cast<size_t>(f) * K.n_in;
+        for (int i = tid; i < K.n_in; i += K.T) a[i] = __fadd_rn(__ldcs(src + i), 0.0f);
+        for (int i = K.n_in + tid; i < K.N; i += K.T) a[i] = 0.0f;
+        st.zero_rows(K.m, tid, K.T);
+        group_sync(bar, K.T);
+        int32_t it = 0;
+        bool ok = K.early_stop && syndrome_ok();
+        while (!ok && it < K.max_iterations) {
+            // One check row: row r of base row b (circulants e0 .. e0 + deg).
+            auto do_row = [&](int32_t b, int32_t e0, int deg, int32_t r) {
+                const uint32_t row = static_cast<uint32_t>(b) * static_cast<uint32_t>(K.Z) +
+                                     static_cast<uint32_t>(r);
+                const uint4 s = st.load(row);
+                float m1 = __uint_as_float(s.x), m2 = __uint_as_float(s.y);
+                uint32_t w = s.z;
+                qc_row<DMAX>(gblk + e0, deg, r4 + 4u * static_cast<uint32_t>(r - qr0), Z4, m1, m2, w,
+                             K.scale, K.offset);
+                st.store(row, m1, m2, w);
+            };
+            if constexpr (Prog::kSpecialised)
+                Prog::iteration(st, a_addr + r4, static_cast<uint32_t>(qr0), K.scale, K.offset, bar, K.T);
+            for (int32_t l = 0; l < K.L && !Prog::kSpecialised; ++l) {
+                const int32_t b1 = s_layer[l + 1];
+                if (!ONE_ROW || qr0 < K.Z) {
+                    for (int32_t b = s_layer[l] + qb0; b < b1; b += K.q_bstep) {
+                        const int32_t e0 = s_eptr[b];
+                        const int deg = s_eptr[b + 1] - e0;
+                        if (ONE_ROW) {
+                            do_row(b, e0, deg, qr0);
+                        } else {
+                            for (int32_t r = qr0; r - qr0 < K.Zp; r += K.T)
+                                if (r < K.Z) do_row(b, e0, deg, r);
+                        }
+                    }
+                }
+                group_sync(bar, K.T);
+            }
+            ++it;
+            if (K.early_stop) ok = syndrome_ok();
+        }
+        if (!K.early_stop) ok = syndrome_ok();
+        float* dst = K.llr_out + static_cast<size_t>(f) * K.n_in;
+        for (int i = tid; i < K.n_in; i += K.T) __stcs(dst + i, a[i]);
+        if (K.bits) {
+            int8_t* bdst = K.bits + static_cast<size_t>(f) * K.k_bits;
+            for (int i = tid; i < K.k_bits; i += K.T) bdst[i] = a[i] < 0.0f ? 1 : 0;
+        }
+        // The iteration count is written last, after a system-scope fence
+        // that follows the group's writes: a host that reads it from mapped
+        // memory (the request server polls frames as they finish) then also
+        // sees the frame's LLRs, bits and flag.
+        group_sync(bar, K.T);
+        if (tid == 0) {
+            K.valid[f] = ok ? 1 : 0;
+            __threadfence_system();
+            K.iters[f] = it;
+        }
+        group_sync(bar, K.T);
+    }
+}
+
+// The table-driven frame loops of every code.
+struct TableDispatch {
+    template <int DMAX>
+    __device__ __forceinline__ static void run(int, const MixedCode& K, unsigned char* smem,
+                                               const int32_t* s_layer, const int32_t* s_eptr,
+                                               const int2* s_blk, int g, int tid) {
+        const bool one_row = K.T >= K.Zp;
+        if (K.r_smem && one_row)
+            mixed_frames<DMAX, true, true, TableProgram>(K, smem, s_layer, s_eptr, s_blk, g, tid);
+        else if (K.r_smem)
+            mixed_frames<DMAX, true, false, TableProgram>(K, smem, s_layer, s_eptr, s_blk, g, tid);
+        else if (one_row)
+            mixed_frames<DMAX, false, true, TableProgram>(K, smem, s_layer, s_eptr, s_blk, g, tid);
+        else
+            mixed_frames<DMAX, false, false, TableProgram>(K, smem, s_layer, s_eptr, s_blk, g, tid);
+    }
+};
+
+// The kernel body: blocks take codes as mixed_pick says; Dispatch::run<DMAX>
+// (code index, code, ...) runs a group's frames of that code (TableDispatch,
+// or a generated dispatch to each code's specialised program).
+template <int DMAX, class Dispatch>
+__device__ __forceinline__ void mixed_body(const MixedParams& p) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ int s_code;
+    if (threadIdx.x == 0) {
+        int c = 0;
+        while (c + 1 < p.num_codes && static_cast<int32_t>(blockIdx.x) >= p.start_block[c + 1]) ++c;
+        s_code = mixed_pick(p, c);
+    }
+    __syncthreads();
+    for (;;) {
+        const int c = s_code;
+        if (c < 0) break;
+        const MixedCode& K = p.code[c];
+        int32_t* s_layer = reinterpret_cast<int32_t*>(smem);
+        int32_t* s_eptr = s_layer + (K.L + 1);
+        int2* s_blk = reinterpret_cast<int2*>(
+            smem + ((static_cast<uint32_t>(K.L + 1 + K.mb + 1) * 4 + 7) & ~7u));
+        for (int i = threadIdx.x; i <= K.L; i += blockDim.x) s_layer[i] = K.layer[i];
+        for (int i = threadIdx.x; i <= K.mb; i += blockDim.x) s_eptr[i] = K.eptr[i];
+        for (int i = threadIdx.x; i < K.nnzb; i += blockDim.x) s_blk[i] = K.blk[i];
+        __syncthreads();
+        const int g = threadIdx.x / K.T;
+        if (g < K.G) {
+            const int tid = threadIdx.x - g * K.T;
+            Dispatch::template run<DMAX>(c, K, smem, s_layer, s_eptr, s_blk, g, tid);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_code = mixed_pick(p, -1);
+        __syncthreads();
+    }
+}
+
+template <int DMAX>
+__global__ void __launch_bounds__(kMixedThreads) ldpc_mixed_kernel(const __grid_constant__ MixedParams p) {
+    mixed_body<DMAX, TableDispatch>(p);
+}
+
+}  // namespace ldpc
+}  // namespace ck

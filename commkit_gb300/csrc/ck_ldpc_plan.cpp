@@ -5,6 +5,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <numeric>
 #include <vector>
 
@@ -161,12 +162,12 @@ int upload(const std::vector<int32_t>& h, int32_t** d) {
 
 }  // namespace
 
-extern "C" int ck_ldpc_plan_create(const int32_t* row_ptr, const int32_t* cols,
-                                   const int32_t* layer_ptr, int32_t m, int32_t N, int32_t L,
-                                   ck_ldpc_plan** out) {
-    ck::clear_error();
-    if (!out) return ck::fail(CK_ERR_INVALID_ARGUMENT, "plan is NULL");
-    *out = nullptr;
+namespace {
+
+// Checks a schedule and fills the host side of `plan` (sizes, degree bound,
+// circulant structure); touches no device.
+int plan_host(const int32_t* row_ptr, const int32_t* cols, const int32_t* layer_ptr, int32_t m, int32_t N,
+              int32_t L, ck_ldpc_plan* plan) {
     if (!row_ptr || !cols || !layer_ptr)
         return ck::fail(CK_ERR_INVALID_ARGUMENT, "row_ptr, cols and layer_ptr are required");
     if (m < 1 || N < 1 || L < 1)
@@ -212,8 +213,6 @@ extern "C" int ck_ldpc_plan_create(const int32_t* row_ptr, const int32_t* cols,
         return ck::fail(CK_ERR_UNSUPPORTED, "row degree %d above the decoder's limit of %d",
                         max_deg, ck::kMaxRowDegree);
 
-    ck_ldpc_plan* plan = new ck_ldpc_plan();
-    CK_CUDA(cudaGetDevice(&plan->device));
     plan->m = m;
     plan->N = N;
     plan->E = E;
@@ -234,14 +233,33 @@ extern "C" int ck_ldpc_plan_create(const int32_t* row_ptr, const int32_t* cols,
         try_qc(row_ptr, cols, layer_ptr, m, N, L, Z, plan);
     }
     if (plan->qc && plan->nnzb > ck::kMaxBlocks) plan->qc = false;
-    int status = CK_OK;
+    return CK_OK;
+}
+
+}  // namespace
+
+extern "C" int ck_ldpc_plan_create(const int32_t* row_ptr, const int32_t* cols,
+                                   const int32_t* layer_ptr, int32_t m, int32_t N, int32_t L,
+                                   ck_ldpc_plan** out) {
+    ck::clear_error();
+    if (!out) return ck::fail(CK_ERR_INVALID_ARGUMENT, "plan is NULL");
+    *out = nullptr;
+    static std::atomic<uint64_t> next_id{1};
+    ck_ldpc_plan* plan = new ck_ldpc_plan();
+    plan->id = next_id.fetch_add(1);
+    int status = plan_host(row_ptr, cols, layer_ptr, m, N, L, plan);
+    if (status == CK_OK) status = ck::cuda_check(cudaGetDevice(&plan->device), "cudaGetDevice");
+    if (status != CK_OK) {
+        delete plan;
+        return status;
+    }
     if (plan->qc) {
         status = upload(plan->h_layer, &plan->d_layer);
         if (status == CK_OK) status = upload(plan->h_eptr, &plan->d_eptr);
         if (status == CK_OK) status = upload(plan->h_blk, &plan->d_blk);
     } else {
         plan->h_layer.assign(layer_ptr, layer_ptr + L + 1);
-        std::vector<int32_t> rp(row_ptr, row_ptr + m + 1), cc(cols, cols + E);
+        std::vector<int32_t> rp(row_ptr, row_ptr + m + 1), cc(cols, cols + plan->E);
         status = upload(plan->h_layer, &plan->d_layer);
         if (status == CK_OK) status = upload(rp, &plan->d_eptr);
         if (status == CK_OK) status = upload(cc, &plan->d_cols);
@@ -255,6 +273,29 @@ extern "C" int ck_ldpc_plan_create(const int32_t* row_ptr, const int32_t* cols,
     return CK_OK;
 }
 
+extern "C" int ck_ldpc_specialised_source(const int32_t* row_ptr, const int32_t* cols,
+                                          const int32_t* layer_ptr, int32_t m, int32_t N, int32_t L,
+                                          int32_t form, char* out, size_t capacity, size_t* length) {
+    ck::clear_error();
+    if (!length) return ck::fail(CK_ERR_INVALID_ARGUMENT, "length is NULL");
+    if (form != 0 && form != 1) return ck::fail(CK_ERR_INVALID_ARGUMENT, "form must be 0 or 1");
+    ck_ldpc_plan plan;
+    CK_TRY(plan_host(row_ptr, cols, layer_ptr, m, N, L, &plan));
+    if (!plan.qc) return ck::fail(CK_ERR_UNSUPPORTED, "the schedule has no circulant structure");
+    const int dmax = plan.max_deg <= 16 ? 16 : 27;
+    const ck_ldpc_plan* plans[1] = {&plan};
+    const bool special[1] = {true};
+    const std::string src =
+        form == 0 ? ck::ldpc::specialised_source(plan, dmax) : ck::ldpc::mixed_source(plans, special, 1, dmax);
+    *length = src.size();
+    if (out && capacity > 0) {
+        const size_t n = std::min(capacity - 1, src.size());
+        memcpy(out, src.data(), n);
+        out[n] = '\0';
+    }
+    return CK_OK;
+}
+
 extern "C" int ck_ldpc_plan_destroy(ck_ldpc_plan* plan) {
     if (!plan) return CK_OK;
     int dev = -1;
@@ -264,6 +305,7 @@ extern "C" int ck_ldpc_plan_destroy(ck_ldpc_plan* plan) {
     if (plan->d_eptr) (void)cudaFree(plan->d_eptr);
     if (plan->d_blk) (void)cudaFree(plan->d_blk);
     if (plan->d_cols) (void)cudaFree(plan->d_cols);
+    ck::ldpc::forget_plan_kernels(plan);
     if (dev >= 0 && dev != plan->device) (void)cudaSetDevice(dev);
     delete plan;
     return CK_OK;
@@ -299,6 +341,25 @@ extern "C" int ck_ldpc_plan_set_launch(ck_ldpc_plan* plan, const ck_ldpc_launch*
                         "at most %d multi-warp frames per block (named barriers)",
                         ck::kMaxNamedGroups);
     plan->launch = *launch;
+    return CK_OK;
+}
+
+extern "C" int ck_ldpc_plan_set_specialise(ck_ldpc_plan* plan, int32_t mode) {
+    ck::clear_error();
+    if (!plan) return ck::fail(CK_ERR_INVALID_ARGUMENT, "NULL plan");
+    if (mode != CK_LDPC_SPECIALISE_AUTO && mode != CK_LDPC_SPECIALISE_OFF && mode != CK_LDPC_SPECIALISE_ON)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "unknown specialisation mode %d", mode);
+    plan->jit_mode = mode;
+    return CK_OK;
+}
+
+extern "C" int ck_ldpc_plan_get_specialise(const ck_ldpc_plan* plan, int32_t* mode, int32_t* state) {
+    ck::clear_error();
+    if (!plan || !mode || !state) return ck::fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::lock_guard<std::mutex> lock(plan->jit_mu);
+    *mode = plan->jit_mode;
+    *state = !plan->jit.tried ? 0 : (plan->jit.lib ? 1 : -1);
+    if (*state < 0) (void)ck::fail(CK_ERR_UNSUPPORTED, "%s", plan->jit.why.c_str());
     return CK_OK;
 }
 

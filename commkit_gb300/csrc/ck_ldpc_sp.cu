@@ -20,6 +20,7 @@
 // logf and tanhf as the reference's kernel does.  Results therefore match
 // the CPU decoder up to the rounding of those two functions (the reference
 // tests its own GPU path against the CPU at 1e-3).
+#include "ck_ldpc_cluster.cuh"
 #include "ck_ldpc_kernel.cuh"
 
 namespace ck {

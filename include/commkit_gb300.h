@@ -298,6 +298,35 @@ typedef struct ck_ldpc_launch {
 int ck_ldpc_plan_set_launch(ck_ldpc_plan* plan, const ck_ldpc_launch* launch);
 int ck_ldpc_plan_get_launch(const ck_ldpc_plan* plan, ck_ldpc_launch* launch);
 
+/*
+ * Code-specialised min-sum decoding of a circulant code (no reference
+ * counterpart; results identical bit for bit).  On first use the plan
+ * generates a decoder kernel with the code's layers, degrees, block columns
+ * and shifts as constants and compiles it with NVRTC; min-sum decodes whose
+ * frame groups have one thread per row slot (threads per frame == Z rounded
+ * up to whole warps) then run it.  AUTO (the default) falls back to the
+ * table-driven kernel where NVRTC is missing or the environment sets
+ * COMMKIT_GB300_SPECIALISE=0; ON makes an unavailable specialisation an
+ * error; OFF always uses the table-driven kernel.  get_specialise reports
+ * the mode and the state: 0 not compiled yet, 1 compiled, -1 unavailable
+ * (ck_last_error() then says why).
+ */
+#define CK_LDPC_SPECIALISE_AUTO 0
+#define CK_LDPC_SPECIALISE_OFF 1
+#define CK_LDPC_SPECIALISE_ON 2
+int ck_ldpc_plan_set_specialise(ck_ldpc_plan* plan, int32_t mode);
+int ck_ldpc_plan_get_specialise(const ck_ldpc_plan* plan, int32_t* mode, int32_t* state);
+/*
+ * The CUDA source a plan of this schedule would compile for its
+ * code-specialised kernels (host only, no device needed): form 0 the plain
+ * decoder, form 1 a mixed decoder of this code alone.  *length gets its
+ * size, and up to capacity - 1 bytes of it go to `out` (NUL-terminated).
+ * CK_ERR_UNSUPPORTED when the schedule is not circulant.
+ */
+int ck_ldpc_specialised_source(const int32_t* row_ptr, const int32_t* cols, const int32_t* layer_ptr,
+                               int32_t m, int32_t N, int32_t L, int32_t form, char* out, size_t capacity,
+                               size_t* length);
+
 #define CK_LDPC_MIN_SUM 0
 #define CK_LDPC_SUM_PRODUCT 1
 

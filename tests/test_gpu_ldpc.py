@@ -94,6 +94,35 @@ def test_nonfinite_llrs(golden_ldpc, torch_dev, ck, which, early_stop):
     np.testing.assert_array_equal(post, nf[p + "_post"])
 
 
+@pytest.mark.parametrize("name,frames,order", [("A", 600, 4), ("B", 400, 16), ("C", 160, 16)])
+@pytest.mark.parametrize("placement", [1, 2])
+def test_specialised_kernel_equals_table_kernel(torch_dev, ck, name, frames, order, placement):
+    """The code-specialised kernel (compiled at run time) against the
+    table-driven kernel on the same frames, message state in shared (1;
+    code C's does not fit there and stays in device memory) or device (2)
+    memory: every output bit for bit; and against the oracle."""
+    from commkit_gb300 import _lib
+
+    torch, dev = torch_dev
+    spec = W.CODES[name]
+    zp = (spec.z + 31) // 32 * 32
+    codes = [_qc_code(ck, name), _qc_code(ck, name)]
+    for code, mode in zip(codes, (_lib.CK_LDPC_SPECIALISE_ON, _lib.CK_LDPC_SPECIALISE_OFF), strict=True):
+        plan = code._plan(0)
+        plan.set_specialise(mode)
+        plan.set_launch(zp, 0, placement)
+    batch = W.coded_batch(spec, frames, order, W.WATERFALL_DB[name] + 0.5, seed=21)
+    x = torch.from_numpy(batch.symbols).to(dev)
+    llr = ck.compute_llr_frames(x, constellation=ck.Constellation.qam(order), noise_var=batch.noise_var)
+    method = ck.MinSum(max_iterations=30)
+    got = [_to_np(ck.decode(llr, code=c, method=method), frames) for c in codes]
+    assert codes[0]._plan(0).specialisation()[1] == 1, codes[0]._plan(0).specialisation()
+    assert codes[1]._plan(0).specialisation()[1] == 0
+    _assert_same(got[0], got[1])
+    assert 0 < np.mean(got[0][3]) < 30  # frames stop at different iterations
+    _assert_same(got[0], _oracle(codes[0], llr.cpu().numpy(), max_iterations=30))
+
+
 @pytest.mark.parametrize("name", ["A", "B"])
 def test_golden_codes(golden_ldpc, torch_dev, ck, name):
     torch, dev = torch_dev

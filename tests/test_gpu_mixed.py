@@ -23,10 +23,15 @@ def _batch(ck, dev, name, frames, order, ebn0, seed):
 
 
 @pytest.mark.parametrize("placement", [0, 2])
-def test_mixed_launch_matches_plain_calls(placement):
+@pytest.mark.parametrize("specialise", ["table_plain", "both_auto"])
+def test_mixed_launch_matches_plain_calls(placement, specialise):
+    """table_plain: plain calls on the table-driven kernel, the mixed launch
+    on the code-specialised one (compiled at run time); both_auto: both
+    specialised."""
     import torch
 
     import commkit_gb300 as ck
+    from commkit_gb300 import _lib
 
     dev = torch.device("cuda", 0)
     cases = [("A", 700, 4, 1.5, ck.MinSum(max_iterations=20)),
@@ -36,8 +41,11 @@ def test_mixed_launch_matches_plain_calls(placement):
     for i, (name, frames, order, ebn0, method) in enumerate(cases):
         code, llr = _batch(ck, dev, name, frames, order, ebn0, seed=30 + i)
         code._plan(0).set_launch(0, 0, placement)
+        if specialise == "table_plain":
+            code._plan(0).set_specialise(_lib.CK_LDPC_SPECIALISE_OFF)
         batches.append((llr, code, method))
         plain.append(ck.decode(llr, code=code, method=method))
+        code._plan(0).set_specialise(_lib.CK_LDPC_SPECIALISE_AUTO)
     mixed = ck.decode_mixed(batches)
     for (llr, code, method), p, m in zip(batches, plain, mixed, strict=True):
         frames = llr.shape[0]
