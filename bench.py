@@ -76,12 +76,13 @@ WORKLOADS = {
 }  # fmt: skip
 
 
-# DRAM traffic of the mixed decoder, dram__bytes_read.sum + dram__bytes_write.sum from one ncu
-# capture (--set full) of a 2048-frame batch of the same mix on GB300: 33.48 + 27.86 MB.  It grows
-# with the frames, so a launch's traffic is scaled by its frame count.
-MIXED_DRAM_BYTES_PER_FRAME = (33.480448e6 + 27.857920e6) / 2048
+# DRAM traffic of the mixed decoder (the code-specialised kernel), dram__bytes_read.sum +
+# dram__bytes_write.sum from one ncu capture (--set full) of a 2048-frame batch of the same mix on
+# GB300: 33.62 + 34.59 MB.  It grows with the frames, so a launch's traffic is scaled by its frame
+# count.
+MIXED_DRAM_BYTES_PER_FRAME = (33.618944e6 + 34.589440e6) / 2048
 MIXED_TRAFFIC_NOTE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of a 2048-frame launch of the same mix, "
-                      "scaled by frames (61.3 MB / 2048 frames)")
+                      "scaled by frames (68.2 MB / 2048 frames)")
 
 
 def parse() -> argparse.Namespace:
@@ -459,7 +460,7 @@ def measure_mixed(args, dist: Dist) -> dict:
                                 "form": "copy_ in, graph replay, copy_ out (pinned host buffers)"}},
         "gpu_launches": (len(names) + 1) * args.steps,
         "roofline": dict(roofline(pk, alg_bytes, edge_updates, dec_ms, sm_count, clocks.get("sm_mhz") or pk["sm_max_mhz"],
-                                  "ck mixed decoder (ldpc_mixed_kernel)"),
+                                  "ck mixed decoder (ck_ldpc_mixed_code, code-specialised)"),
                          traffic=MIXED_DRAM_BYTES_PER_FRAME * sum(int(work[n].symbols.shape[0]) for n in names),
                          traffic_source=MIXED_TRAFFIC_NOTE),
         "decode": {"fer": fer, "iterations_min_mean_max": iters},
@@ -539,8 +540,11 @@ def measure_single(args, dist: Dist, wname: str) -> dict:
                 "h2d_bytes_per_step": int(sym_host.numel() * 8),
                 "d2h_bytes_per_step": int(sum(t.numel() * t.element_size() for t in out))},
         "launch_shape": code._plan(dev.index).get_launch(),
+        "specialised": code._plan(dev.index).specialisation()[1] == 1,
         "roofline": roofline(pk, frames * (8 * code.n + code.k + 5), float(iters.sum()) * code.checks.size,
-                             decode_ms, sm_count, pk["sm_max_mhz"], "ck decoder (ldpc_decode_kernel)"),
+                             decode_ms, sm_count, pk["sm_max_mhz"],
+                             "ck decoder (ck_ldpc_code_r*, code-specialised)"
+                             if code._plan(dev.index).specialisation()[1] == 1 else "ck decoder (decode_kernel)"),
         "demapper": {"launch_ms": demap_ms, "achieved_gbs": demap_bytes / (demap_ms * 1e-3) / 1e9,
                      "frac": demap_bytes / (demap_ms * 1e-3) / 1e9 / pk["hbm_gbs"]},
         "decode": {"iterations_mean": float(iters.mean()),
