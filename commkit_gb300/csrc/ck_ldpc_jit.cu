@@ -113,12 +113,25 @@ std::string program_struct(const ck_ldpc_plan& plan, const char* name) {
     s += "        uint32_t base4, qr0;\n";
     s += "        asm volatile(\"mov.b32 %0, %1;\" : \"=r\"(base4) : \"r\"(base4_in));\n";
     s += "        asm volatile(\"mov.b32 %0, %1;\" : \"=r\"(qr0) : \"r\"(qr0_in));\n";
+    // Each row's message state in device memory is loaded one row ahead
+    // (the thread's own rows: no other thread writes them, so the load may
+    // cross a barrier), which hides its L2 latency behind the previous row's
+    // arithmetic.  The padding lanes of a Z that is not a multiple of 32 load
+    // from row 0 of their base row and never use it.
+    const bool pad = Zp != Z;
+    auto row_of = [&](int32_t b) {
+        std::string r = std::to_string(static_cast<long long>(b) * Z) + "u + ";
+        return r + (pad ? "(qr0 < " + std::to_string(Z) + "u ? qr0 : 0u)" : std::string("qr0"));
+    };
+    if (plan.mb > 0) s += "        uint4 next = st.pre(" + row_of(plan.h_layer[0]) + ");\n";
     for (int32_t l = 0; l < plan.L; ++l) {
         add(s, "        // layer %lld\n", l);
-        if (Zp != Z) add(s, "        if (qr0 < %lldu) {\n", Z);
         for (int32_t b = plan.h_layer[l]; b < plan.h_layer[l + 1]; ++b) {
             const int32_t e0 = plan.h_eptr[b], deg = plan.h_eptr[b + 1] - e0;
-            add(s, "        {\n            uint32_t c[%lld];\n", deg);
+            s += "        {\n            const uint4 cur = st.take(next, " + row_of(b) + ");\n";
+            if (b + 1 < plan.mb) s += "            next = st.pre(" + row_of(b + 1) + ");\n";
+            if (pad) add(s, "            if (qr0 < %lldu) {\n", Z);
+            add(s, "            uint32_t c[%lld];\n", deg);
             for (int32_t e = 0; e < deg; ++e) {
                 const int32_t first = plan.h_blk[2 * (e0 + e)];    // j Z + shift
                 const int32_t end = plan.h_blk[2 * (e0 + e) + 1];  // (j + 1) Z
@@ -127,10 +140,11 @@ std::string program_struct(const ck_ldpc_plan& plan, const char* name) {
                 if (end - first < Z) add(s, "%lldu;", 4ll * Z);
                 s += "\n";
             }
-            add(s, "            st.template row_cols<%lld>(c, %lldu + qr0, scale, offset);\n        }\n", deg,
+            add(s, "            st.template row_cols<%lld>(c, cur, %lldu + qr0, scale, offset);\n", deg,
                 static_cast<long long>(b) * Z);
+            if (pad) s += "            }\n";
+            s += "        }\n";
         }
-        if (Zp != Z) s += "        }\n";
         s += "        ck::group_sync(bar, T);\n";
     }
     s += "    }\n};\n";

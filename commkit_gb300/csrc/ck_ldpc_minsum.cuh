@@ -239,12 +239,21 @@ struct MinSumState {
         ck::ldpc::qc_row<DMAX>(gblk, deg, r4, Z4, m1, m2, w, p.scale, p.offset);
         store(row, m1, m2, w);
     }
+    // Load-ahead for the code-specialised programs: pre(row) starts loading
+    // a row's state one row early when it lives in device memory (L2
+    // latency); take(pre, row) gives the row's state (the early load, or a
+    // shared-memory load now).
+    __device__ __forceinline__ uint4 pre(uint32_t row) const {
+        return R_SMEM ? make_uint4(0u, 0u, 0u, 0u) : load(row);
+    }
+    __device__ __forceinline__ uint4 take(const uint4 early, uint32_t row) const {
+        return R_SMEM ? load(row) : early;
+    }
     // One circulant row with its columns computed by the caller (the
-    // code-specialised programs).
+    // code-specialised programs), its state `s` from take().
     template <int D>
-    __device__ __forceinline__ void row_cols(const uint32_t (&c)[D], uint32_t row, float scale,
-                                             float offset) const {
-        const uint4 s = load(row);
+    __device__ __forceinline__ void row_cols(const uint32_t (&c)[D], const uint4 s, uint32_t row,
+                                             float scale, float offset) const {
         float m1 = __uint_as_float(s.x), m2 = __uint_as_float(s.y);
         uint32_t w = s.z;
         qc_row_cols<D>(c, m1, m2, w, scale, offset);
