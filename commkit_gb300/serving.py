@@ -333,8 +333,12 @@ class Server:
             _lib.check(lib.ck_llr_separable_maxlog_frames(
                 sym_base + 8 * g_sym, g_frames * S, S, s2_base + 4 * g_s2, ctypes.byref(re), ctypes.byref(im),
                 slot.llr[name].data_ptr() + 4 * f_off * self.codes[name].n, st), "server demap")  # fmt: skip
-        arr = self._batch_array(counts, slot, out)
-        _lib.check(lib.ck_ldpc_decode_mixed(arr, len(counts), slot.ws.data_ptr(), slot.ws.numel(), st),
+        # Every code takes part in every launch (no frames where a batch has
+        # none), so all batches run the one mixed kernel compiled for this
+        # server's codes when its slots were built.
+        every = {name: counts.get(name, 0) for name in self.codes}
+        arr = self._batch_array(every, slot, out)
+        _lib.check(lib.ck_ldpc_decode_mixed(arr, len(every), slot.ws.data_ptr(), slot.ws.numel(), st),
                    "server decode")  # fmt: skip
         slot.event.record(slot.stream)
         self._busy.append(slot)
