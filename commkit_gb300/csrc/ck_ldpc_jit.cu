@@ -97,6 +97,8 @@ void add(std::string& s, const char* fmt, long long a = 0, long long b = 0, long
 // (qr0 + shift) mod Z) and its state row b Z + qr0, then the group barrier.
 std::string program_struct(const ck_ldpc_plan& plan, const char* name) {
     const int32_t Z = plan.Z, Zp = (Z + 31) / 32 * 32;
+    // ceil(2^32 / Z): the high word of (qr0 + shift) * magic is the wrap bit.
+    const unsigned long long magic = ((1ull << 32) + static_cast<unsigned long long>(Z) - 1) / static_cast<unsigned long long>(Z);
     std::string s;
     s += "struct ";
     s += name;
@@ -135,10 +137,15 @@ std::string program_struct(const ck_ldpc_plan& plan, const char* name) {
             for (int32_t e = 0; e < deg; ++e) {
                 const int32_t first = plan.h_blk[2 * (e0 + e)];    // j Z + shift
                 const int32_t end = plan.h_blk[2 * (e0 + e) + 1];  // (j + 1) Z
-                add(s, "            c[%lld] = base4 + %lldu;", e, 4ll * first);
-                if (end - first < Z) add(s, " if (qr0 >= %lldu) c[%lld] -= ", end - first, e);
-                if (end - first < Z) add(s, "%lldu;", 4ll * Z);
-                s += "\n";
+                const long long shift = Z - (end - first);
+                if (shift == 0) {
+                    add(s, "            c[%lld] = base4 + %lldu;\n", e, 4ll * first);
+                } else {
+                    add(s, "            c[%lld] = wrapped_base(base4, qr0, %lluu, %lluull, ", e,
+                        static_cast<long long>(magic), static_cast<long long>(magic * static_cast<unsigned long long>(shift)));
+                    add(s, "%lluu) + %lldu;\n", static_cast<long long>((0x100000000ull - 4ull * Z) & 0xffffffffull),
+                        4ll * first);
+                }
             }
             add(s, "            st.template row_cols<%lld>(c, cur, %lldu + qr0, scale, offset);\n", deg,
                 static_cast<long long>(b) * Z);
@@ -158,7 +165,9 @@ std::string program_source(const ck_ldpc_plan& plan, int dmax) {
     s += program_struct(plan, "CodeProgram");
     s += "}  // namespace\n";
     for (int r = 0; r < 2; ++r) {
-        add(s, "extern \"C\" __global__ void __launch_bounds__(%lld) ck_ldpc_code_r%lld(const __grid_constant__ Params p) {\n",
+        // A minimum of one block per SM, stated: without it ptxas held some of
+        // these kernels to 40 registers and spilled.
+        add(s, "extern \"C\" __global__ void __launch_bounds__(%lld, 1) ck_ldpc_code_r%lld(const __grid_constant__ Params p) {\n",
             max_block_threads(true, dmax), r);
         add(s, "    decode_body<MinSumState, true, %lld, true, ", dmax);
         s += r ? "true" : "false";
@@ -192,7 +201,7 @@ std::string mixed_program_source(const ck_ldpc_plan* const* plans, const bool* s
         s += "                break;\n";
     }
     s += "            default:\n                break;\n        }\n    }\n};\n}  // namespace\n";
-    add(s, "extern \"C\" __global__ void __launch_bounds__(kMixedThreads) ck_ldpc_mixed_code(const __grid_constant__ MixedParams p) {\n    mixed_body<%lld, CodeDispatch>(p);\n}\n", dmax);
+    add(s, "extern \"C\" __global__ void __launch_bounds__(kMixedThreads, 1) ck_ldpc_mixed_code(const __grid_constant__ MixedParams p) {\n    mixed_body<%lld, CodeDispatch>(p);\n}\n", dmax);
     return s;
 }
 

@@ -131,6 +131,22 @@ __device__ __forceinline__ void qc_row_cols(const uint32_t (&c)[D], float& m1, f
     w = (signs & 0x07ffffffu) | (idx << 27);
 }
 
+// Row-qr0 column base of a circulant with shift s in the code-specialised
+// programs, on the FMA pipe (the kernel is bound by the ALU pipe): the wrap
+// (qr0 + s >= Z) is the high word of qr0 * M + s * M with M = ceil(2^32 / Z)
+// (exact: qr0 + s < 2 Z and (qr0 + s) Z < 2^32), and the base is
+// base4 - wrap * 4 Z; the caller adds the column's constant part.
+__device__ __forceinline__ uint32_t wrapped_base(uint32_t base4, uint32_t qr0, uint32_t M, uint64_t sM,
+                                                 uint32_t neg_z4) {
+    uint32_t lo, hi, c;
+    asm("{\n\t.reg .u64 t;\n\tmad.wide.u32 t, %2, %3, %4;\n\tmov.b64 {%0, %1}, t;\n\t}"
+        : "=r"(lo), "=r"(hi)
+        : "r"(qr0), "r"(M), "l"(sM));
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(c) : "r"(hi), "r"(neg_z4), "r"(base4));
+    (void)lo;
+    return c;
+}
+
 // Row r of a circulant base row: gblk[e] = (shared address of circulant
 // e's row-0 column, address of its block's end), r4 = 4 r, Z4 = 4 Z; row
 // r's column is r4 + gblk[e].x, wrapped back by Z4 once it reaches the end.
