@@ -138,12 +138,11 @@ __device__ __forceinline__ void qc_row_cols(const uint32_t (&c)[D], float& m1, f
 // base4 - wrap * 4 Z; the caller adds the column's constant part.
 __device__ __forceinline__ uint32_t wrapped_base(uint32_t base4, uint32_t qr0, uint32_t M, uint64_t sM,
                                                  uint32_t neg_z4) {
-    uint32_t lo, hi, c;
-    asm("{\n\t.reg .u64 t;\n\tmad.wide.u32 t, %2, %3, %4;\n\tmov.b64 {%0, %1}, t;\n\t}"
-        : "=r"(lo), "=r"(hi)
+    uint32_t hi, c;
+    asm("{\n\t.reg .u64 t;\n\t.reg .u32 lo;\n\tmad.wide.u32 t, %1, %2, %3;\n\tmov.b64 {lo, %0}, t;\n\t}"
+        : "=r"(hi)
         : "r"(qr0), "r"(M), "l"(sM));
     asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(c) : "r"(hi), "r"(neg_z4), "r"(base4));
-    (void)lo;
     return c;
 }
 

@@ -123,6 +123,43 @@ def test_specialised_kernel_equals_table_kernel(torch_dev, ck, name, frames, ord
     _assert_same(got[0], _oracle(codes[0], llr.cpu().numpy(), max_iterations=30))
 
 
+@pytest.mark.parametrize("z,seed", [(27, 1), (32, 2), (100, 3), (160, 4), (45, 5)])
+def test_specialised_random_codes(torch_dev, ck, z, seed):
+    """Random circulant codes (liftings that are and are not multiples of
+    32, rows of degree 2 to 16 over a dual-diagonal parity part, punctured
+    columns) decoded by the generated kernel, against the table-driven
+    kernel and the oracle."""
+    from commkit_gb300 import _lib
+
+    torch, dev = torch_dev
+    rng = np.random.default_rng(seed)
+    mb, nb = int(rng.integers(3, 9)), int(rng.integers(12, 22))
+    base = np.full((mb, nb), -1, dtype=np.int64)
+    kb = nb - mb
+    for i in range(mb):
+        deg = int(rng.integers(1, min(14, kb) + 1))
+        cols = rng.choice(kb, size=deg, replace=False)
+        base[i, cols] = rng.integers(0, z, size=deg)
+        base[i, kb + i] = 0  # dual-diagonal parity part: full rank
+        if i + 1 < mb:
+            base[i + 1, kb + i] = 0
+    punct = z if seed % 2 else 0
+    codes = [ck.LDPCCode.quasi_cyclic(base, lifting=z, punctured=punct) for _ in range(2)]
+    zp = (z + 31) // 32 * 32
+    for code, mode in zip(codes, (_lib.CK_LDPC_SPECIALISE_ON, _lib.CK_LDPC_SPECIALISE_OFF), strict=True):
+        code._plan(0).set_specialise(mode)
+        code._plan(0).set_launch(zp, 0, 0)
+    assert codes[0]._plan(0).info["lifting"] == z
+    frames = 96
+    llr = (0.8 + 1.6 * rng.standard_normal((frames, codes[0].n))).astype(np.float32)
+    x = torch.from_numpy(llr).to(dev)
+    method = ck.MinSum(scale=0.8, offset=0.02, max_iterations=15)
+    got = [_to_np(ck.decode(x, code=c, method=method), frames) for c in codes]
+    assert codes[0]._plan(0).specialisation()[1] == 1
+    _assert_same(got[0], got[1])
+    _assert_same(got[0], _oracle(codes[0], llr, scale=0.8, offset=0.02, max_iterations=15))
+
+
 @pytest.mark.parametrize("name", ["A", "B"])
 def test_golden_codes(golden_ldpc, torch_dev, ck, name):
     torch, dev = torch_dev
