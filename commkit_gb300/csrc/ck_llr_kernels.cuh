@@ -61,21 +61,44 @@ __device__ __forceinline__ float neg_sq_scaled(float d, float inv_s2) {
 template <int KA>
 struct MaxlogAxis {
     static constexpr int L = 1 << KA;
+    float step, rstep;  // lev[1] - lev[0] and its rounded reciprocal
     float lev[L];
     int32_t lab[L];
-    int32_t lo[KA * L];
-    int32_t hi[KA * L];
+    // For bit b and snapped level s: the nearest level below (lo) and above
+    // (hi) whose bit b differs, as level VALUES, +inf where there is none
+    // (the reference's index -1).
+    float lo[KA * L];
+    float hi[KA * L];
     int32_t pos[KA];
 };
 
 // LLRs of one axis's KA bits (axis bit order) of the coordinate `x`.
+//
+// Per bit the reference takes m_other = max(-3e38, f(x - lo), f(x - hi))
+// over the opposite levels that exist, with f(d) = -(d*d)*inv_s2 rounded
+// twice.  f falls as |d| grows and rounding is monotone, so that maximum
+// is f of the smaller |d| (equal magnitudes give equal values): one metric
+// per bit instead of two.  A missing level is +inf, whose |x - inf| never
+// wins against a finite distance; the cases where every candidate is
+// infinite or NaN end at -3e38 on both routes, as do NaN inputs.
 template <int KA>
 __device__ __forceinline__ void axis_maxlog(float x, const MaxlogAxis<KA>& t, float inv_s2,
                                             float* o) {
     constexpr int L = 1 << KA;
-    const float q = __fdiv_rn(__fsub_rn(x, t.lev[0]), __fsub_rn(t.lev[1], t.lev[0]));
-    int s = __float2int_rn(q);  // round half to even, as np.rint
-    s = min(max(s, 0), L - 1);
+    // s = rint((x - lev0) / step), clamped to [0, L - 1] (round half to
+    // even, as np.rint).  The quotient comes from a multiply by the rounded
+    // reciprocal, within 3 units in the last place of the IEEE quotient
+    // (two roundings of 2^-24 plus the reciprocal's), so it rounds to the
+    // same integer unless it lies within that distance of a half-integer;
+    // there (rarely) the IEEE division decides.  qp - rint(qp) is exact.
+    // NaN and infinite x clamp as the integer conversion of the reference
+    // does (NaN to 0, +-inf to the ends).
+    const float a = __fsub_rn(x, t.lev[0]);
+    const float qp = __fmul_rn(a, t.rstep);
+    float rq = rintf(qp);
+    if (fabsf(fabsf(__fsub_rn(qp, rq)) - 0.5f) <= __fmul_rn(fabsf(qp), 0x1p-20f))
+        rq = rintf(__fdiv_rn(a, t.step));
+    int s = static_cast<int>(fminf(fmaxf(rq, 0.0f), static_cast<float>(L - 1)));
     float d = __fsub_rn(x, t.lev[s]);
     // Near a midpoint the rounded quotient can land one level off: keep the
     // nearer of s and its neighbour towards x.
@@ -91,11 +114,8 @@ __device__ __forceinline__ void axis_maxlog(float x, const MaxlogAxis<KA>& t, fl
     const int32_t label = t.lab[s];
 #pragma unroll
     for (int b = 0; b < KA; ++b) {
-        float m_other = -3.0e38f;
-        int j = t.lo[b * L + s];
-        if (j >= 0) m_other = fmaxf(m_other, neg_sq_scaled(__fsub_rn(x, t.lev[j]), inv_s2));
-        j = t.hi[b * L + s];
-        if (j >= 0) m_other = fmaxf(m_other, neg_sq_scaled(__fsub_rn(x, t.lev[j]), inv_s2));
+        const float dn = fminf(fabsf(__fsub_rn(x, t.lo[b * L + s])), fabsf(__fsub_rn(x, t.hi[b * L + s])));
+        const float m_other = fmaxf(-3.0e38f, neg_sq_scaled(dn, inv_s2));
         const bool one = (label >> (KA - 1 - b)) & 1;
         o[b] = one ? __fsub_rn(m_other, m_own) : __fsub_rn(m_own, m_other);
     }
@@ -109,10 +129,15 @@ __device__ __forceinline__ void load_maxlog_axis(MaxlogAxis<KA>& t, const ck_axi
         t.lab[i] = a.labels[i];
     }
     for (int i = threadIdx.x; i < KA * L; i += blockDim.x) {
-        t.lo[i] = a.lo[i];
-        t.hi[i] = a.hi[i];
+        const int32_t lo = a.lo[i], hi = a.hi[i];
+        t.lo[i] = lo >= 0 ? a.levels[lo] : ck::inf_f();
+        t.hi[i] = hi >= 0 ? a.levels[hi] : ck::inf_f();
     }
     for (int i = threadIdx.x; i < KA; i += blockDim.x) t.pos[i] = a.pos[i];
+    if (threadIdx.x == 0) {
+        t.step = __fsub_rn(a.levels[1], a.levels[0]);
+        t.rstep = __frcp_rn(t.step);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -238,6 +263,17 @@ struct NoiseScale {
     __device__ __forceinline__ float at(uint32_t i) const {
         return frames ? __ldg(frames + frame_len.div(i)) : value;
     }
+    // Symbols i and i + 1: one division; the second is in the next frame
+    // only when i + 1 starts it.
+    __device__ __forceinline__ void pair(uint32_t i, float& a, float& b) const {
+        if (!frames) {
+            a = b = value;
+            return;
+        }
+        const uint32_t f = frame_len.div(i);
+        a = __ldg(frames + f);
+        b = i + 1 == (f + 1) * frame_len.d ? __ldg(frames + f + 1) : a;
+    }
 };
 
 // Both axes' tables of one method, in shared memory.
@@ -309,6 +345,17 @@ __global__ void __launch_bounds__(kThreads) llr_kernel(const float2* __restrict_
                                                        float* __restrict__ out) {
     constexpr int K = 2 * KA;
     __shared__ Tables<KA, METHOD> tab;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t npairs = n >> 1;
+    const float4* x4 = reinterpret_cast<const float4*>(x);
+    // The first two pairs are requested before the tables load (their
+    // latencies overlap), and each step requests the next step's pairs
+    // before computing its own.
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 na = zero4, nb = zero4;
+    if (PAIRS && t0 < npairs) na = ld_stream(x4 + t0);
+    if (PAIRS && t0 + stride < npairs) nb = ld_stream(x4 + t0 + stride);
     tab.load(re, im);
     __syncthreads();
     bool standard = true;
@@ -316,25 +363,24 @@ __global__ void __launch_bounds__(kThreads) llr_kernel(const float2* __restrict_
     for (int b = 0; b < KA; ++b)
         standard = standard && tab.re.pos[b] == b && tab.im.pos[b] == KA + b;
 
-    const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
     if (PAIRS) {
-        const uint32_t npairs = n >> 1;
-        const float4* x4 = reinterpret_cast<const float4*>(x);
         for (uint32_t p = t0; p < npairs; p += 2 * stride) {
             const uint32_t pb = p + stride;
             const bool two = pb < npairs;
-            const float4 va = ld_stream(x4 + p);
-            float4 vb = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (two) vb = ld_stream(x4 + pb);
+            const float4 va = na, vb = nb;
+            const uint32_t pn = p + 2 * stride;
+            na = pn < npairs ? ld_stream(x4 + pn) : zero4;
+            nb = pn + stride < npairs ? ld_stream(x4 + pn + stride) : zero4;
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 if (h == 1 && !two) break;
                 const uint32_t pp = h ? pb : p;
                 const float4 v = h ? vb : va;
                 float o[2 * K];
-                tab.symbol(make_float2(v.x, v.y), noise.at(2 * pp), o);
-                tab.symbol(make_float2(v.z, v.w), noise.at(2 * pp + 1), o + K);
+                float sa, sb;
+                noise.pair(2 * pp, sa, sb);
+                tab.symbol(make_float2(v.x, v.y), sa, o);
+                tab.symbol(make_float2(v.z, v.w), sb, o + K);
                 if (standard) {
                     float4* dst = reinterpret_cast<float4*>(out + static_cast<uint64_t>(pp) * 2 * K);
 #pragma unroll
