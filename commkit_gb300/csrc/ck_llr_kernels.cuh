@@ -349,13 +349,7 @@ __global__ void __launch_bounds__(kThreads) llr_kernel(const float2* __restrict_
     const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t npairs = n >> 1;
     const float4* x4 = reinterpret_cast<const float4*>(x);
-    // The first two pairs are requested before the tables load (their
-    // latencies overlap), and each step requests the next step's pairs
-    // before computing its own.
     const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 na = zero4, nb = zero4;
-    if (PAIRS && t0 < npairs) na = ld_stream(x4 + t0);
-    if (PAIRS && t0 + stride < npairs) nb = ld_stream(x4 + t0 + stride);
     tab.load(re, im);
     __syncthreads();
     bool standard = true;
@@ -367,10 +361,8 @@ __global__ void __launch_bounds__(kThreads) llr_kernel(const float2* __restrict_
         for (uint32_t p = t0; p < npairs; p += 2 * stride) {
             const uint32_t pb = p + stride;
             const bool two = pb < npairs;
-            const float4 va = na, vb = nb;
-            const uint32_t pn = p + 2 * stride;
-            na = pn < npairs ? ld_stream(x4 + pn) : zero4;
-            nb = pn + stride < npairs ? ld_stream(x4 + pn + stride) : zero4;
+            const float4 va = ld_stream(x4 + p);
+            const float4 vb = two ? ld_stream(x4 + pb) : zero4;
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 if (h == 1 && !two) break;
