@@ -357,7 +357,37 @@ __global__ void __launch_bounds__(kThreads) llr_kernel(const float2* __restrict_
     for (int b = 0; b < KA; ++b)
         standard = standard && tab.re.pos[b] == b && tab.im.pos[b] == KA + b;
 
-    if (PAIRS) {
+    if (PAIRS && METHOD != 0) {
+        // The level-metric methods are long (exp/log per level, the rare
+        // underflow redo): one symbol at a time through a single copy of the
+        // code, so the loop stays in the instruction cache and the registers
+        // hold one symbol's state (unrolled over two pairs, the 64-QAM exact
+        // kernel took 160 registers and stalled on instruction fetch).
+        for (uint32_t p = t0; p < npairs; p += stride) {
+            const float4 v = ld_stream(x4 + p);
+            float sa, sb;
+            noise.pair(2 * p, sa, sb);
+#pragma unroll 1
+            for (int h = 0; h < 2; ++h) {
+                float o[K];
+                tab.symbol(h ? make_float2(v.z, v.w) : make_float2(v.x, v.y), h ? sb : sa, o);
+                const uint32_t i = 2 * p + h;
+                if (standard) {
+                    float2* dst = reinterpret_cast<float2*>(out + static_cast<uint64_t>(i) * K);
+#pragma unroll
+                    for (int q = 0; q < K / 2; ++q) __stcs(dst + q, make_float2(o[2 * q], o[2 * q + 1]));
+                } else {
+                    store_scattered<KA>(tab, out, i, o);
+                }
+            }
+        }
+        if ((n & 1u) && t0 == 0) {
+            const uint32_t i = n - 1;
+            float o[K];
+            tab.symbol(x[i], noise.at(i), o);
+            store_scattered<KA>(tab, out, i, o);
+        }
+    } else if (PAIRS) {
         for (uint32_t p = t0; p < npairs; p += 2 * stride) {
             const uint32_t pb = p + stride;
             const bool two = pb < npairs;
