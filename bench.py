@@ -66,6 +66,7 @@ WORKLOADS = {
     "demapper": dict(desc="separable demapper: 2^22 symbols, 1024 frames x 4096, per-frame Es/N0 U[8,20] dB, "
                           "16- and 64-QAM, max-log and exact"),
     "mpoint": dict(desc="M-point demapper: 16-PSK, 128-cross-QAM, 8-QAM at 2^22 symbols, max-log and exact"),
+    "montecarlo": dict(desc="error_rate_curve (device Monte-Carlo loop) of codes A and C around the waterfall"),
     "dvbs2": dict(frames=64, max_it=50,
                   desc="the reference's LDPC benchmark: DVB-S2 normal frame rate 1/2 (N=64800, K=32400), "
                        "64 QPSK codewords at Es/N0 1.5 dB, one decode() call, MinSum() and SumProduct() defaults"),
@@ -687,6 +688,44 @@ def measure_mpoint(dist: Dist) -> dict:
             "fp64_sample_symbols": FP64_SAMPLE, "results": out}
 
 
+def measure_montecarlo(dist: Dist) -> dict:
+    """The Monte-Carlo error-rate loop (``error_rate_curve``) of codes A and
+    C at three Es/N0 points around each waterfall, a fixed number of blocks
+    per point (no early end on errors): bits, encoding, mapping, noise,
+    demapping, decoding and error counts all on the device, one 56-byte
+    result copy per batch.  At the reference's batch (2^18 transmitted bits,
+    203 / 10 blocks) and at 4096-block batches."""
+    import torch
+
+    import commkit_gb300 as ck
+    from commkit_gb300 import workloads as W
+
+    out = {}
+    for name, order in (("A", 4), ("C", 16)):
+        spec = W.CODES[name]
+        code = ck.LDPCCode.quasi_cyclic(spec.base(), lifting=spec.z)
+        c = ck.Constellation.qam(order)
+        k = int(round(np.log2(order)))
+        es0 = W.WATERFALL_DB[name] + 10 * np.log10(code.k / code.n * k)
+        grid = [es0 - 0.5, es0, es0 + 0.5]
+        for label, batch, blocks in (("reference_batch", None, 4096 if name == "A" else 1024),
+                                     ("batch_4096", 4096, 16384 if name == "A" else 8192)):  # fmt: skip
+            kw = dict(constellation=c, esn0_db=grid, method=ck.MinSum(max_iterations=50), min_block_errors=10**9,
+                      max_blocks=blocks, rng=1, batch_blocks=batch)  # fmt: skip
+            ck.error_rate_curve(code, **{**kw, "max_blocks": min(blocks, 512)})  # warm-up (plans, graphs)
+            torch.cuda.synchronize(dist.dev)
+            t = time.perf_counter()
+            curve = ck.error_rate_curve(code, **kw)
+            torch.cuda.synchronize(dist.dev)
+            dt = time.perf_counter() - t
+            nblk = int(np.sum(curve.num_blocks))
+            out[f"{name}_{label}"] = {"blocks": nblk, "s": dt, "blocks_per_s": nblk / dt,
+                                      "info_gbps": nblk * code.k / dt / 1e9, "fer": [float(v) for v in curve.fer],
+                                      "mean_iterations": [float(v) for v in curve.mean_iterations]}  # fmt: skip
+    return {"workload": "error_rate_curve of codes A (QPSK) and C (16-QAM) at the waterfall Es/N0 and +-0.5 dB, "
+                        "MinSum 50 it, fixed blocks per point, wall clock of the public call", "results": out}
+
+
 def measure_dvbs2(dist: Dist, steps: int = 10, warmup: int = 3) -> dict:
     """The reference's own LDPC benchmark (``benchmarks/bench_coding.py:37-38,
     55-56,75-86``): 64 DVB-S2 normal-frame rate-1/2 codewords over QPSK at
@@ -820,6 +859,13 @@ def main() -> None:
                 "steps": 10, "warmup": 3, "ms_per_step": r["us"] / 1e3, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
                 "config": {"workload": mp_["workload"]}, "mpoint": mp_}  # fmt: skip
+    elif args.workload == "montecarlo":
+        mc = measure_montecarlo(dist)
+        r = mc["results"]["C_batch_4096"]
+        line = {"metric": "Monte-Carlo decoded info Gb/s", "value": r["info_gbps"], "unit": UNIT, "n_gpus": 1,
+                "steps": 1, "warmup": 1, "ms_per_step": r["s"] * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+                "config": {"workload": mc["workload"]}, "montecarlo": mc}  # fmt: skip
     elif args.workload == "dvbs2":
         dv = measure_dvbs2(dist, args.steps, args.warmup)
         ms = dv["min_sum"]["ms"]
@@ -843,7 +889,7 @@ def main() -> None:
                 "gpu_launches": 2 * args.steps, "roofline": s["roofline"], "demapper": s["demapper"],
                 "decode": s["decode"], "parity": s["parity"]}  # fmt: skip
     if dist.rank == 0:
-        if not args.no_cpu_baseline and args.workload not in ("served", "dvbs2", "mpoint", "demapper"):
+        if not args.no_cpu_baseline and args.workload not in ("served", "dvbs2", "mpoint", "demapper", "montecarlo"):
             sample, threads, desc = cpu_sample(args, 10.0)
             t, bits = oracle_step(sample, args.w["max_it"], threads, args.w.get("method", "maxlog"))
             line["cpu_baseline"] = {"value": bits / t / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
@@ -855,6 +901,7 @@ def main() -> None:
                             ("2", lambda: measure_demapper(dist)),
                             ("2_mpoint", lambda: measure_mpoint(dist)),
                             ("reference_ldpc_benchmark", lambda: measure_dvbs2(dist)),
+                            ("f1_montecarlo", lambda: measure_montecarlo(dist)),
                             ("5", lambda: measure_served(args, dist))):  # fmt: skip
                 try:
                     configs[key] = fn()
