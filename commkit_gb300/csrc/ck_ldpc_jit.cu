@@ -60,6 +60,10 @@ const Nvrtc& nvrtc() {
         std::string tried;
         std::string paths[] = {"libnvrtc.so.13", "libnvrtc.so", "", "/usr/local/cuda/lib64/libnvrtc.so.13"};
         if (const char* home = getenv("CUDA_HOME")) paths[2] = std::string(home) + "/lib64/libnvrtc.so.13";
+        if (const char* only = getenv("COMMKIT_GB300_NVRTC")) {  // an explicit library, and nothing else
+            paths[0] = only;
+            paths[1] = paths[2] = paths[3] = "";
+        }
         for (const std::string& p : paths) {
             if (p.empty()) continue;
             h = dlopen(p.c_str(), RTLD_NOW | RTLD_LOCAL);
@@ -154,7 +158,37 @@ std::string program_struct(const ck_ldpc_plan& plan, const char* name) {
         }
         s += "        ck::group_sync(bar, T);\n";
     }
-    s += "    }\n};\n";
+    s += "    }\n";
+    // The syndrome test over the same rows: per base row the parity of the
+    // sign bits (the posterior holds no -0 and only positive NaNs, so the
+    // sign bit is "< 0"), one group OR per base row, stopping at the first
+    // unsatisfied one.
+    s += "    __device__ __forceinline__ static bool syndrome(const uint32_t base4_in, const uint32_t qr0_in,\n";
+    s += "                                                    const int bar, const int T) {\n";
+    s += "        uint32_t base4, qr0;\n";
+    s += "        asm volatile(\"mov.b32 %0, %1;\" : \"=r\"(base4) : \"r\"(base4_in));\n";
+    s += "        asm volatile(\"mov.b32 %0, %1;\" : \"=r\"(qr0) : \"r\"(qr0_in));\n";
+    for (int32_t b = 0; b < plan.mb; ++b) {
+        const int32_t e0 = plan.h_eptr[b], deg = plan.h_eptr[b + 1] - e0;
+        s += "        {\n            uint32_t x = 0u;\n";
+        if (pad) add(s, "            if (qr0 < %lldu) {\n", Z);
+        for (int32_t e = 0; e < deg; ++e) {
+            const int32_t first = plan.h_blk[2 * (e0 + e)];
+            const int32_t end = plan.h_blk[2 * (e0 + e) + 1];
+            const long long shift = Z - (end - first);
+            if (shift == 0) {
+                add(s, "            x ^= __float_as_uint(ld_shared_f32(base4 + %lldu));\n", 4ll * first);
+            } else {
+                add(s, "            x ^= __float_as_uint(ld_shared_f32(wrapped_base(base4, qr0, %lluu, %lluull, ",
+                    static_cast<long long>(magic), static_cast<long long>(magic * static_cast<unsigned long long>(shift)));
+                add(s, "%lluu) + %lldu));\n", static_cast<long long>((0x100000000ull - 4ull * Z) & 0xffffffffull),
+                    4ll * first);
+            }
+        }
+        if (pad) s += "            }\n";
+        s += "            if (ck::group_any(static_cast<int>(x >> 31), bar, T)) return false;\n        }\n";
+    }
+    s += "        return true;\n    }\n};\n";
     return s;
 }
 

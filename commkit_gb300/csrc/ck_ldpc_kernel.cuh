@@ -198,8 +198,11 @@ struct TableProgram {
 //   template <class St> static void iteration(const St& st, uint32_t base4,
 //       uint32_t qr0, float scale, float offset, int bar, int T)
 // runs one iteration (every layer, each followed by the group barrier) with
-// the code's layers, degrees, block columns and shifts as constants;
-// base4 is the shared address of the posterior plus 4 qr0.
+// the code's layers, degrees, block columns and shifts as constants, and
+//   static bool syndrome(uint32_t base4, uint32_t qr0, int bar, int T)
+// the early-stop test over the same rows (true in every thread of the group
+// when every check holds); base4 is the shared address of the posterior
+// plus 4 qr0.
 template <template <bool> class State, bool QC, int DMAX, bool APP_SMEM, bool R_SMEM, bool ONE_ROW,
           class Prog>
 __device__ __forceinline__ void decode_body(const Params& p) {
@@ -293,8 +296,20 @@ __device__ __forceinline__ void decode_body(const Params& p) {
         group_sync(bar, p.T);
 
         int32_t it = 0;
-        bool ok = p.early_stop && syndrome_ok<QC>(p, a, s_eptr, s_blk, tid, bar, qr0, qb0);
-        while (!ok && it < p.max_iterations) {
+        // The syndrome test: the code's generated one, or the table-driven one.
+        auto satisfied = [&]() -> bool {
+            if constexpr (Prog::kSpecialised)
+                return Prog::syndrome(ck::smem_addr(a) + 4u * static_cast<uint32_t>(qr0),
+                                      static_cast<uint32_t>(qr0), bar, p.T);
+            return syndrome_ok<QC>(p, a, s_eptr, s_blk, tid, bar, qr0, qb0);
+        };
+        // One call site of the test (it is long when generated): before the
+        // first iteration and after each one with early stop, after the last
+        // one without.
+        bool ok = false;
+        for (;;) {
+            if (p.early_stop || it == p.max_iterations) ok = satisfied();
+            if (ok || it >= p.max_iterations) break;
             if constexpr (Prog::kSpecialised) {
                 Prog::iteration(st, ck::smem_addr(a) + 4u * static_cast<uint32_t>(qr0),
                                 static_cast<uint32_t>(qr0), p.scale, p.offset, bar, p.T);
@@ -339,9 +354,7 @@ __device__ __forceinline__ void decode_body(const Params& p) {
                 group_sync(bar, p.T);
             }
             ++it;
-            if (p.early_stop) ok = syndrome_ok<QC>(p, a, s_eptr, s_blk, tid, bar, qr0, qb0);
         }
-        if (!p.early_stop) ok = syndrome_ok<QC>(p, a, s_eptr, s_blk, tid, bar, qr0, qb0);
 
         float* dst = p.llr_out + static_cast<size_t>(f) * p.n_in;
         for (int i = tid; i < p.n_in; i += p.T) __stcs(dst + i, a[i]);

@@ -96,7 +96,7 @@ __device__ __forceinline__ void mixed_frames(const MixedCode& K, unsigned char* 
     const uint32_t r4 = 4u * static_cast<uint32_t>(qr0);
     const uint32_t Z4 = 4u * static_cast<uint32_t>(K.Z);
 
-    auto syndrome_ok = [&]() -> bool {
+    auto syndrome_table = [&]() -> bool {
         const int32_t rounds = (K.mb + K.q_bstep - 1) / K.q_bstep;
         for (int32_t k = 0; k < rounds; ++k) {
             const int32_t b = k * K.q_bstep + qb0;
@@ -114,6 +114,12 @@ __device__ __forceinline__ void mixed_frames(const MixedCode& K, unsigned char* 
         return true;
     };
 
+    auto syndrome_ok = [&]() -> bool {
+        if constexpr (Prog::kSpecialised)
+            return Prog::syndrome(a_addr + r4, static_cast<uint32_t>(qr0), bar, K.T);
+        return syndrome_table();
+    };
+
     for (;;) {
         if (tid == 0) *s_frame = atomicAdd(K.counter, 1u);
         group_sync(bar, K.T);
@@ -126,8 +132,10 @@ __device__ __forceinline__ void mixed_frames(const MixedCode& K, unsigned char* 
         st.zero_rows(K.m, tid, K.T);
         group_sync(bar, K.T);
         int32_t it = 0;
-        bool ok = K.early_stop && syndrome_ok();
-        while (!ok && it < K.max_iterations) {
+        bool ok = false;  // one call site of the test, as in decode_body
+        for (;;) {
+            if (K.early_stop || it == K.max_iterations) ok = syndrome_ok();
+            if (ok || it >= K.max_iterations) break;
             // One check row: row r of base row b (circulants e0 .. e0 + deg).
             auto do_row = [&](int32_t b, int32_t e0, int deg, int32_t r) {
                 const uint32_t row = static_cast<uint32_t>(b) * static_cast<uint32_t>(K.Z) +
@@ -158,9 +166,7 @@ __device__ __forceinline__ void mixed_frames(const MixedCode& K, unsigned char* 
                 group_sync(bar, K.T);
             }
             ++it;
-            if (K.early_stop) ok = syndrome_ok();
         }
-        if (!K.early_stop) ok = syndrome_ok();
         float* dst = K.llr_out + static_cast<size_t>(f) * K.n_in;
         for (int i = tid; i < K.n_in; i += K.T) __stcs(dst + i, a[i]);
         if (K.bits) {

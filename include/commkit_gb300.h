@@ -306,7 +306,8 @@ int ck_ldpc_plan_get_launch(const ck_ldpc_plan* plan, ck_ldpc_launch* launch);
  * frame groups have one thread per row slot (threads per frame == Z rounded
  * up to whole warps) then run it.  AUTO (the default) falls back to the
  * table-driven kernel where NVRTC is missing or the environment sets
- * COMMKIT_GB300_SPECIALISE=0; ON makes an unavailable specialisation an
+ * COMMKIT_GB300_SPECIALISE=0 (COMMKIT_GB300_NVRTC names the NVRTC library
+ * to load instead of searching for it); ON makes an unavailable specialisation an
  * error; OFF always uses the table-driven kernel.  get_specialise reports
  * the mode and the state: 0 not compiled yet, 1 compiled, -1 unavailable
  * (ck_last_error() then says why).

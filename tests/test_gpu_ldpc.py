@@ -123,6 +123,42 @@ def test_specialised_kernel_equals_table_kernel(torch_dev, ck, name, frames, ord
     _assert_same(got[0], _oracle(codes[0], llr.cpu().numpy(), max_iterations=30))
 
 
+def test_specialisation_without_nvrtc():
+    """Where NVRTC cannot be loaded, AUTO decodes on the table-driven kernel
+    (the same bits) and says why, and ON is an error (a child process: the
+    library looks for NVRTC once per process)."""
+    import os
+    import subprocess
+    import sys
+
+    code = r"""
+import numpy as np, torch, commkit_gb300 as ck
+from commkit_gb300 import _lib, workloads as W
+s = W.CODES["A"]
+code = ck.LDPCCode.quasi_cyclic(s.base(), lifting=s.z)
+code._plan(0).set_launch(64, 0, 0)
+x = torch.from_numpy((1.0 + np.random.default_rng(0).standard_normal((8, code.n))).astype(np.float32)).cuda()
+r = ck.decode(x, code=code)
+mode, state, why = code._plan(0).specialisation()
+assert state == -1 and "NVRTC not found" in why, (state, why)
+code2 = ck.LDPCCode.quasi_cyclic(s.base(), lifting=s.z)
+code2._plan(0).set_specialise(_lib.CK_LDPC_SPECIALISE_ON)
+code2._plan(0).set_launch(64, 0, 0)
+try:
+    ck.decode(x, code=code2)
+    raise SystemExit("ON without NVRTC did not fail")
+except ValueError as e:
+    assert "unavailable" in str(e), e
+print("ok", int(r.iterations.sum()))
+"""
+    env = dict(os.environ, COMMKIT_GB300_NVRTC="/nonexistent/libnvrtc.so.13")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    res = subprocess.run([sys.executable, "-c", code], env=env, cwd=root, capture_output=True, text=True,
+                         timeout=300)  # fmt: skip
+    assert res.returncode == 0, res.stdout + res.stderr
+    assert res.stdout.startswith("ok")
+
+
 @pytest.mark.parametrize("z,seed", [(27, 1), (32, 2), (100, 3), (160, 4), (45, 5)])
 def test_specialised_random_codes(torch_dev, ck, z, seed):
     """Random circulant codes (liftings that are and are not multiples of
