@@ -161,13 +161,16 @@ std::string program_struct(const ck_ldpc_plan& plan, const char* name) {
     s += "    }\n";
     // The syndrome test over the same rows: per base row the parity of the
     // sign bits (the posterior holds no -0 and only positive NaNs, so the
-    // sign bit is "< 0"), one group OR per base row, stopping at the first
-    // unsatisfied one.
+    // sign bit is "< 0"), ORed over a round of base rows, one group OR per
+    // round, stopping at the first unsatisfied round.  The first round is
+    // one base row (an unconverged frame usually fails there), the others
+    // eight (a converged frame pays for few group ORs).
     s += "    __device__ __forceinline__ static bool syndrome(const uint32_t base4_in, const uint32_t qr0_in,\n";
     s += "                                                    const int bar, const int T) {\n";
     s += "        uint32_t base4, qr0;\n";
     s += "        asm volatile(\"mov.b32 %0, %1;\" : \"=r\"(base4) : \"r\"(base4_in));\n";
     s += "        asm volatile(\"mov.b32 %0, %1;\" : \"=r\"(qr0) : \"r\"(qr0_in));\n";
+    s += "        uint32_t bad = 0u;\n";
     for (int32_t b = 0; b < plan.mb; ++b) {
         const int32_t e0 = plan.h_eptr[b], deg = plan.h_eptr[b + 1] - e0;
         s += "        {\n            uint32_t x = 0u;\n";
@@ -186,7 +189,11 @@ std::string program_struct(const ck_ldpc_plan& plan, const char* name) {
             }
         }
         if (pad) s += "            }\n";
-        s += "            if (ck::group_any(static_cast<int>(x >> 31), bar, T)) return false;\n        }\n";
+        s += "            bad |= x >> 31;\n        }\n";
+        if (b == 0 || b % 8 == 0 || b + 1 == plan.mb) {
+            s += "        if (ck::group_any(static_cast<int>(bad), bar, T)) return false;\n";
+            if (b + 1 < plan.mb) s += "        bad = 0u;\n";
+        }
     }
     s += "        return true;\n    }\n};\n";
     return s;
