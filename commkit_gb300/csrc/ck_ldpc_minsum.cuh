@@ -13,8 +13,8 @@ namespace ldpc {
 // One check row, min-sum: reads the row's compressed state (m1, m2, w),
 // updates the posterior `a` of its deg variables (columns from col_of) and
 // writes the new state back.  Two passes as the reference's min_sum_row
-// (commkit/_cuda/src/ldpc.cu:45-72), with Q kept in registers between them
-// (columns are recomputed in the second pass rather than held).
+// (commkit/_cuda/src/ldpc.cu:45-72), with Q and the columns kept in
+// registers between them.
 template <int DMAX, class ColOf>
 __device__ __forceinline__ void min_sum_row(float* __restrict__ a, const int deg,
                                             const ColOf& col_of, float& m1, float& m2,
@@ -24,15 +24,19 @@ __device__ __forceinline__ void min_sum_row(float* __restrict__ a, const int deg
     const uint32_t osign = w;
     const float om1 = m1, om2 = m2;
     float q[DMAX];
+    int col[DMAX];  // loaded once, all before the first posterior load
     float min1 = ck::inf_f(), min2 = ck::inf_f();
     uint32_t idx = 31u;  // no edge; matches the reference's -1 when every |Q| is inf
     uint32_t negs = 0u;
+#pragma unroll
+    for (int e = 0; e < DMAX; ++e)
+        if (e < deg) col[e] = col_of(e);
 #pragma unroll
     for (int e = 0; e < DMAX; ++e) {
         if (e < deg) {
             const float r_old =
                 flip_sign(static_cast<uint32_t>(e) == oidx ? om2 : om1, (osign >> e) & 1u);
-            const float qe = __fsub_rn(a[col_of(e)], r_old);
+            const float qe = __fsub_rn(a[col[e]], r_old);
             q[e] = qe;
             negs |= (qe < 0.0f ? 1u : 0u) << e;
             const float mag = fabsf(qe);
@@ -49,7 +53,7 @@ __device__ __forceinline__ void min_sum_row(float* __restrict__ a, const int deg
     for (int e = 0; e < DMAX; ++e) {
         if (e < deg) {
             const float rn = flip_sign(static_cast<uint32_t>(e) == idx ? n2 : n1, (signs >> e) & 1u);
-            a[col_of(e)] = __fadd_rn(q[e], rn);
+            a[col[e]] = __fadd_rn(q[e], rn);
         }
     }
     m1 = n1;

@@ -95,12 +95,16 @@ struct SumProductState {
                                             const int deg, const int32_t e0,
                                             const ColOf& col_of) const {
         float q[DMAX], ph[DMAX];
+        int col[DMAX];  // loaded once, all before the first posterior load
         float total = 0.0f;
         bool neg = false;
 #pragma unroll
+        for (int e = 0; e < DMAX; ++e)
+            if (e < deg) col[e] = col_of(e);
+#pragma unroll
         for (int e = 0; e < DMAX; ++e) {
             if (e < deg) {
-                const float qe = __fsub_rn(a[col_of(e)], ld(static_cast<uint32_t>(e0 + e)));
+                const float qe = __fsub_rn(a[col[e]], ld(static_cast<uint32_t>(e0 + e)));
                 q[e] = qe;
                 neg ^= qe < 0.0f;
                 ph[e] = phi(fabsf(qe));
@@ -112,7 +116,7 @@ struct SumProductState {
             if (e < deg) {
                 const float mag = phi(__fsub_rn(total, ph[e]));
                 const float rn = (neg != (q[e] < 0.0f)) ? -mag : mag;
-                a[col_of(e)] = __fadd_rn(q[e], rn);
+                a[col[e]] = __fadd_rn(q[e], rn);
                 st(static_cast<uint32_t>(e0 + e), rn);
             }
         }
