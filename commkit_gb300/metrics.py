@@ -63,19 +63,36 @@ def _report(v: Any, was_1d: bool) -> float | np.ndarray:
     return float(out[0]) if was_1d else out
 
 
+def _array_only(noise_var: Any, esn0_db: Any, name: str) -> None:
+    """``noise_var``/``esn0_db`` demap a Signal's symbols in the reference;
+    LLR arrays already contain the noise (``commkit/metrics/information.py:
+    64-68``)."""
+    if noise_var is not None or esn0_db is not None:
+        raise ValueError(f"{name}: noise_var and esn0_db are for Signal input; LLR arrays "
+                         "already contain the noise.")  # fmt: skip
+
+
 def gmi(llrs: Any, reference: Any = None, *, constellation: Constellation | None = None,
+        noise_var: float | None = None, esn0_db: float | None = None, method: str = "maxlog",
         num_skip_symbols: int = 0) -> float | np.ndarray:  # fmt: skip
     """Generalized mutual information in bits per symbol
     (``commkit/metrics/information.py:90-166``): ``H(X) - sum_b E[log2(1 +
     e^{-(1-2c_b) L_b})]`` for LLRs ``(N k,)`` (a float) or ``(C, N k)``
-    (``(C,)``) on a CUDA device, with the transmitted ``reference`` bits."""
+    (``(C,)``) on a CUDA device, with the transmitted ``reference`` bits.
+    ``noise_var``, ``esn0_db`` and ``method`` belong to the reference's
+    Signal input (received symbols), which this package does not take: with
+    an LLR array, ``noise_var``/``esn0_db`` raise ``ValueError`` as there."""
+    _array_only(noise_var, esn0_db, "gmi()")
     loss, c, was_1d = _loss(llrs, reference, constellation, num_skip_symbols, "gmi()")
     k = c.bits_per_symbol
     return _report(k * (c.entropy / k - loss), was_1d)
 
 
 def ngmi(llrs: Any, reference: Any = None, *, constellation: Constellation | None = None,
+         noise_var: float | None = None, esn0_db: float | None = None, method: str = "maxlog",
          num_skip_symbols: int = 0) -> float | np.ndarray:  # fmt: skip
-    """Normalized GMI, ``1 - loss`` (``commkit/metrics/information.py:169-236``)."""
+    """Normalized GMI, ``1 - loss`` (``commkit/metrics/information.py:169-236``);
+    the arguments as for :func:`gmi`."""
+    _array_only(noise_var, esn0_db, "ngmi()")
     loss, _, was_1d = _loss(llrs, reference, constellation, num_skip_symbols, "ngmi()")
     return _report(1.0 - loss, was_1d)

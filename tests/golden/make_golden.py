@@ -36,6 +36,8 @@ Every output here is the reference's own result on seeded inputs:
   (``--only=dvbs2``);
 * ``gmi_golden.npz``: the reference's ``gmi`` / ``ngmi`` of seeded 16-QAM,
   8-PSK and shaped 64-QAM LLRs (``--only=gmi``);
+* ``api_signatures.json``: parameter names, kinds and defaults of the
+  reference's public calls on this path (``--only=api``);
 * ``ldpc_nonfinite.npz``: min-sum on LLRs with infinities and a NaN,
   DVB-S2 short 1/2 and PON (``--only=nonfinite``).
 
@@ -475,8 +477,48 @@ SP_CASES = (
 )
 
 
+API_CALLABLES = (
+    ("mapping", "compute_llr"), ("coding", "decode"), ("coding", "encode"), ("metrics", "gmi"),
+    ("metrics", "ngmi"), ("coding", "error_rate_curve"), ("mapping", "Constellation.llr"),
+    ("mapping", "Constellation.qam"), ("mapping", "Constellation.psk"), ("mapping", "Constellation.pam"),
+    ("mapping", "Constellation.shaped"), ("mapping", "Constellation"), ("coding", "LDPCCode"),
+    ("coding", "LDPCCode.quasi_cyclic"), ("coding", "MinSum"), ("coding", "SumProduct"),
+)  # fmt: skip
+
+
+def api_signatures(ref: str) -> dict:
+    """Parameter names, kinds and defaults of the reference's public calls on
+    this path (the drop-in surface), for the signature test."""
+    import importlib
+    import inspect
+
+    _import_reference(ref)
+    out = {}
+    for mod, name in API_CALLABLES:
+        obj = importlib.import_module(f"commkit.{mod}")
+        for part in name.split("."):
+            obj = getattr(obj, part)
+        params = []
+        for pname, prm in inspect.signature(obj).parameters.items():
+            if pname == "self":
+                continue
+            default = None if prm.default is inspect.Parameter.empty else repr(prm.default)
+            params.append([pname, prm.kind.name, default])
+        out[f"{mod}.{name}"] = params
+    return out
+
+
 def main(ref: str, only: str | None = None) -> None:
     t0 = time.time()
+    if only == "api":
+        import json
+        import multiprocessing as mp
+
+        with ProcessPoolExecutor(max_workers=1, mp_context=mp.get_context("spawn")) as pool:
+            res = pool.submit(api_signatures, ref).result()
+        (HERE / "api_signatures.json").write_text(json.dumps(res, indent=1) + "\n")
+        print(f"API signatures written in {time.time() - t0:.0f} s")
+        return
     if only == "dvbs2":
         import multiprocessing as mp
 
