@@ -45,6 +45,8 @@ EXPORTS = (
     "ck_llr_points_frames",
     "ck_random_bits",
     "ck_ldpc_encode",
+    "ck_ldpc_encode_generator",
+    "ck_ldpc_column_signs",
     "ck_map_awgn",
     "ck_count_errors",
     "ck_gmi_loss",
@@ -155,6 +157,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         "ck_llr_points_frames": ([p, i64, i64, p, p, p, p, i32, i32, i32, p, p], ctypes.c_int),
         "ck_random_bits": ([p, i64, ctypes.c_uint64, ctypes.c_uint64, p], ctypes.c_int),
         "ck_ldpc_encode": ([p, i64, i32, i32, i32, p, p, i32, p, p, ctypes.c_size_t, p, p], ctypes.c_int),
+        "ck_ldpc_encode_generator": ([p, i64, i32, i32, i32, p, p, p, p, ctypes.c_size_t, p, p], ctypes.c_int),
+        "ck_ldpc_column_signs": ([p, i64, i32, p, i32, p, p], ctypes.c_int),
         "ck_map_awgn": ([p, i64, i32, p, ctypes.c_float, ctypes.c_float, ctypes.c_uint64, ctypes.c_uint64, p, p],
                         ctypes.c_int),
         "ck_count_errors": ([p, p, p, p, i64, i32, i32, p, p, p, p], ctypes.c_int),

@@ -156,9 +156,27 @@ class LDPCCode:
 
     @cached_property
     def k(self) -> int:
-        """Information bits per codeword: N - m (the parity part is invertible)."""
-        _require_invertible_parity(self)
-        return self.num_variables - self.num_checks
+        """Information bits per codeword: N - rank(H) (``ldpc.py:122-125``)."""
+        return int(self._info.size)
+
+    @cached_property
+    def _info(self) -> np.ndarray:
+        """The information columns, increasing (``commkit/coding/ldpc.py:445-481``):
+        the first N - m when the parity part (the last m columns) is
+        invertible, else the columns that are not pivots of H's reduced row
+        echelon form with pivots taken from the last column backwards."""
+        m, n = self.num_checks, self.num_variables
+        if _parity_invertible(self):
+            info = np.arange(n - m, dtype=np.int64)
+        else:
+            info = _generator(self)[0].astype(np.int64)
+        info.setflags(write=False)
+        return info
+
+    @property
+    def _leading_info(self) -> bool:
+        """True when the information columns are the first k."""
+        return self.k == 0 or int(self._info[-1]) == self.k - 1
 
     @property
     def rate(self) -> float:
@@ -202,21 +220,33 @@ class LDPCCode:
         return plan
 
 
-# Largest parity part encoded through a dense inverse (the reference's
-# _MAX_INVERSE, commkit/coding/ldpc.py:46).
+# Largest parity part encoded through a dense inverse, and largest H reduced
+# to a systematic generator (the reference's _MAX_INVERSE and _MAX_DENSE,
+# commkit/coding/ldpc.py:46-48).
 _MAX_INVERSE = 8192
+_MAX_DENSE = 1 << 27
 
 
 @dataclass(frozen=True)
 class _Encoder:
     """Information columns of H as CSR (``info_row_ptr``, ``info_cols``) and
     the parity part: an accumulator of ``stride`` (``p_j = s_j + p_{j-stride}``)
-    or the packed rows of ``H_p^-1`` (``inverse``, ``(m, ceil(m/32))`` uint32)."""
+    or the packed rows of ``H_p^-1`` (``inverse``, ``(m, ceil(m/32))`` uint32);
+    or, for a parity part that is not invertible, ``generator`` =
+    ``(info columns, pivot columns, packed generator rows)`` of
+    :func:`_generator`, with the CSR empty and ``stride`` 0."""
 
     info_row_ptr: np.ndarray
     info_cols: np.ndarray
     stride: int
     inverse: np.ndarray | None
+    generator: tuple | None = None
+
+    def scratch_bytes(self, R: int, m: int, k: int) -> int:
+        """Device scratch that encoding ``R`` frames takes."""
+        if self.generator is not None:
+            return 4 * R * ((k + 31) // 32)
+        return R * m + (4 * R * ((m + 31) // 32) + 4 if self.inverse is not None else 0)
 
 
 def _build_encoder(code: LDPCCode) -> _Encoder:
@@ -241,12 +271,10 @@ def _build_encoder(code: LDPCCode) -> _Encoder:
     want = np.sort(np.concatenate([c * m + c, (c[c + g < m] + g) * m + c[c + g < m]]))
     if got.size == want.size and np.array_equal(got, want):
         return _Encoder(row_ptr, info_cols, g, None)
-    if m > _MAX_INVERSE:
-        raise NotImplementedError(
-            f"encode(): the parity part of {code!r} is not an accumulator and m = {m} is above "
-            f"{_MAX_INVERSE}; the device encoder takes accumulators and inverses only"
-        )  # fmt: skip
-    return _Encoder(row_ptr, info_cols, 0, _gf2_inverse_packed(pr, pc, m))
+    if m <= _MAX_INVERSE and _parity_invertible(code):
+        return _Encoder(row_ptr, info_cols, 0, _gf2_inverse_packed(pr, pc, m))
+    empty = np.zeros(1, np.int32)
+    return _Encoder(empty, empty[:0], 0, None, _generator(code))
 
 
 def _gf2_inverse_packed(pr: np.ndarray, pc: np.ndarray, m: int) -> np.ndarray:
@@ -275,11 +303,13 @@ def _gf2_inverse_packed(pr: np.ndarray, pc: np.ndarray, m: int) -> np.ndarray:
     return np.ascontiguousarray(inv32[:, : (m + 31) // 32])
 
 
-def _require_invertible_parity(code: LDPCCode) -> None:
-    """Raise unless the parity part ``H_p`` (last m columns) is invertible over GF(2).
+def _parity_invertible(code: LDPCCode) -> bool:
+    """Whether the parity part ``H_p`` (last m columns) is invertible over GF(2).
 
     Lower triangular with a unit diagonal (dual-diagonal / accumulate parts)
-    is settled from the edges; otherwise by elimination on packed bits.
+    is settled from the edges; otherwise by elimination on packed bits, for
+    m up to 16384 (a larger H is beyond the generator's size limit as well,
+    so the answer "no" then ends in :func:`_generator`'s ``ValueError``).
     """
     m, n = code.num_checks, code.num_variables
     k = n - m
@@ -289,9 +319,9 @@ def _require_invertible_parity(code: LDPCCode) -> None:
     diag = np.zeros(m, bool)
     diag[pr[pr == pc]] = True
     if diag.all() and not np.any(pc > pr):
-        return
+        return True
     if m > 16384:
-        raise NotImplementedError(f"parity part of {m} checks is not triangular; rank test too large")
+        return False
     words = (m + 63) // 64
     mat = np.zeros((m, words), np.uint64)
     np.bitwise_or.at(mat, (pr, pc // 64), np.left_shift(np.uint64(1), (pc % 64).astype(np.uint64)))
@@ -300,13 +330,73 @@ def _require_invertible_parity(code: LDPCCode) -> None:
         w, bit = c // 64, np.uint64(1) << np.uint64(c % 64)
         hits = np.flatnonzero(mat[r:, w] & bit)
         if hits.size == 0:
-            raise NotImplementedError("the parity part of H is singular; such codes are not supported")
+            return False
         piv = r + hits[0]
         if piv != r:
             mat[[r, piv]] = mat[[piv, r]]
         below = r + 1 + np.flatnonzero(mat[r + 1 :, w] & bit)
         mat[below] ^= mat[r]
         r += 1
+    return True
+
+
+def _generator(code: LDPCCode) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """``(info, pivots, gen)`` of H's reduced row echelon form over GF(2),
+    pivot columns chosen from the last column backwards (the reference's
+    ``row_reduce(h, reverse=True)``, ``commkit/coding/_gf2.py:45-88``, as its
+    "dense" encoder uses it, ``commkit/coding/ldpc.py:476-481``).
+
+    ``pivots`` (rank,) int32 is the pivot column of each reduced row and
+    ``info`` (N - rank,) int32 the other columns, increasing; codeword bit
+    ``pivots[i]`` is the GF(2) sum of the information bits where reduced row
+    i has a one.  ``gen`` packs those rows over the information columns,
+    ``(rank, ceil(k/32))`` uint32 (information bit j at bit j % 32 of word
+    j // 32).  Column j is a pivot exactly when it is independent of the
+    columns to its right, so the split does not depend on how the
+    elimination is carried out.  Cached on the code.
+    """
+    got = code.__dict__.get("_generator_tables")
+    if got is not None:
+        return got
+    m, n = code.num_checks, code.num_variables
+    if m * n > _MAX_DENSE:
+        raise ValueError(
+            f"LDPCCode ({m} x {n}): the parity part is neither dual-diagonal nor "
+            "invertible, and H is too large for a dense systematic generator."
+        )
+    words = (n + 63) // 64
+    one = np.uint64(1)
+    h = np.zeros((m, words), np.uint64)
+    cols = code.variables.astype(np.int64)
+    np.bitwise_or.at(h, (code.checks.astype(np.int64), cols // 64), np.left_shift(one, (cols % 64).astype(np.uint64)))
+    pivots: list[int] = []
+    r = 0
+    for col in range(n - 1, -1, -1):
+        if r == m:
+            break
+        w, bit = col // 64, one << np.uint64(col % 64)
+        hits = np.flatnonzero(h[r:, w] & bit)
+        if hits.size == 0:
+            continue
+        piv = r + int(hits[0])
+        if piv != r:
+            h[[r, piv]] = h[[piv, r]]
+        others = np.flatnonzero(h[:, w] & bit)
+        h[others[others != r]] ^= h[r]
+        pivots.append(col)
+        r += 1
+    piv = np.asarray(pivots, np.int32)
+    info = np.setdiff1d(np.arange(n, dtype=np.int32), piv)
+    dense = np.unpackbits(h[:r].view(np.uint8), axis=1, bitorder="little")[:, :n]
+    k = info.size
+    sel = np.zeros((r, (k + 31) // 32 * 32), np.uint8)
+    sel[:, :k] = dense[:, info]
+    gen = np.packbits(sel, axis=1, bitorder="little").view(np.uint32)
+    for a in (info, piv, gen):
+        a.setflags(write=False)
+    out = (info, piv, np.ascontiguousarray(gen))
+    code.__dict__["_generator_tables"] = out
+    return out
 
 
 class _Plan:
@@ -435,6 +525,12 @@ def decode(llrs: Any, *, code: LDPCCode, method: MinSum | SumProduct | None = No
     blocks = x2.reshape(rows, code.n)
     xd = _device.wrap(blocks, "llrs")
     k = code.k
+    leading = code._leading_info
+    if not leading and int(code._info[-1]) >= code.n:
+        raise NotImplementedError(
+            f"decode(): {code!r} has information columns among its punctured bits, which the "
+            "a-posteriori LLRs do not hold"
+        )  # fmt: skip
     out_llrs = _device.empty(xd, (rows, code.n), np.float32)
     bits = _device.empty(xd, (rows, k), np.int8)
     iters = _device.empty(xd, (rows,), np.int32)
@@ -454,10 +550,18 @@ def decode(llrs: Any, *, code: LDPCCode, method: MinSum | SumProduct | None = No
                 plan.handle, xd.ptr, _device.wrap(out_llrs).ptr, rows, code.n,
                 rule, scale, offset,
                 int(method.max_iterations), 1 if method.early_stop else 0,
-                _device.wrap(iters).ptr, _device.wrap(valid_u8).ptr, _device.wrap(bits).ptr, k,
+                _device.wrap(iters).ptr, _device.wrap(valid_u8).ptr,
+                _device.wrap(bits).ptr if leading else None, k if leading else 0,
                 ws_ptr, ws_bytes, stream,
             )  # fmt: skip
             _lib.check(st, "decode()")
+            if not leading:
+                # Hard decisions at the information columns (ldpc.py:582-586).
+                st = _lib.lib().ck_ldpc_column_signs(
+                    _device.wrap(out_llrs).ptr, rows, code.n, _device.wrap(_info_columns(code, xd)).ptr, k,
+                    _device.wrap(bits).ptr, stream,
+                )  # fmt: skip
+                _lib.check(st, "decode() bits")
     valid = valid_u8.view(_bool_dtype(xd))
 
     def shaped(a, size):
@@ -474,16 +578,39 @@ def _encoder_tables(code: LDPCCode, like: _device.DeviceArray) -> tuple:
     t = per.get(like.device)
     if t is None:
         e = code._encoder
-        inv = None if e.inverse is None else _device.to_device(like, e.inverse.view(np.int32))
-        t = per[like.device] = (_device.to_device(like, e.info_row_ptr), _device.to_device(like, e.info_cols), inv)
+        if e.generator is not None:
+            info, piv, gen = e.generator
+            t = (_device.to_device(like, info), _device.to_device(like, piv),
+                 _device.to_device(like, gen.view(np.int32)))  # fmt: skip
+        else:
+            inv = None if e.inverse is None else _device.to_device(like, e.inverse.view(np.int32))
+            t = (_device.to_device(like, e.info_row_ptr), _device.to_device(like, e.info_cols), inv)
+        per[like.device] = t
     return t
+
+
+def _info_columns(code: LDPCCode, like: _device.DeviceArray):
+    """The information columns as int32 on ``like``'s device, cached."""
+    per = code.__dict__.setdefault("_info_dev", {})
+    t = per.get(like.device)
+    if t is None:
+        t = per[like.device] = _device.to_device(like, code._info.astype(np.int32))
+    return t
+
+
+def _require_leading_info(code: LDPCCode, what: str) -> None:
+    if not code._leading_info:
+        raise NotImplementedError(
+            f"{what}: the information columns of {code!r} are not the first k (its parity part is not "
+            "invertible); decode() and encode() take such codes"
+        )  # fmt: skip
 
 
 def encode_blocks(code: LDPCCode, info: Any, words: Any = None, scratch: Any = None) -> Any:
     """``(R, k)`` int8 information rows on a CUDA device to ``(R, n)`` int8
     codewords, systematic (``commkit/coding/ldpc.py:511-536``).  ``words``
-    and ``scratch`` (int8, ``R m`` bytes, plus ``4 R ceil(m/32) + 4`` for an
-    inverse encoder) may be preallocated."""
+    and ``scratch`` (int8, ``code._encoder.scratch_bytes(R, m, k)`` bytes)
+    may be preallocated."""
     xd = _device.wrap(info, "info")
     _device.check(xd, "info", np.int8, (None, code.k))
     R = xd.shape[0]
@@ -495,16 +622,22 @@ def encode_blocks(code: LDPCCode, info: Any, words: Any = None, scratch: Any = N
     if R == 0:
         return words
     e = code._encoder
-    need = R * m + (4 * R * ((m + 31) // 32) + 4 if e.inverse is not None else 0)
     if scratch is None:
-        scratch = _device.empty(xd, (need,), np.int8)
+        scratch = _device.empty(xd, (e.scratch_bytes(R, m, k),), np.int8)
     sd = _device.wrap(scratch, "scratch")
     with _device.on_device(xd):
-        rp, ci, inv = _encoder_tables(code, xd)
-        st = _lib.lib().ck_ldpc_encode(
-            xd.ptr, R, k, m, n, _device.wrap(rp).ptr, _device.wrap(ci).ptr, e.stride,
-            None if inv is None else _device.wrap(inv).ptr, sd.ptr, sd.size, wd.ptr, _device.stream_of(xd),
-        )  # fmt: skip
+        if e.generator is not None:
+            info_cols, piv, gen = _encoder_tables(code, xd)
+            st = _lib.lib().ck_ldpc_encode_generator(
+                xd.ptr, R, k, e.generator[1].size, n, _device.wrap(info_cols).ptr, _device.wrap(piv).ptr,
+                _device.wrap(gen).ptr, sd.ptr, sd.size, wd.ptr, _device.stream_of(xd),
+            )  # fmt: skip
+        else:
+            rp, ci, inv = _encoder_tables(code, xd)
+            st = _lib.lib().ck_ldpc_encode(
+                xd.ptr, R, k, m, n, _device.wrap(rp).ptr, _device.wrap(ci).ptr, e.stride,
+                None if inv is None else _device.wrap(inv).ptr, sd.ptr, sd.size, wd.ptr, _device.stream_of(xd),
+            )  # fmt: skip
         _lib.check(st, "encode()")
     return words
 
@@ -514,7 +647,9 @@ def encode(bits: Any, *, code: LDPCCode) -> Any:
 
     ``bits`` ``(N,)`` or ``(C, N)`` integers 0/1 on a CUDA device, ``N`` a
     multiple of ``code.k``; returns int8 ``(..., N / k * n)`` on the same
-    device, each block ``[info | parity]`` (punctured parity bits left out).
+    device, each block ``[info | parity]`` (punctured parity bits left out),
+    or, for a code whose parity part is not invertible, the information bits
+    at ``code``'s information columns and the parity bits at the others.
     """
     if not isinstance(code, LDPCCode):
         raise TypeError(f"encode(): code must be an LDPCCode, got {type(code).__name__}.")
@@ -569,6 +704,7 @@ def decode_mixed(batches, *, workspace: Any = None, outputs: list | None = None)
     for llrs, code, method in batches:
         if not isinstance(code, LDPCCode):
             raise TypeError(f"decode_mixed(): code must be an LDPCCode, got {type(code).__name__}.")
+        _require_leading_info(code, "decode_mixed()")
         method = _resolve_method(method)
         if not isinstance(method, MinSum):
             raise NotImplementedError("decode_mixed(): mixed launches decode with MinSum; decode "

@@ -203,6 +203,50 @@ __global__ void copy_info_kernel(const int8_t* __restrict__ info, int64_t B, int
     }
 }
 
+// Systematic generator encoding: information bit j of a frame goes to
+// column cols[j], and bit i of the parity (a GF(2) product of generator row
+// i with the packed information bits) to column pivots[i].  Columns at or
+// beyond n (punctured) are not written.
+__global__ void scatter_info_kernel(const int8_t* __restrict__ info, int64_t B, int32_t k, int32_t n,
+                                    const int32_t* __restrict__ cols, int8_t* __restrict__ words) {
+    const uint64_t total = static_cast<uint64_t>(B) * k;
+    for (uint64_t t = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; t < total;
+         t += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const uint64_t f = t / k;
+        const int32_t c = cols[t - f * k];
+        if (c < n) words[f * n + c] = info[t];
+    }
+}
+
+__global__ void generator_kernel(const uint32_t* __restrict__ packed_u, const uint32_t* __restrict__ gen,
+                                 int64_t B, int32_t rank, int32_t words_per, int32_t n,
+                                 const int32_t* __restrict__ pivots, int8_t* __restrict__ words) {
+    const uint64_t total = static_cast<uint64_t>(B) * rank;
+    for (uint64_t t = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; t < total;
+         t += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const uint64_t f = t / rank;
+        const int32_t i = static_cast<int32_t>(t - f * rank);
+        const int32_t c = pivots[i];
+        if (c >= n) continue;
+        const uint32_t* row = gen + static_cast<uint64_t>(i) * words_per;
+        const uint32_t* u = packed_u + f * words_per;
+        uint32_t par = 0;
+        for (int32_t w = 0; w < words_per; ++w) par ^= __popc(row[w] & u[w]);
+        words[f * n + c] = static_cast<int8_t>(par & 1u);
+    }
+}
+
+// Hard decisions at chosen columns: bits[f, j] = (llrs[f, cols[j]] < 0).
+__global__ void column_signs_kernel(const float* __restrict__ llrs, int64_t B, int32_t n,
+                                    const int32_t* __restrict__ cols, int32_t k, int8_t* __restrict__ bits) {
+    const uint64_t total = static_cast<uint64_t>(B) * k;
+    for (uint64_t t = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; t < total;
+         t += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const uint64_t f = t / k;
+        bits[t] = static_cast<int8_t>(llrs[f * n + cols[t - f * k]] < 0.0f);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Map + AWGN: symbol i takes bits [i kb, (i + 1) kb) of the record (MSB
 // first) as the label of a point; noise from Philox counter i of `stream`.
@@ -378,6 +422,46 @@ extern "C" int ck_ldpc_encode(const int8_t* info, int64_t B, int32_t k, int32_t 
                                                                                    words);
     }
     return ck::cuda_check(cudaGetLastError(), "encoder launch");
+}
+
+extern "C" int ck_ldpc_encode_generator(const int8_t* info, int64_t B, int32_t k, int32_t rank, int32_t n,
+                                        const int32_t* info_cols, const int32_t* pivot_cols,
+                                        const uint32_t* gen, int8_t* scratch, size_t scratch_bytes,
+                                        int8_t* words, void* stream) {
+    ck::clear_error();
+    if (B < 0 || k < 1 || rank < 1 || n < 1 || n > k + rank)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "bad sizes (B=%lld k=%d rank=%d n=%d)",
+                        static_cast<long long>(B), k, rank, n);
+    if (B == 0) return CK_OK;
+    if (!info || !words || !info_cols || !pivot_cols || !gen || !scratch)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "an array is NULL");
+    const int32_t words_per = (k + 31) / 32;
+    const size_t need = static_cast<size_t>(B) * words_per * 4;
+    if (scratch_bytes < need)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "scratch of %zu bytes, %zu needed", scratch_bytes, need);
+    if (reinterpret_cast<uintptr_t>(scratch) % 4)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "scratch must be 4-byte aligned");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    uint32_t* packed = reinterpret_cast<uint32_t*>(scratch);
+    scatter_info_kernel<<<grid_for(static_cast<uint64_t>(B) * k), kThreads, 0, st>>>(info, B, k, n, info_cols,
+                                                                                     words);
+    pack_kernel<<<grid_for(static_cast<uint64_t>(B) * words_per), kThreads, 0, st>>>(info, B, k, words_per,
+                                                                                     packed);
+    generator_kernel<<<grid_for(static_cast<uint64_t>(B) * rank), kThreads, 0, st>>>(packed, gen, B, rank,
+                                                                                     words_per, n, pivot_cols,
+                                                                                     words);
+    return ck::cuda_check(cudaGetLastError(), "generator encoder launch");
+}
+
+extern "C" int ck_ldpc_column_signs(const float* llrs, int64_t B, int32_t n, const int32_t* cols, int32_t k,
+                                    int8_t* bits, void* stream) {
+    ck::clear_error();
+    if (B < 0 || n < 1 || k < 0) return ck::fail(CK_ERR_INVALID_ARGUMENT, "bad sizes");
+    if (B == 0 || k == 0) return CK_OK;
+    if (!llrs || !cols || !bits) return ck::fail(CK_ERR_INVALID_ARGUMENT, "an array is NULL");
+    column_signs_kernel<<<grid_for(static_cast<uint64_t>(B) * k), kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+        llrs, B, n, cols, k, bits);
+    return ck::cuda_check(cudaGetLastError(), "column signs launch");
 }
 
 extern "C" int ck_map_awgn(const int8_t* bits, int64_t n_sym, int32_t bits_per_symbol,

@@ -158,10 +158,8 @@ class LinkBatch:
 
         by_label[_packed(c.bit_labels)] = c.points.astype(np.complex64)
         self.points = torch.from_numpy(by_label).to(dev)
-        e = code._encoder
-        m = code.num_checks
-        self.scratch = torch.empty(self.blocks * m + (4 * self.blocks * ((m + 31) // 32) + 4 if e.inverse is not None
-                                                      else 0), dtype=torch.int8, device=dev)  # fmt: skip
+        self.scratch = torch.empty(code._encoder.scratch_bytes(self.blocks, code.num_checks, code.k),
+                                   dtype=torch.int8, device=dev)
         self.ws = torch.empty(max(code._plan(dev.index).workspace_size(
             self.blocks, _lib.CK_LDPC_SUM_PRODUCT if isinstance(self.method, SumProduct) else _lib.CK_LDPC_MIN_SUM),
             256), dtype=torch.uint8, device=dev)  # fmt: skip

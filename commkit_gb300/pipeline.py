@@ -31,7 +31,7 @@ from typing import Any
 import numpy as np
 
 from . import _device, _lib
-from .coding import DecodeResult, LDPCCode, MinSum, decode_mixed
+from .coding import DecodeResult, LDPCCode, MinSum, _require_leading_info, decode_mixed
 from .mapping import Constellation, _axis_struct, _table_kind, compute_llr_frames, device_tables, inv_s2_frames
 
 
@@ -63,6 +63,7 @@ class MixedReceiver:
         self.lpt = bool(lpt)
         for s in slots:
             k = s.constellation.bits_per_symbol
+            _require_leading_info(s.code, "MixedReceiver")
             if s.code.n % k:
                 raise ValueError(f"n = {s.code.n} is not a multiple of {k} bits per symbol")
             S = s.code.n // k

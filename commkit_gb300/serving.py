@@ -40,7 +40,7 @@ from typing import Any
 import numpy as np
 
 from . import _lib
-from .coding import LDPCCode, MinSum
+from .coding import LDPCCode, MinSum, _require_leading_info
 from .mapping import Constellation
 
 # Largest piece of one request's symbols a gather block copies (so one big
@@ -193,6 +193,8 @@ class Server:
 
         self.torch = torch
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        for code in codes.values():
+            _require_leading_info(code, "Server")
         self.codes = codes
         self.method = method
         self.orders = tuple(orders)

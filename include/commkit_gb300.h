@@ -174,6 +174,29 @@ int ck_ldpc_encode(const int8_t* info, int64_t B, int32_t k, int32_t m, int32_t 
                    void* stream);
 
 /*
+ * Encoding through a systematic generator, for parity-check matrices whose
+ * last m columns are not invertible (the reference's "dense" kind,
+ * commkit/coding/ldpc.py:476-481 and :511-533): information bit j goes to
+ * column info_cols[j] (k of them, increasing) and parity bit i, the GF(2)
+ * product of gen row i with the information bits, to column pivot_cols[i]
+ * (rank of them).  gen is (rank, ceil(k/32)) uint32, row i bit j = entry
+ * (i, info_cols[j]) of the reduced row echelon form of H.  Columns >= n
+ * (punctured) are not written.  scratch: 4 B ceil(k/32) bytes, 4-aligned.
+ */
+int ck_ldpc_encode_generator(const int8_t* info, int64_t B, int32_t k, int32_t rank, int32_t n,
+                             const int32_t* info_cols, const int32_t* pivot_cols, const uint32_t* gen,
+                             int8_t* scratch, size_t scratch_bytes, int8_t* words, void* stream);
+
+/*
+ * Hard decisions at chosen columns: bits (B, k) int8 with
+ * bits[f, j] = (llrs[f, cols[j]] < 0), llrs (B, n) float32, every
+ * cols[j] < n.  The decoder's bits for codes whose information columns are
+ * not the first k (commkit/coding/ldpc.py:582-586).
+ */
+int ck_ldpc_column_signs(const float* llrs, int64_t B, int32_t n, const int32_t* cols, int32_t k,
+                         int8_t* bits, void* stream);
+
+/*
  * Symbols (n_sym,) complex64 of a bit record: symbol i is the point whose
  * label is bits [i b, (i + 1) b) (MSB first), b = bits_per_symbol, plus
  * Gaussian noise of standard deviation std_re / std_im per component

@@ -39,7 +39,12 @@ Every output here is the reference's own result on seeded inputs:
 * ``api_signatures.json``: parameter names, kinds and defaults of the
   reference's public calls on this path (``--only=api``);
 * ``ldpc_nonfinite.npz``: min-sum on LLRs with infinities and a NaN,
-  DVB-S2 short 1/2 and PON (``--only=nonfinite``).
+  DVB-S2 short 1/2 and PON (``--only=nonfinite``);
+* ``ldpc_generator.npz``: three codes whose parity part is not invertible
+  (a cycle-free code, a random code with a redundant check, a circulant
+  code whose block columns have weight two), with the reference's ``k``,
+  information and pivot columns, encodings of seeded words and min-sum
+  decodes (``--only=generator``).
 
 Large outputs are stored as SHA-256 digests of their bytes (negative zeros
 folded to +0) plus their first frame; inputs drawn from ``default_rng``
@@ -508,8 +513,88 @@ def api_signatures(ref: str) -> dict:
     return out
 
 
+def generator_codes() -> dict:
+    """``name -> (checks, variables, m, N)`` of the three seeded codes of
+    ``ldpc_generator.npz``, each with a parity part that is not invertible."""
+    out = {}
+    tree = [[0, 1, 3], [3, 4, 5], [1, 2, 6], [5, 7, 8]]
+    r = np.concatenate([[i] * len(row) for i, row in enumerate(tree)])
+    out["tree"] = (r, np.concatenate(tree), 4, 9)
+    # 23 random checks on 48 bits (column weight 2 or 3), then their first
+    # two rows' sum as a 24th check: rank 23 at most.
+    rng = np.random.default_rng(21)
+    m, n = 23, 48
+    h = np.zeros((m + 1, n), np.int8)
+    for c in range(n):
+        h[rng.choice(m, size=int(rng.integers(2, 4)), replace=False), c] = 1
+    for i in range(m):
+        while h[i].sum() < 2:
+            h[i, rng.integers(n)] = 1
+    h[m] = h[0] ^ h[1]
+    assert h[m].sum() >= 2
+    rr, cc = np.nonzero(h)
+    out["redundant"] = (rr, cc, m + 1, n)
+    # Circulant code, 4 x 8 base, Z = 8: every block column has two shifted
+    # identities, so the block rows sum to zero and H has rank < m.
+    rng = np.random.default_rng(22)
+    base = -np.ones((4, 8), np.int64)
+    while (base >= 0).sum(1).min() < 2:  # every check needs two bits
+        base[:] = -1
+        for j in range(8):
+            base[rng.choice(4, size=2, replace=False), j] = rng.integers(0, 8, size=2)
+    z = 8
+    bi, bj = np.nonzero(base >= 0)
+    lift = np.arange(z)
+    rr = (bi[:, None] * z + lift).ravel()
+    cc = (bj[:, None] * z + (lift + base[bi, bj][:, None]) % z).ravel()
+    out["qc_even"] = (rr, cc, 4 * z, 8 * z)
+    return out
+
+
+def generator_case(ref: str) -> dict:
+    """The reference on :func:`generator_codes`: ``k``, the information and
+    pivot columns of its "dense" encoder (``commkit/coding/ldpc.py:476-481``),
+    ``encode`` of 5 seeded words (``default_rng(31)``) and ``MinSum()``
+    decodes of 4 frames of ``2 + 1.5 N(0,1)`` (``default_rng(32)``, the
+    all-zero word)."""
+    _import_reference(ref)
+    from commkit.coding import LDPCCode, MinSum, decode, encode
+
+    out = {}
+    for name, (rows, cols, m, n) in generator_codes().items():
+        code = LDPCCode(np.asarray(rows, np.int64), np.asarray(cols, np.int64), m, n)
+        enc = code._encoder
+        out[f"{name}_checks"] = np.asarray(rows, np.int32)
+        out[f"{name}_variables"] = np.asarray(cols, np.int32)
+        out[f"{name}_m"] = np.int32(m)
+        out[f"{name}_N"] = np.int32(n)
+        out[f"{name}_kind"] = np.array(enc.kind)
+        out[f"{name}_k"] = np.int32(code.k)
+        out[f"{name}_info"] = np.asarray(enc.info, np.int32)
+        out[f"{name}_pivots"] = np.asarray(enc.parity, np.int32)
+        u = np.random.default_rng(31).integers(0, 2, size=(5, code.k)).astype(np.int8)
+        out[f"{name}_u"] = u
+        out[f"{name}_words"] = np.asarray(encode(u.reshape(-1), code=code), np.int8).reshape(5, code.n)
+        llrs = (2.0 + 1.5 * np.random.default_rng(32).standard_normal((4, code.n))).astype(np.float32)
+        out[f"{name}_llrs"] = llrs
+        res = decode(llrs.reshape(-1), code=code, method=MinSum())
+        out[f"{name}_post"] = np.asarray(res.llrs, np.float32).reshape(4, -1)
+        out[f"{name}_bits"] = np.asarray(res.bits, np.int8).reshape(4, -1)
+        out[f"{name}_valid"] = np.asarray(res.valid, bool)
+        out[f"{name}_iters"] = np.asarray(res.iterations, np.int32)
+    return out
+
+
 def main(ref: str, only: str | None = None) -> None:
     t0 = time.time()
+    if only == "generator":
+        import multiprocessing as mp
+
+        with ProcessPoolExecutor(max_workers=1, mp_context=mp.get_context("spawn")) as pool:
+            res = pool.submit(generator_case, ref).result()
+        np.savez_compressed(HERE / "ldpc_generator.npz", **res)
+        print(f"generator fixtures written in {time.time() - t0:.0f} s")
+        return
     if only == "api":
         import json
         import multiprocessing as mp
