@@ -120,6 +120,10 @@ class Batch(ctypes.Structure):
         ("bits", ctypes.c_void_p),
         ("k_bits", ctypes.c_int32),
         ("order", ctypes.c_void_p),
+        ("symbols", ctypes.c_void_p),
+        ("inv_s2", ctypes.c_void_p),
+        ("axis_re", ctypes.POINTER(AxisMaxlog)),
+        ("axis_im", ctypes.POINTER(AxisMaxlog)),
     ]
 
 

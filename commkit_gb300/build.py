@@ -42,7 +42,7 @@ def nvcc() -> str:
 
 # Kernel headers the code-specialised decoders are compiled from at run time
 # (NVRTC): embedded in the library as strings.
-JIT_HEADERS = ("ck_device.cuh", "ck_ldpc_kernel.cuh", "ck_ldpc_minsum.cuh", "ck_ldpc_mixed.cuh")
+JIT_HEADERS = ("ck_device.cuh", "ck_llr_axis.cuh", "ck_ldpc_kernel.cuh", "ck_ldpc_minsum.cuh", "ck_ldpc_mixed.cuh")
 JIT_SOURCE = BUILD / "ck_jit_headers.cpp"
 
 

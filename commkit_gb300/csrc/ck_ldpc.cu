@@ -626,8 +626,28 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
         if (b.max_iterations < 0) return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: bad max_iterations", c);
         if (b.bits && (b.k_bits < 0 || b.k_bits > b.n_in))
             return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: bad k_bits", c);
-        if (b.B > 0 && (!b.llr_in || !b.llr_out || !b.iters || !b.valid))
+        if (b.B > 0 && ((!b.llr_in && !b.symbols) || !b.llr_out || !b.iters || !b.valid))
             return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: missing arrays", c);
+        int32_t ka = 0;
+        if (b.symbols) {
+            // Fused demapping: closed-form max-log tables of a square
+            // separable constellation, 1 to 4 bits per axis.
+            if (!b.inv_s2 || !b.axis_re || !b.axis_im)
+                return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: symbols need inv_s2 and both axes", c);
+            ka = b.axis_re->k;
+            if (ka < 1 || ka > 4 || b.axis_im->k != ka || b.axis_re->L != (1 << ka) || b.axis_im->L != (1 << ka))
+                return ck::fail(CK_ERR_UNSUPPORTED, "batch %d: fused demapping takes 1 to 4 bits on each of two "
+                                "equal axes", c);
+            if (b.n_in % (2 * ka))
+                return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: n_in %d is not a multiple of %d bits per "
+                                "symbol", c, b.n_in, 2 * ka);
+            if (reinterpret_cast<uintptr_t>(b.symbols) % 8)
+                return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: symbols must be 8-byte aligned", c);
+            const ck_axis_maxlog* ax[2] = {b.axis_re, b.axis_im};
+            for (int a = 0; a < 2; ++a)
+                if (!ax[a]->levels || !ax[a]->labels || !ax[a]->lo || !ax[a]->hi || !ax[a]->pos)
+                    return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: an axis table is NULL", c);
+        }
         if (plan->max_deg > 16) R->wide = true;
         const int32_t Zp = (plan->Z + 31) / 32 * 32;
         int32_t T = plan->launch.threads_per_frame;
@@ -637,8 +657,11 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
         }
         if (T % Zp != 0 && Zp % T != 0)
             return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: threads_per_frame %d vs lifting", c, T);
-        const uint32_t tables = align_up(align_up(static_cast<uint32_t>(plan->L + 1 + plan->mb + 1) * 4, 8) +
-                                             static_cast<uint32_t>(plan->nnzb) * 8, 128);
+        const uint32_t code_tables = align_up(static_cast<uint32_t>(plan->L + 1 + plan->mb + 1) * 4, 8) +
+                                     static_cast<uint32_t>(plan->nnzb) * 8;
+        const uint32_t axes_off = align_up(code_tables, 16);
+        const uint32_t tables =
+            align_up(ka ? axes_off + static_cast<uint32_t>(sizeof(ck::ldpc::MixedAxes<4>)) : code_tables, 128);
         const uint32_t ctrl = 128;
         const uint32_t gblk = align_up(static_cast<uint32_t>(plan->nnzb) * 8, 128);
         const uint32_t app = align_up(static_cast<uint32_t>(plan->N) * 4, 128);
@@ -695,6 +718,20 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
         K.r_off = ctrl + gblk + app;
         K.r_stride = r_stride;
         K.weight = static_cast<float>(plan->E);
+        K.ka = ka;
+        K.axes_off = axes_off;
+        if (ka) {
+            K.sym = static_cast<const float2*>(b.symbols);
+            K.inv_s2 = b.inv_s2;
+            const ck_axis_maxlog* ax[2] = {b.axis_re, b.axis_im};
+            for (int a = 0; a < 2; ++a) {
+                K.ax_levels[a] = ax[a]->levels;
+                K.ax_labels[a] = ax[a]->labels;
+                K.ax_lo[a] = ax[a]->lo;
+                K.ax_hi[a] = ax[a]->hi;
+                K.ax_pos[a] = ax[a]->pos;
+            }
+        }
         R->block_threads = std::max(R->block_threads, T * G);
         R->smem = std::max(R->smem, tables + static_cast<uint32_t>(G) * group);
     }

@@ -5,6 +5,7 @@
 #pragma once
 
 #include "ck_ldpc_minsum.cuh"
+#include "ck_llr_axis.cuh"
 
 namespace ck {
 namespace ldpc {
@@ -42,7 +43,63 @@ struct MixedCode {
     uint32_t* g_r;
     uint32_t* counter;
     float weight;  // edges per frame
+    // Fused demapping (sym != null): frame f's channel LLRs are the
+    // closed-form max-log LLRs of its n_in / (2 ka) symbols at
+    // sym + f * n_in / (2 ka), with 1/sigma^2 = inv_s2[f]; llr_in is unused.
+    // The two axes' tables (ck_axis_maxlog arrays, [0] = in-phase) are
+    // loaded into the block's table region at axes_off on a code switch.
+    const float2* sym;
+    const float* inv_s2;
+    const float* ax_levels[2];
+    const int32_t* ax_labels[2];
+    const int32_t* ax_lo[2];
+    const int32_t* ax_hi[2];
+    const int32_t* ax_pos[2];
+    int32_t ka;
+    uint32_t axes_off;
 };
+
+// The fused demapper's two axis tables, as laid out at MixedCode::axes_off.
+template <int KA>
+struct MixedAxes {
+    ck::llr::MaxlogAxis<KA> ax[2];
+};
+
+// Loads code K's axis tables into the block's shared table region (all
+// threads of the block; the caller synchronizes).
+template <int KA>
+__device__ __forceinline__ void mixed_load_axes(const MixedCode& K, unsigned char* smem) {
+    MixedAxes<KA>* t = reinterpret_cast<MixedAxes<KA>*>(smem + K.axes_off);
+    for (int a = 0; a < 2; ++a)
+        ck::llr::load_maxlog_axis<KA>(t->ax[a], K.ax_levels[a], K.ax_labels[a], K.ax_lo[a], K.ax_hi[a],
+                                      K.ax_pos[a], threadIdx.x, blockDim.x);
+}
+
+// Frame f's channel LLRs into `a` (n_in values, then the caller zeroes the
+// punctured tail): symbol i's 2 KA LLRs go to a[2 KA i + pos[b]], each as
+// x + 0 like the loaded LLRs of the unfused path.  The same arithmetic as
+// the demapper kernels, so the same bits.
+template <int KA>
+__device__ __forceinline__ void mixed_demap_frame(const MixedCode& K, const unsigned char* smem, float* a,
+                                                  uint32_t f, int tid) {
+    constexpr int KB = 2 * KA;
+    const MixedAxes<KA>* t = reinterpret_cast<const MixedAxes<KA>*>(smem + K.axes_off);
+    const uint32_t S = static_cast<uint32_t>(K.n_in) / KB;
+    const float2* x = K.sym + static_cast<size_t>(f) * S;
+    const float s2 = K.inv_s2[f];
+    for (uint32_t i = tid; i < S; i += K.T) {
+        const float2 v = __ldcs(x + i);
+        float o[KB];
+        ck::llr::axis_maxlog<KA>(v.x, t->ax[0], s2, o);
+        ck::llr::axis_maxlog<KA>(v.y, t->ax[1], s2, o + KA);
+        float* dst = a + KB * i;
+#pragma unroll
+        for (int b = 0; b < KA; ++b) {
+            dst[t->ax[0].pos[b]] = __fadd_rn(o[b], 0.0f);
+            dst[t->ax[1].pos[b]] = __fadd_rn(o[KA + b], 0.0f);
+        }
+    }
+}
 
 struct MixedParams {
     MixedCode code[kMaxMixed];
@@ -126,8 +183,17 @@ __device__ __forceinline__ void mixed_frames(const MixedCode& K, unsigned char* 
         const uint32_t pos = *s_frame;
         if (pos >= K.B) break;
         const uint32_t f = K.order ? static_cast<uint32_t>(__ldg(K.order + pos)) : pos;
-        const float* src = K.llr_in + static_cast<size_t>(f) * K.n_in;
-        for (int i = tid; i < K.n_in; i += K.T) a[i] = __fadd_rn(__ldcs(src + i), 0.0f);
+        if (K.sym) {
+            switch (K.ka) {
+                case 1: mixed_demap_frame<1>(K, smem, a, f, tid); break;
+                case 2: mixed_demap_frame<2>(K, smem, a, f, tid); break;
+                case 3: mixed_demap_frame<3>(K, smem, a, f, tid); break;
+                default: mixed_demap_frame<4>(K, smem, a, f, tid); break;
+            }
+        } else {
+            const float* src = K.llr_in + static_cast<size_t>(f) * K.n_in;
+            for (int i = tid; i < K.n_in; i += K.T) a[i] = __fadd_rn(__ldcs(src + i), 0.0f);
+        }
         for (int i = K.n_in + tid; i < K.N; i += K.T) a[i] = 0.0f;
         st.zero_rows(K.m, tid, K.T);
         group_sync(bar, K.T);
@@ -229,6 +295,14 @@ __device__ __forceinline__ void mixed_body(const MixedParams& p) {
         for (int i = threadIdx.x; i <= K.L; i += blockDim.x) s_layer[i] = K.layer[i];
         for (int i = threadIdx.x; i <= K.mb; i += blockDim.x) s_eptr[i] = K.eptr[i];
         for (int i = threadIdx.x; i < K.nnzb; i += blockDim.x) s_blk[i] = K.blk[i];
+        if (K.sym) {
+            switch (K.ka) {
+                case 1: mixed_load_axes<1>(K, smem); break;
+                case 2: mixed_load_axes<2>(K, smem); break;
+                case 3: mixed_load_axes<3>(K, smem); break;
+                default: mixed_load_axes<4>(K, smem); break;
+            }
+        }
         __syncthreads();
         const int g = threadIdx.x / K.T;
         if (g < K.G) {

@@ -34,6 +34,7 @@
 #include <stdint.h>
 
 #include "ck_common.cuh"
+#include "ck_llr_axis.cuh"
 
 namespace ck {
 namespace llr {
@@ -48,96 +49,12 @@ __device__ __forceinline__ float4 ld_stream(const float4* p) { return __ldcs(p);
 __device__ __forceinline__ float2 ld_stream(const float2* p) { return __ldcs(p); }
 __device__ __forceinline__ void st_stream(float4* p, float4 v) { __stcs(p, v); }
 
-// -(d*d)*inv_s2 with two roundings and no contraction.
-__device__ __forceinline__ float neg_sq_scaled(float d, float inv_s2) {
-    return __fmul_rn(-__fmul_rn(d, d), inv_s2);
-}
-
-// ---------------------------------------------------------------------------
-// Closed-form max-log (commkit/_cuda/src/llr.cu:262-302,
-// commkit/mapping/_numba_llr.py:179-210)
-// ---------------------------------------------------------------------------
-
-template <int KA>
-struct MaxlogAxis {
-    static constexpr int L = 1 << KA;
-    float step, rstep;  // lev[1] - lev[0] and its rounded reciprocal
-    float lev[L];
-    int32_t lab[L];
-    // For bit b and snapped level s: the nearest level below (lo) and above
-    // (hi) whose bit b differs, as level VALUES, +inf where there is none
-    // (the reference's index -1).
-    float lo[KA * L];
-    float hi[KA * L];
-    int32_t pos[KA];
-};
-
-// LLRs of one axis's KA bits (axis bit order) of the coordinate `x`.
-//
-// Per bit the reference takes m_other = max(-3e38, f(x - lo), f(x - hi))
-// over the opposite levels that exist, with f(d) = -(d*d)*inv_s2 rounded
-// twice.  f falls as |d| grows and rounding is monotone, so that maximum
-// is f of the smaller |d| (equal magnitudes give equal values): one metric
-// per bit instead of two.  A missing level is +inf, whose |x - inf| never
-// wins against a finite distance; the cases where every candidate is
-// infinite or NaN end at -3e38 on both routes, as do NaN inputs.
-template <int KA>
-__device__ __forceinline__ void axis_maxlog(float x, const MaxlogAxis<KA>& t, float inv_s2,
-                                            float* o) {
-    constexpr int L = 1 << KA;
-    // s = rint((x - lev0) / step), clamped to [0, L - 1] (round half to
-    // even, as np.rint).  The quotient comes from a multiply by the rounded
-    // reciprocal, within 3 units in the last place of the IEEE quotient
-    // (two roundings of 2^-24 plus the reciprocal's), so it rounds to the
-    // same integer unless it lies within that distance of a half-integer;
-    // there (rarely) the IEEE division decides.  qp - rint(qp) is exact.
-    // NaN and infinite x clamp as the integer conversion of the reference
-    // does (NaN to 0, +-inf to the ends).
-    const float a = __fsub_rn(x, t.lev[0]);
-    const float qp = __fmul_rn(a, t.rstep);
-    float rq = rintf(qp);
-    if (fabsf(fabsf(__fsub_rn(qp, rq)) - 0.5f) <= __fmul_rn(fabsf(qp), 0x1p-20f))
-        rq = rintf(__fdiv_rn(a, t.step));
-    int s = static_cast<int>(fminf(fmaxf(rq, 0.0f), static_cast<float>(L - 1)));
-    float d = __fsub_rn(x, t.lev[s]);
-    // Near a midpoint the rounded quotient can land one level off: keep the
-    // nearer of s and its neighbour towards x.
-    const int s2 = d > 0.0f ? s + 1 : s - 1;
-    if (s2 >= 0 && s2 < L) {
-        const float d2 = __fsub_rn(x, t.lev[s2]);
-        if (__fmul_rn(d2, d2) < __fmul_rn(d, d)) {
-            s = s2;
-            d = d2;
-        }
-    }
-    const float m_own = neg_sq_scaled(d, inv_s2);
-    const int32_t label = t.lab[s];
-#pragma unroll
-    for (int b = 0; b < KA; ++b) {
-        const float dn = fminf(fabsf(__fsub_rn(x, t.lo[b * L + s])), fabsf(__fsub_rn(x, t.hi[b * L + s])));
-        const float m_other = fmaxf(-3.0e38f, neg_sq_scaled(dn, inv_s2));
-        const bool one = (label >> (KA - 1 - b)) & 1;
-        o[b] = one ? __fsub_rn(m_other, m_own) : __fsub_rn(m_own, m_other);
-    }
-}
+// The closed-form max-log pieces (MaxlogAxis, axis_maxlog) are in
+// ck_llr_axis.cuh, shared with the mixed decoder's fused frame load.
 
 template <int KA>
 __device__ __forceinline__ void load_maxlog_axis(MaxlogAxis<KA>& t, const ck_axis_maxlog& a) {
-    constexpr int L = 1 << KA;
-    for (int i = threadIdx.x; i < L; i += blockDim.x) {
-        t.lev[i] = a.levels[i];
-        t.lab[i] = a.labels[i];
-    }
-    for (int i = threadIdx.x; i < KA * L; i += blockDim.x) {
-        const int32_t lo = a.lo[i], hi = a.hi[i];
-        t.lo[i] = lo >= 0 ? a.levels[lo] : ck::inf_f();
-        t.hi[i] = hi >= 0 ? a.levels[hi] : ck::inf_f();
-    }
-    for (int i = threadIdx.x; i < KA; i += blockDim.x) t.pos[i] = a.pos[i];
-    if (threadIdx.x == 0) {
-        t.step = __fsub_rn(a.levels[1], a.levels[0]);
-        t.rstep = __frcp_rn(t.step);
-    }
+    load_maxlog_axis<KA>(t, a.levels, a.labels, a.lo, a.hi, a.pos, threadIdx.x, blockDim.x);
 }
 
 // ---------------------------------------------------------------------------

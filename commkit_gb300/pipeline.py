@@ -20,6 +20,13 @@ received symbols where the host put them and the decoder writes each
 frame's results straight into host memory, so a step needs no copy in
 either direction.  The LLRs, the noise scales and the message state stay in
 HBM.
+
+With ``fused=True`` (the default) the slots whose demapping is the
+closed-form max-log of a square separable constellation are demapped by the
+decoder itself as it loads each frame (``ck_ldpc_batch.symbols``): a step is
+then one launch, the channel LLRs never go through device memory, and with
+``host_io`` the symbol reads from host memory overlap the decoding of other
+frames.  The LLRs are the same bits as the demapper kernel's.
 """
 
 from __future__ import annotations
@@ -49,7 +56,8 @@ class CodeSlot:
 class MixedReceiver:
     """Demap + mixed-code decode of fixed-size batches on one CUDA device."""
 
-    def __init__(self, slots: list[CodeSlot], device: Any = None, host_io: bool = False, lpt: bool = True):
+    def __init__(self, slots: list[CodeSlot], device: Any = None, host_io: bool = False, lpt: bool = True,
+                 fused: bool = True):  # fmt: skip
         import torch
 
         if not slots or len(slots) > 4:
@@ -61,6 +69,8 @@ class MixedReceiver:
         io = {"pin_memory": True} if self.host_io else {"device": self.device}
         self.sym, self.s2, self.llr, self.outputs, self.order = [], [], [], [], []
         self.lpt = bool(lpt)
+        # Per slot: the (re, im) axis structs of a fused demap, or None.
+        self._fused: list = []
         for s in slots:
             k = s.constellation.bits_per_symbol
             _require_leading_info(s.code, "MixedReceiver")
@@ -71,6 +81,7 @@ class MixedReceiver:
             self.s2.append(torch.ones((s.frames,), dtype=torch.float32, device=self.device))
             self.order.append(torch.arange(s.frames, dtype=torch.int32, device=self.device))
             self.llr.append(torch.empty((s.frames, s.code.n), dtype=torch.float32, device=self.device))
+            self._fused.append(self._fusable(s) if fused else None)
             self.outputs.append((
                 torch.empty((s.frames, s.code.n), dtype=torch.float32, **io),
                 torch.empty((s.frames, s.code.k), dtype=torch.int8, **io),
@@ -79,6 +90,27 @@ class MixedReceiver:
             ))  # fmt: skip
         self.workspace = torch.empty(max(self._workspace_bytes(), 256), dtype=torch.uint8, device=self.device)
         self.graph = None
+
+    def _fusable(self, s: CodeSlot):
+        """The axis structs for demapping slot ``s`` inside the decoder, or
+        None where the demapper kernel runs first (level metrics, exact
+        LLRs, non-separable or non-square constellations)."""
+        if s.demap != "maxlog" or _table_kind(s.constellation, s.demap) != "maxlog":
+            return None
+        like = _device.wrap(self.llr[0] if self.llr else self.torch.empty(1, device=self.device))
+        tabs = device_tables(s.constellation, "maxlog", like)
+        if len(tabs) != 10:  # two axes of five tables each
+            return None
+        half = len(tabs) // 2
+        re, im = _axis_struct(tabs[:half], "maxlog"), _axis_struct(tabs[half:], "maxlog")
+        if re.k != im.k or not 1 <= re.k <= 4:
+            return None
+        return (re, im, tabs)
+
+    @property
+    def fused(self) -> list[bool]:
+        """Per slot, whether the decoder demaps it."""
+        return [f is not None for f in self._fused]
 
     def _batches(self) -> Any:
         arr = (_lib.Batch * len(self.slots))()
@@ -90,6 +122,12 @@ class MixedReceiver:
                                 int(s.method.max_iterations), 1 if s.method.early_stop else 0,
                                 out[2].data_ptr(), out[3].data_ptr(), out[1].data_ptr(), s.code.k,
                                 self.order[i].data_ptr())  # fmt: skip
+            f = self._fused[i] if i < len(self._fused) else None
+            if f is not None:
+                arr[i].symbols = self.sym[i].data_ptr()
+                arr[i].inv_s2 = self.s2[i].data_ptr()
+                arr[i].axis_re = ctypes.pointer(f[0])
+                arr[i].axis_im = ctypes.pointer(f[1])
         return arr
 
     def _workspace_bytes(self) -> int:
@@ -119,20 +157,23 @@ class MixedReceiver:
                 self.order[i].copy_(self.torch.from_numpy(order), non_blocking=False)
 
     def step(self) -> None:
-        """Demap every slot and decode them all in one mixed launch (no allocation)."""
-        if not self.host_io:
+        """Demap every slot and decode them all in one mixed launch (no
+        allocation); fused slots are demapped by the decoder."""
+        if not self.host_io and not any(self.fused):
             for i, s in enumerate(self.slots):
                 compute_llr_frames(self.sym[i], constellation=s.constellation, method=s.demap,
                                    inv_s2=self.s2[i], out=self.llr[i])  # fmt: skip
             decode_mixed([(self.llr[i], s.code, s.method) for i, s in enumerate(self.slots)],
                          workspace=self.workspace, outputs=self.outputs)  # fmt: skip
             return
-        # Host I/O: the same kernels, given the pinned host addresses.
+        # The kernels through the C ABI (pinned host addresses with host_io).
         lib = _lib.lib()
         like = _device.wrap(self.llr[0])
         st = _device.stream_of(like)
         with _device.on_device(like):
             for i, s in enumerate(self.slots):
+                if self._fused[i] is not None:
+                    continue
                 F, S = self.sym[i].shape
                 kind = _table_kind(s.constellation, s.demap)
                 tabs = device_tables(s.constellation, kind, like)

@@ -416,6 +416,19 @@ typedef struct ck_ldpc_batch {
      * frames are taken from the queue (heaviest expected first shortens the
      * launch's tail); NULL for 0..B-1.  Results stay at their frame's place. */
     const int32_t* order;
+    /* Optional demapping inside the decoder.  When `symbols` is not NULL,
+     * llr_in is not read: frame f's channel LLRs are the closed-form
+     * max-log LLRs (bit-identical to ck_llr_separable_maxlog_frames) of its
+     * n_in / k symbols at symbols + f * n_in / k, with 1/sigma^2 =
+     * inv_s2[f] and k = axis_re->k + axis_im->k (equal axes of 1 to 4
+     * bits).  symbols (B, n_in / k) complex64, 8-byte aligned, in device or
+     * mapped host memory; inv_s2 (B,) float32; the axis structs in host
+     * memory, their arrays on the device.  Saves the LLR round trip through
+     * device memory and the demapper launch. */
+    const void* symbols;
+    const float* inv_s2;
+    const ck_axis_maxlog* axis_re;
+    const ck_axis_maxlog* axis_im;
 } ck_ldpc_batch;
 
 #define CK_LDPC_MAX_MIXED 4

@@ -74,11 +74,13 @@ def test_mixed_single_code_and_empty_batch():
     np.testing.assert_array_equal(m1.bits.cpu().numpy(), p.bits.cpu().numpy())
 
 
+@pytest.mark.parametrize("fused", [True, False])
 @pytest.mark.parametrize("host_io", [False, True])
-def test_receiver_graph_replay_matches_plain_calls(host_io):
+def test_receiver_graph_replay_matches_plain_calls(host_io, fused):
     """The mixed receiver, captured once as a CUDA graph and replayed on a
     new batch, gives the plain calls' results; with ``host_io`` its kernels
-    read the symbols from and write the results to pinned host memory."""
+    read the symbols from and write the results to pinned host memory, and
+    ``fused`` demaps inside the decoder (the same LLR bits)."""
     import torch
 
     import commkit_gb300 as ck
@@ -91,8 +93,9 @@ def test_receiver_graph_replay_matches_plain_calls(host_io):
     codes = {n: ck.LDPCCode.quasi_cyclic(W.CODES[n].base(), lifting=W.CODES[n].z) for n in names}
     consts = {n: ck.Constellation.qam(W.MIXED_ORDERS[n]) for n in names}
     rx = MixedReceiver([CodeSlot(codes[n], consts[n], work[n].symbols.shape[0], method) for n in names], dev,
-                       host_io=host_io)  # fmt: skip
+                       host_io=host_io, fused=fused)  # fmt: skip
     assert rx.sym[0].is_cuda != host_io and rx.outputs[0][0].is_cuda != host_io
+    assert rx.fused == [fused] * len(names)
     rx.load([work[n].symbols for n in names], [work[n].noise_var for n in names])
     rx.capture()
     work2 = W.mixed_workload(total=600, seed=6)  # same shapes, new frames
@@ -105,4 +108,46 @@ def test_receiver_graph_replay_matches_plain_calls(host_io):
         p = ck.decode(llr, code=codes[n], method=method)
         np.testing.assert_array_equal(r.llrs.cpu().numpy(), p.llrs.cpu().numpy())
         np.testing.assert_array_equal(r.bits.cpu().numpy(), p.bits.cpu().numpy())
+        np.testing.assert_array_equal(r.iterations.cpu().numpy(), p.iterations.cpu().numpy().reshape(-1))
+
+
+@pytest.mark.parametrize("order", [4, 16, 64, 256])
+def test_fused_demap_every_square_order(order):
+    """The decoder's fused demapping against the demapper kernel, one to four
+    bits per axis, on noisy symbols plus ties at level midpoints, far-out
+    points and non-finite coordinates; an exact-LLR slot beside it is
+    demapped by the demapper kernel first."""
+    import torch
+
+    import commkit_gb300 as ck
+    from commkit_gb300.pipeline import CodeSlot, MixedReceiver
+
+    dev = torch.device("cuda", 0)
+    code = ck.LDPCCode.quasi_cyclic(W.CODES["B"].base(), lifting=W.CODES["B"].z)
+    c = ck.Constellation.qam(order)
+    k = c.bits_per_symbol
+    S = code.n // k
+    F = 7
+    rng = np.random.default_rng(order)
+    pts = c.points.astype(np.complex64)
+    sym = pts[rng.integers(0, order, size=(F, S))] + (0.15 * (rng.standard_normal((F, S))
+                                                             + 1j * rng.standard_normal((F, S)))).astype(np.complex64)
+    sym = sym.astype(np.complex64)
+    lev = np.unique(pts.real)
+    mid = (lev[:-1] + lev[1:]) / 2
+    sym[0, : mid.size] = (mid + 1j * mid[::-1]).astype(np.complex64)  # ties
+    sym[1, :4] = np.array([50 + 50j, -50 - 50j, np.inf + 0j, complex(np.nan, 1.0)], np.complex64)
+    nv = np.linspace(0.05, 0.4, F)
+    method = ck.MinSum(max_iterations=8)
+    slots = [CodeSlot(code, c, F, method), CodeSlot(code, c, F, method, demap="exact")]
+    rx = MixedReceiver(slots, dev, fused=True)
+    assert rx.fused == [True, False]
+    rx.load([sym, sym], [nv, nv])
+    rx.step()
+    torch.cuda.synchronize()
+    x = torch.from_numpy(sym).to(dev)
+    for r, how in zip(rx.results(), ("maxlog", "exact"), strict=True):
+        llr = ck.compute_llr_frames(x, noise_var=nv, constellation=c, method=how)
+        p = ck.decode(llr, code=code, method=method)
+        np.testing.assert_array_equal(r.llrs.cpu().numpy(), p.llrs.cpu().numpy())
         np.testing.assert_array_equal(r.iterations.cpu().numpy(), p.iterations.cpu().numpy().reshape(-1))

@@ -16,10 +16,10 @@ import pytest
 import oracle
 from commkit_gb300 import _lib
 from commkit_gb300 import workloads as W
+from commkit_gb300.build import JIT_HEADERS as HEADERS
 from tests.conftest import GOLDEN
 
 CSRC = Path(__file__).resolve().parents[1] / "commkit_gb300" / "csrc"
-HEADERS = ("ck_device.cuh", "ck_ldpc_kernel.cuh", "ck_ldpc_minsum.cuh", "ck_ldpc_mixed.cuh")
 
 
 def _nvrtc():
