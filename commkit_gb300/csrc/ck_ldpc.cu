@@ -109,6 +109,7 @@ struct Resolved {
 constexpr int kMaxCluster = 8;  // the portable cluster size
 
 constexpr size_t kHeaderBytes = 256;
+static_assert(4 * kMaxMixed <= kHeaderBytes, "the mixed launch's queue counters sit in the header");
 
 int device_limits(int dev, int* sms, int* smem_optin) {
     CK_CUDA(cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev));
@@ -577,7 +578,7 @@ struct MixedResolved {
     uint32_t smem;
     int grid;
     size_t ws_bytes;
-    size_t r_off[kMaxMixed];
+    uint32_t block_words;  // device-memory message state per block, shared by the codes
     bool wide;  // some code has rows above degree 16
 };
 
@@ -762,7 +763,7 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
     R->grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(need, int64_t(sms) * per_sm)));
     // Starting split of the blocks in proportion to each code's work
     // (frames x edges x iteration budget), at least one block per code with frames.
-    double total = 0.0, work[kMaxMixed] = {0, 0, 0, 0};
+    double total = 0.0, work[kMaxMixed] = {};
     for (int c = 0; c < n; ++c) {
         const MixedCode& K = R->p.code[c];
         work[c] = static_cast<double>(K.B) * K.weight * std::max(1, K.max_iterations) / K.G;
@@ -776,14 +777,17 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
         start = std::min(R->grid, start + share);
     }
     R->p.start_block[n] = R->grid;
-    // Workspace: counters, then each code's device-memory message slots.
-    size_t off = kHeaderBytes;
-    for (int c = 0; c < n; ++c) {
-        R->r_off[c] = off;
+    // Workspace: counters, then the device-memory message slots.  A block
+    // runs one code at a time, so the codes share each block's region,
+    // sized for the largest (G groups x 3 r_stride words), in 256-byte units.
+    uint32_t block_words = 0;
+    for (int c = 0; c < n; ++c)
         if (!R->p.code[c].r_smem)
-            off += ((static_cast<size_t>(R->grid) * R->p.code[c].G * R->p.code[c].r_stride * 12 + 255) / 256) * 256;
-    }
-    R->ws_bytes = off;
+            block_words = std::max<uint32_t>(block_words, static_cast<uint32_t>(R->p.code[c].G) * 3u *
+                                                              R->p.code[c].r_stride);
+    R->block_words = (block_words + 63u) / 64u * 64u;
+    for (int c = 0; c < n; ++c) R->p.code[c].block_words = R->block_words;
+    R->ws_bytes = kHeaderBytes + static_cast<size_t>(R->grid) * R->block_words * 4u;
     return CK_OK;
 }
 
@@ -823,7 +827,7 @@ extern "C" int ck_ldpc_decode_mixed(const ck_ldpc_batch* batches, int32_t num_ba
     unsigned char* wsb = static_cast<unsigned char*>(ws);
     for (int c = 0; c < num_batches; ++c) {
         R.p.code[c].counter = reinterpret_cast<uint32_t*>(wsb + 4 * c);
-        R.p.code[c].g_r = reinterpret_cast<uint32_t*>(wsb + R.r_off[c]);
+        R.p.code[c].g_r = reinterpret_cast<uint32_t*>(wsb + kHeaderBytes);
     }
     int status = ck::cuda_check(cudaMemsetAsync(wsb, 0, kHeaderBytes, s), "cudaMemsetAsync");
     if (status == CK_OK) {

@@ -220,8 +220,19 @@ std::string program_source(const ck_ldpc_plan& plan, int dmax) {
 // The mixed decoder of n codes; code c runs its program when special[c].
 std::string mixed_program_source(const ck_ldpc_plan* const* plans, const bool* special, int n, int dmax) {
     std::string s = "#include \"ck_ldpc_mixed.cuh\"\nusing namespace ck::ldpc;\nnamespace {\n";
-    for (int c = 0; c < n; ++c)
-        if (special[c]) s += program_struct(*plans[c], ("CodeProgram" + std::to_string(c)).c_str());
+    // A code may fill several batches (one per constellation): one program
+    // and one call site per distinct (plan, specialised), its batches as
+    // cases of the same branch.
+    std::vector<int> first(n);
+    for (int c = 0; c < n; ++c) {
+        first[c] = c;
+        for (int u = 0; u < c; ++u)
+            if (plans[u] == plans[c] && special[u] == special[c]) {
+                first[c] = u;
+                break;
+            }
+        if (first[c] == c && special[c]) s += program_struct(*plans[c], ("CodeProgram" + std::to_string(c)).c_str());
+    }
     s += "struct CodeDispatch {\n";
     s += "    template <int DMAX>\n";
     s += "    __device__ __forceinline__ static void run(int c, const MixedCode& K, unsigned char* smem,\n";
@@ -229,7 +240,9 @@ std::string mixed_program_source(const ck_ldpc_plan* const* plans, const bool* s
     s += "                                               const int2* s_blk, int g, int tid) {\n";
     s += "        switch (c) {\n";
     for (int c = 0; c < n; ++c) {
-        add(s, "            case %lld:\n", c);
+        if (first[c] != c) continue;
+        for (int d = c; d < n; ++d)
+            if (first[d] == c) add(s, "            case %lld:\n", d);
         if (special[c]) {
             const std::string prog = "CodeProgram" + std::to_string(c);
             s += "                if (K.r_smem)\n";
@@ -348,7 +361,8 @@ int specialised_kernel(const ck_ldpc_plan* plan, int dmax, bool r_smem, const vo
 int mixed_specialised_kernel(const ck_ldpc_plan* const* plans, const int32_t* T, int n, int dmax,
                              const void** out) {
     *out = nullptr;
-    bool special[8] = {};
+    bool special[CK_LDPC_MAX_MIXED] = {};
+    if (n < 1 || n > CK_LDPC_MAX_MIXED) return CK_OK;
     bool any = false, required = false;
     std::vector<uint64_t> key{static_cast<uint64_t>(dmax)};
     for (int c = 0; c < n; ++c) {

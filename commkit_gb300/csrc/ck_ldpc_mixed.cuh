@@ -19,7 +19,7 @@ namespace ldpc {
 // same rows, same order, same bits.
 // ---------------------------------------------------------------------------
 
-constexpr int kMaxMixed = 4;  // CK_LDPC_MAX_MIXED
+constexpr int kMaxMixed = 12;  // CK_LDPC_MAX_MIXED
 constexpr int kMixedThreads = 768;
 
 struct MixedCode {
@@ -40,7 +40,11 @@ struct MixedCode {
     int32_t max_iterations, early_stop;
     int32_t T, G, q_bstep, r_smem;
     uint32_t tables_bytes, group_bytes, gblk_off, app_off, r_off, r_stride;
+    // Device-memory message state: block b's groups use the words
+    // [b * block_words, (b + 1) * block_words) of g_r, 3 r_stride per group.
+    // A block runs one code at a time, so every code shares the region.
     uint32_t* g_r;
+    uint32_t block_words;
     uint32_t* counter;
     float weight;  // edges per frame
     // Fused demapping (sym != null): frame f's channel LLRs are the
@@ -141,8 +145,9 @@ __device__ __forceinline__ void mixed_frames(const MixedCode& K, unsigned char* 
     unsigned char* gbase = smem + K.tables_bytes + static_cast<uint32_t>(g) * K.group_bytes;
     volatile uint32_t* s_frame = reinterpret_cast<volatile uint32_t*>(gbase + 8);
     float* a = reinterpret_cast<float*>(gbase + K.app_off);
-    const uint32_t slot = blockIdx.x * static_cast<uint32_t>(K.G) + static_cast<uint32_t>(g);
-    const MinSumState<R_SMEM> st(reinterpret_cast<uint4*>(gbase + K.r_off), K.g_r, slot, K.r_stride);
+    const MinSumState<R_SMEM> st(reinterpret_cast<uint4*>(gbase + K.r_off),
+                                 K.g_r + static_cast<size_t>(blockIdx.x) * K.block_words, static_cast<uint32_t>(g),
+                                 K.r_stride);
     int2* gblk = reinterpret_cast<int2*>(gbase + K.gblk_off);
     const uint32_t a_addr = ck::smem_addr(a);
     for (int i = tid; i < K.nnzb; i += K.T)

@@ -5,19 +5,21 @@ They arrive over time (:func:`poisson_requests` draws a seeded stream).
 The :class:`Server` keeps LLRs and check-message state on the device and
 admits requests whenever a batch slot is free; a slot's device memory is
 allocated once, so the HBM budget is ``slots x bytes per slot``.  Each
-batch takes the arrived requests that fit one slot, demaps them per (code,
-constellation) and decodes every code in ONE launch of the mixed-code
-persistent kernel, on the slot's own CUDA stream: batches admitted while
-others run overlap with them on the device.
+batch takes the arrived requests that fit one slot and decodes them in ONE
+launch of the mixed-code persistent kernel, one batch entry per (code,
+constellation), which demaps each frame as it loads it; on the slot's own
+CUDA stream: batches admitted while others run overlap with them on the
+device.
 
 Zero-copy on GB300: the Grace host memory is coherent with the GPU over
 NVLink-C2C and pinned allocations have one address on both sides.  So a
 batch is assembled by one gather kernel that reads every request's pinned
 symbols (and the frames' noise scales) in place, and the decoder writes
 each frame's a-posteriori LLRs, bits, iterations and syndrome flag straight
-into a pinned output arena.  A batch costs one gather launch, one demap
-launch per (code, constellation), one decode launch and an event: no
-per-request copy call, no device-to-host copy, no allocation.
+into a pinned output arena.  A batch costs one gather launch, one decode
+launch and an event: no per-request copy call, no device-to-host copy, no
+allocation.  (Where a constellation's demapping cannot run inside the
+decoder, a demap launch per (code, constellation) fills LLR buffers first.)
 
 The arena is a ring: request results (:attr:`Request.llrs` etc.) are views
 into it and stay valid until ``output_arena_bytes`` of later results have
@@ -163,9 +165,10 @@ class _Slot:
         self.llr = {}
         for name, cap in caps.items():
             self.llr[name] = torch.empty((cap, server.codes[name].n), dtype=torch.float32, device=dev)
-        arr = server._batch_array({name: cap for name, cap in caps.items()}, self, {})
+        entries = server._sizing_entries()
+        arr = server._batch_array(entries, self, {})
         need = ctypes.c_size_t(0)
-        _lib.check(_lib.lib().ck_ldpc_mixed_workspace_size(arr, len(caps), ctypes.byref(need)), "server slot")
+        _lib.check(_lib.lib().ck_ldpc_mixed_workspace_size(arr, len(entries), ctypes.byref(need)), "server slot")
         self.ws = torch.empty(max(int(need.value), 256), dtype=torch.uint8, device=dev)
         self.bytes = (self.sym_dev.numel() * 8 + self.s2_dev.numel() * 4 + self.ws.numel()
                       + sum(t.numel() * 4 for t in self.llr.values()))  # fmt: skip
@@ -183,12 +186,13 @@ class Server:
     ``frames_per_slot`` caps each code's frames in one batch; the slots'
     device memory (``max_inflight`` of them) must fit ``hbm_budget``.
     ``output_arena_bytes`` sizes the pinned result ring (by default two
-    full batches of every slot).
+    full batches of every slot).  ``fused=False`` demaps in separate
+    launches before the decoder (the same bits).
     """
 
     def __init__(self, codes: dict[str, LDPCCode], method: MinSum, *, hbm_budget: int = 4 << 30,
                  max_inflight: int = 3, device: Any = None, frames_per_slot: dict | None = None,
-                 orders=(4, 16, 64), output_arena_bytes: int | None = None):  # fmt: skip
+                 orders=(4, 16, 64), output_arena_bytes: int | None = None, fused: bool = True):  # fmt: skip
         import torch
 
         self.torch = torch
@@ -218,6 +222,12 @@ class Server:
         max_segments = sum(self.caps.values()) + sym_bytes // _CHUNK + 2 * len(codes) * len(self.orders) + 8
         with torch.cuda.device(self.device):
             self._tables = {o: self._axis_structs(o) for o in self.orders}
+            # The decoder demaps the frames itself (one batch entry per code
+            # and constellation) when every constellation allows it and the
+            # entries fit one launch; else a demap launch per (code,
+            # constellation) fills the slot's LLR buffers first.
+            self.fused = (fused and len(codes) * len(self.orders) <= _lib.CK_LDPC_MAX_MIXED
+                          and all(t[0].k == t[1].k and 1 <= t[0].k <= 4 for t in self._tables.values()))
             self.slots = [_Slot(self, self.caps, sym_bytes, max_segments) for _ in range(max_inflight)]
         used = sum(sl.bytes for sl in self.slots)
         if used > hbm_budget:
@@ -243,20 +253,40 @@ class Server:
         half = len(tabs) // 2
         return (_axis_struct(tabs[:half], "maxlog"), _axis_struct(tabs[half:], "maxlog"), tabs)
 
-    def _batch_array(self, counts: dict, slot: _Slot, out: dict):
-        """The mixed decode's per-code arguments; outputs at the host
-        addresses ``out[name] = (llr, bits, iters, valid)``, or in a scratch
-        layout when ``out`` is empty (workspace sizing only)."""
-        arr = (_lib.Batch * len(counts))()
+    def _batch_array(self, entries: list, slot: _Slot, out: dict):
+        """The mixed decode's batch arguments, one per entry ``(name, order,
+        B, frame offset, symbol offset, noise offset)``: ``order`` None for
+        a code's LLRs in the slot's buffer, else the decoder demaps that
+        constellation's frames from the slot's symbols.  Outputs at the host
+        addresses ``out[name] = (llr, bits, iters, valid)`` plus the frame
+        offset, or in a scratch layout when ``out`` is empty (workspace
+        sizing only)."""
+        arr = (_lib.Batch * len(entries))()
         m = self.method
-        for i, (name, B) in enumerate(counts.items()):
+        for i, (name, order, B, f_off, g_sym, g_s2) in enumerate(entries):
             code = self.codes[name]
             llr_o, bits_o, it_o, ok_o = out.get(name, (1, 1, 1, 1))
-            arr[i] = _lib.Batch(code._plan(self.device.index).handle, slot.llr[name].data_ptr(), llr_o, B, code.n,
+            if name in out:
+                llr_o, bits_o = llr_o + 4 * f_off * code.n, bits_o + f_off * code.k
+                it_o, ok_o = it_o + 4 * f_off, ok_o + f_off
+            arr[i] = _lib.Batch(code._plan(self.device.index).handle,
+                                slot.llr[name].data_ptr() + 4 * f_off * code.n, llr_o, B, code.n,
                                 _lib.CK_LDPC_MIN_SUM, np.float32(m.scale), np.float32(m.offset),
                                 int(m.max_iterations), 1 if m.early_stop else 0, it_o, ok_o, bits_o,
                                 code.k)  # fmt: skip
+            if order is not None:
+                re, im, _ = self._tables[order]
+                arr[i].symbols = slot.sym_dev.data_ptr() + 8 * g_sym
+                arr[i].inv_s2 = slot.s2_dev.data_ptr() + 4 * g_s2
+                arr[i].axis_re = ctypes.pointer(re)
+                arr[i].axis_im = ctypes.pointer(im)
         return arr
+
+    def _sizing_entries(self) -> list:
+        """Every entry at its code's full slot capacity (workspace sizing)."""
+        if self.fused:
+            return [(n, o, cap, 0, 0, 0) for n, cap in self.caps.items() for o in self.orders]
+        return [(n, None, cap, 0, 0, 0) for n, cap in self.caps.items()]
 
     def _fits(self, batch: list[Request], r: Request) -> bool:
         frames = sum(q.frames for q in batch if q.code == r.code) + r.frames
@@ -330,17 +360,22 @@ class Server:
         lib = _lib.lib()
         st = slot.stream.cuda_stream
         _lib.check(lib.ck_gather(slot.segs.data_ptr(), nseg, st), "server gather")
-        for order, g_sym, S, g_frames, g_s2, name, f_off in demaps:
-            re, im, _ = self._tables[order]
-            _lib.check(lib.ck_llr_separable_maxlog_frames(
-                sym_base + 8 * g_sym, g_frames * S, S, s2_base + 4 * g_s2, ctypes.byref(re), ctypes.byref(im),
-                slot.llr[name].data_ptr() + 4 * f_off * self.codes[name].n, st), "server demap")  # fmt: skip
-        # Every code takes part in every launch (no frames where a batch has
-        # none), so all batches run the one mixed kernel compiled for this
-        # server's codes when its slots were built.
-        every = {name: counts.get(name, 0) for name in self.codes}
-        arr = self._batch_array(every, slot, out)
-        _lib.check(lib.ck_ldpc_decode_mixed(arr, len(every), slot.ws.data_ptr(), slot.ws.numel(), st),
+        # Every code (and constellation) takes part in every launch, with no
+        # frames where a batch has none, so all batches run the one mixed
+        # kernel compiled for this server's codes when its slots were built.
+        if self.fused:
+            got = {(name, order): (B, f_off, g_sym, g_s2) for order, g_sym, _, B, g_s2, name, f_off in demaps}
+            entries = [(name, order, *got.get((name, order), (0, 0, 0, 0))) for name in self.codes
+                       for order in self.orders]  # fmt: skip
+        else:
+            for order, g_sym, S, g_frames, g_s2, name, f_off in demaps:
+                re, im, _ = self._tables[order]
+                _lib.check(lib.ck_llr_separable_maxlog_frames(
+                    sym_base + 8 * g_sym, g_frames * S, S, s2_base + 4 * g_s2, ctypes.byref(re), ctypes.byref(im),
+                    slot.llr[name].data_ptr() + 4 * f_off * self.codes[name].n, st), "server demap")  # fmt: skip
+            entries = [(name, None, counts.get(name, 0), 0, 0, 0) for name in self.codes]
+        arr = self._batch_array(entries, slot, out)
+        _lib.check(lib.ck_ldpc_decode_mixed(arr, len(entries), slot.ws.data_ptr(), slot.ws.numel(), st),
                    "server decode")  # fmt: skip
         slot.event.record(slot.stream)
         self._busy.append(slot)

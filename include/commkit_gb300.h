@@ -431,15 +431,17 @@ typedef struct ck_ldpc_batch {
     const ck_axis_maxlog* axis_im;
 } ck_ldpc_batch;
 
-#define CK_LDPC_MAX_MIXED 4
+#define CK_LDPC_MAX_MIXED 12
 
 /* Device scratch bytes of a mixed-code launch of these batches. */
 int ck_ldpc_mixed_workspace_size(const ck_ldpc_batch* batches, int32_t num_batches,
                                  size_t* bytes);
 
 /*
- * Frames of up to CK_LDPC_MAX_MIXED different quasi-cyclic codes (lengths,
- * rates, iteration budgets) decoded in ONE launch of a persistent kernel.
+ * Frames of up to CK_LDPC_MAX_MIXED batches of quasi-cyclic codes (lengths,
+ * rates, iteration budgets; a code may appear in several batches, e.g. one
+ * per constellation with fused demapping) decoded in ONE launch of a
+ * persistent kernel.
  * Every block can host any code's frame groups; it starts on a code chosen
  * in proportion to the work, pulls that code's frames from a device queue
  * (a frame retires as soon as its syndrome passes, and its group takes the

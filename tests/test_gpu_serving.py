@@ -9,7 +9,8 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_served_results_equal_standalone_decodes():
+@pytest.mark.parametrize("fused", [True, False])
+def test_served_results_equal_standalone_decodes(fused):
     import torch
 
     import commkit_gb300 as ck
@@ -22,7 +23,9 @@ def test_served_results_equal_standalone_decodes():
     assert len(reqs) > 20
     codes = {n: ck.LDPCCode.quasi_cyclic(W.CODES[n].base(), lifting=W.CODES[n].z) for n in "ABC"}
     method = ck.MinSum(max_iterations=30)
-    server = Server(codes, method, hbm_budget=2 << 30, max_inflight=3, device=dev, output_arena_bytes=256 << 20)
+    server = Server(codes, method, hbm_budget=2 << 30, max_inflight=3, device=dev, output_arena_bytes=256 << 20,
+                    fused=fused)  # fmt: skip
+    assert server.fused == fused
     done = server.serve(reqs)
     assert sorted(r.rid for r in done) == [r.rid for r in reqs]
     assert all(r.latency > 0 for r in done)
