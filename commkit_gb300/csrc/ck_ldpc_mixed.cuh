@@ -87,12 +87,27 @@ template <int KA>
 __device__ __forceinline__ void mixed_demap_frame(const MixedCode& K, const unsigned char* smem, float* a,
                                                   uint32_t f, int tid) {
     constexpr int KB = 2 * KA;
+    constexpr int kAhead = 4;  // symbol loads in flight per thread
     const MixedAxes<KA>* t = reinterpret_cast<const MixedAxes<KA>*>(smem + K.axes_off);
     const uint32_t S = static_cast<uint32_t>(K.n_in) / KB;
+    const uint32_t T = static_cast<uint32_t>(K.T);
     const float2* x = K.sym + static_cast<size_t>(f) * S;
     const float s2 = K.inv_s2[f];
-    for (uint32_t i = tid; i < S; i += K.T) {
-        const float2 v = __ldcs(x + i);
+    // The thread's symbols tid, tid + T, ... come through a ring of kAhead
+    // registers: the loads of the next ones are in flight while one is
+    // demapped (the symbols may sit in host memory, microseconds away).
+    float2 ring[kAhead];
+#pragma unroll
+    for (int r = 0; r < kAhead; ++r) {
+        const uint32_t i = tid + r * T;
+        ring[r] = i < S ? __ldcs(x + i) : make_float2(0.0f, 0.0f);
+    }
+    for (uint32_t i = tid; i < S; i += T) {
+        const float2 v = ring[0];
+#pragma unroll
+        for (int r = 0; r + 1 < kAhead; ++r) ring[r] = ring[r + 1];
+        const uint32_t next = i + kAhead * T;
+        ring[kAhead - 1] = next < S ? __ldcs(x + next) : make_float2(0.0f, 0.0f);
         float o[KB];
         ck::llr::axis_maxlog<KA>(v.x, t->ax[0], s2, o);
         ck::llr::axis_maxlog<KA>(v.y, t->ax[1], s2, o + KA);
