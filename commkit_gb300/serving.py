@@ -37,6 +37,7 @@ import gc
 import time
 from collections import deque
 from dataclasses import dataclass, field
+from functools import cached_property
 from typing import Any
 
 import numpy as np
@@ -68,7 +69,7 @@ class Request:
     valid: Any = None
     iterations: Any = None
 
-    @property
+    @cached_property
     def frames(self) -> int:
         return int(self.symbols.shape[0])
 
@@ -239,6 +240,7 @@ class Server:
         self._busy: list[_Slot] = []
         self.completed: list[Request] = []
         self._t0 = 0.0
+        self._fit: list | None = None
 
     def _out_frame_bytes(self, name: str) -> int:
         code = self.codes[name]
@@ -289,9 +291,26 @@ class Server:
         return [(n, None, cap, 0, 0, 0) for n, cap in self.caps.items()]
 
     def _fits(self, batch: list[Request], r: Request) -> bool:
-        frames = sum(q.frames for q in batch if q.code == r.code) + r.frames
-        syms = sum(q.frames * q.symbols.shape[1] for q in batch) + r.frames * r.symbols.shape[1]
-        return frames <= self.caps[r.code] and syms <= self._sym_cap
+        """Whether ``r`` fits the slot beside ``batch``.  The batch's totals
+        (frames per code, symbols) are kept from the previous call while the
+        caller appends each accepted request, so filling a batch costs O(1)
+        per request rather than a pass over the batch."""
+        st = self._fit
+        if st is None or st[0] is not batch or st[1] != len(batch):
+            per_code: dict[str, int] = {}
+            syms = 0
+            for q in batch:
+                per_code[q.code] = per_code.get(q.code, 0) + q.frames
+                syms += q.frames * q.symbols.shape[1]
+            st = self._fit = [batch, len(batch), per_code, syms]
+        frames = st[2].get(r.code, 0) + r.frames
+        syms = st[3] + r.frames * r.symbols.shape[1]
+        ok = frames <= self.caps[r.code] and syms <= self._sym_cap
+        if ok:  # the caller appends r next
+            st[1] += 1
+            st[2][r.code] = frames
+            st[3] = syms
+        return ok
 
     def _wait_region(self, lo: int, hi: int) -> None:
         """Blocks until no batch in flight writes into arena bytes [lo, hi)."""

@@ -39,3 +39,35 @@ def test_request_larger_than_a_slot_raises():
     adm.arrive(_req(0, 50))
     with pytest.raises(MemoryError, match="does not fit"):
         adm.next_batch(_fits({"A": 16}))
+
+
+def test_server_fits_keeps_running_totals():
+    """The server's slot test (frames per code, symbols per slot) keeps the
+    batch's totals between calls; it must admit exactly what a pass over the
+    whole batch admits."""
+    from types import SimpleNamespace
+
+    from commkit_gb300.serving import Server
+
+    rng = np.random.default_rng(0)
+    fake = SimpleNamespace(caps={"A": 40, "B": 30, "C": 12}, _sym_cap=900, _fit=None)
+
+    def naive(batch, r):
+        frames = sum(q.frames for q in batch if q.code == r.code) + r.frames
+        syms = sum(q.frames * q.symbols.shape[1] for q in batch) + r.frames * r.symbols.shape[1]
+        return frames <= fake.caps[r.code] and syms <= fake._sym_cap
+
+    reqs = [Request(i, "ABC"[rng.integers(3)], 4, np.zeros((int(rng.integers(1, 9)), int(rng.integers(2, 12))),
+                                                            np.complex64), 0.1, arrival=i * 1e-3)
+            for i in range(400)]  # fmt: skip
+    got, want = Admission(slots=1), Admission(slots=1)
+    for r in reqs:
+        got.arrive(r)
+        want.arrive(r)
+    while want.pending:
+        a = got.next_batch(lambda b, r: Server._fits(fake, b, r))
+        b = want.next_batch(naive)
+        assert [r.rid for r in a] == [r.rid for r in b]
+        got.release()
+        want.release()
+    assert not got.pending
