@@ -885,7 +885,8 @@ def measure_served(args, dist: Dist) -> dict:
     slots = int(os.environ.get("CK_SERVE_SLOTS", "12"))
     # 4 GiB per 12 slots: every slot holds a full request of each code.
     server = Server(codes, ck.MinSum(max_iterations=WORKLOADS["served"]["max_it"]),
-                    hbm_budget=max(4 << 30, slots * ((4 << 30) // 12)), max_inflight=slots, device=dev)  # fmt: skip
+                    hbm_budget=max(4 << 30, slots * ((4 << 30) // 12)), max_inflight=slots, device=dev,
+                    spread_long=os.environ.get("CK_SERVE_SPREAD", "0") == "1")  # fmt: skip
     k_of = {n: c.k for n, c in codes.items()}
 
     def info_bits(reqs):
@@ -936,6 +937,8 @@ def measure_served(args, dist: Dist) -> dict:
                        "requests": len(backlog), "frames": int(sum(r.frames for r in backlog)),
                        "method": "overload at 3x a backlog estimate for 0.5 s, completed / wall until drained"},
         "latency_vs_load": sweep, "p99_ms_at_70pct": sweep["70%"]["p99_ms"], "batch_slots": slots,
+        "policy": {"fused": server.fused, "priority_split": server.split, "long_codes": sorted(server.long_codes),
+                   "spread_long": server.spread_long},
         "pool_build_s": t_build, "clocks": clk.summary(),
     }  # fmt: skip
 

@@ -125,6 +125,7 @@ class Batch(ctypes.Structure):
         ("inv_s2", ctypes.c_void_p),
         ("axis_re", ctypes.POINTER(AxisMaxlog)),
         ("axis_im", ctypes.POINTER(AxisMaxlog)),
+        ("frames_per_block", ctypes.c_int32),
     ]
 
 

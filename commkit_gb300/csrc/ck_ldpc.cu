@@ -625,6 +625,7 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
         if (b.B < 0 || b.B >= (int64_t(1) << 31)) return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: bad B", c);
         if (b.n_in < 1 || b.n_in > plan->N) return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: bad n_in", c);
         if (b.max_iterations < 0) return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: bad max_iterations", c);
+        if (b.frames_per_block < 0) return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: bad frames_per_block", c);
         if (b.bits && (b.k_bits < 0 || b.k_bits > b.n_in))
             return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: bad k_bits", c);
         if (b.B > 0 && ((!b.llr_in && !b.symbols) || !b.llr_out || !b.iters || !b.valid))
@@ -682,7 +683,7 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
         // plain launch's tuned frames per block (one block of G groups among
         // several per SM) says nothing about a mixed block, which is alone
         // on its SM.
-        const int32_t G = gmax;
+        const int32_t G = b.frames_per_block > 0 ? std::min(gmax, b.frames_per_block) : gmax;
         if (G < 1) return ck::fail(CK_ERR_UNSUPPORTED, "batch %d: a frame does not fit a block", c);
         MixedCode& K = R->p.code[c];
         K.layer = plan->d_layer;
@@ -782,7 +783,7 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
     // sized for the largest (G groups x 3 r_stride words), in 256-byte units.
     uint32_t block_words = 0;
     for (int c = 0; c < n; ++c)
-        if (!R->p.code[c].r_smem)
+        if (!R->p.code[c].r_smem && R->p.code[c].B > 0)  // a code without frames never runs
             block_words = std::max<uint32_t>(block_words, static_cast<uint32_t>(R->p.code[c].G) * 3u *
                                                               R->p.code[c].r_stride);
     R->block_words = (block_words + 63u) / 64u * 64u;

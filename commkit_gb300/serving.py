@@ -154,6 +154,10 @@ class _Slot:
         torch = server.torch
         dev = server.device
         self.stream = torch.cuda.Stream(dev)
+        # The short codes' launch, on a higher-priority stream (see Server).
+        self.stream_hi = torch.cuda.Stream(dev, priority=-1) if server.split else None
+        self.gathered = torch.cuda.Event()
+        self.hi_done = torch.cuda.Event()
         self.caps = caps
         total = sum(caps.values())
         self.sym_dev = torch.empty(sym_bytes // 8, dtype=torch.complex64, device=dev)
@@ -166,12 +170,19 @@ class _Slot:
         self.llr = {}
         for name, cap in caps.items():
             self.llr[name] = torch.empty((cap, server.codes[name].n), dtype=torch.float32, device=dev)
+        def workspace(entries):
+            arr = server._batch_array(entries, self, {})
+            need = ctypes.c_size_t(0)
+            _lib.check(_lib.lib().ck_ldpc_mixed_workspace_size(arr, len(entries), ctypes.byref(need)),
+                       "server slot")  # fmt: skip
+            return torch.empty(max(int(need.value), 256), dtype=torch.uint8, device=dev)
+
         entries = server._sizing_entries()
-        arr = server._batch_array(entries, self, {})
-        need = ctypes.c_size_t(0)
-        _lib.check(_lib.lib().ck_ldpc_mixed_workspace_size(arr, len(entries), ctypes.byref(need)), "server slot")
-        self.ws = torch.empty(max(int(need.value), 256), dtype=torch.uint8, device=dev)
+        self.ws = workspace(entries)
+        self.ws_hi = (workspace([e if e[0] not in server.long_codes else (e[0], e[1], 0, 0, 0, 0) for e in entries])
+                      if server.split else None)  # fmt: skip
         self.bytes = (self.sym_dev.numel() * 8 + self.s2_dev.numel() * 4 + self.ws.numel()
+                      + (self.ws_hi.numel() if self.ws_hi is not None else 0)
                       + sum(t.numel() * 4 for t in self.llr.values()))  # fmt: skip
         self.event = torch.cuda.Event()
         self.batch: list = []
@@ -188,12 +199,16 @@ class Server:
     device memory (``max_inflight`` of them) must fit ``hbm_budget``.
     ``output_arena_bytes`` sizes the pinned result ring (by default two
     full batches of every slot).  ``fused=False`` demaps in separate
-    launches before the decoder (the same bits).
+    launches before the decoder (the same bits).  ``priority_split``
+    decodes the long codes' frames of a batch in their own launch, the
+    others' on a higher-priority stream (the same bits).  ``spread_long``
+    gives each long frame a thread block, and so an SM, of its own.
     """
 
     def __init__(self, codes: dict[str, LDPCCode], method: MinSum, *, hbm_budget: int = 4 << 30,
                  max_inflight: int = 3, device: Any = None, frames_per_slot: dict | None = None,
-                 orders=(4, 16, 64), output_arena_bytes: int | None = None, fused: bool = True):  # fmt: skip
+                 orders=(4, 16, 64), output_arena_bytes: int | None = None, fused: bool = True,
+                 priority_split: bool = True, spread_long: bool = False):  # fmt: skip
         import torch
 
         self.torch = torch
@@ -229,6 +244,15 @@ class Server:
             # constellation) fills the slot's LLR buffers first.
             self.fused = (fused and len(codes) * len(self.orders) <= _lib.CK_LDPC_MAX_MIXED
                           and all(t[0].k == t[1].k and 1 <= t[0].k <= 4 for t in self._tables.values()))
+            # Long codes (a quarter of the heaviest frame's edges or more) and
+            # the others decode in separate launches of a batch, the others on
+            # a higher-priority stream: the GPU does not preempt, but it hands
+            # freed SMs to pending higher-priority blocks first, so short
+            # requests stop queueing behind long frames not yet started.
+            heaviest = max(c.checks.size for c in codes.values())
+            self.long_codes = {n for n, c in codes.items() if c.checks.size * 4 >= heaviest}
+            self.split = bool(priority_split and self.fused and len(self.long_codes) < len(codes))
+            self.spread_long = bool(spread_long)
             self.slots = [_Slot(self, self.caps, sym_bytes, max_segments) for _ in range(max_inflight)]
         used = sum(sl.bytes for sl in self.slots)
         if used > hbm_budget:
@@ -276,6 +300,8 @@ class Server:
                                 _lib.CK_LDPC_MIN_SUM, np.float32(m.scale), np.float32(m.offset),
                                 int(m.max_iterations), 1 if m.early_stop else 0, it_o, ok_o, bits_o,
                                 code.k)  # fmt: skip
+            if self.spread_long and name in self.long_codes:
+                arr[i].frames_per_block = 1
             if order is not None:
                 re, im, _ = self._tables[order]
                 arr[i].symbols = slot.sym_dev.data_ptr() + 8 * g_sym
@@ -378,6 +404,9 @@ class Server:
         slot.waiting = [(r, name, off_r) for r, name, off_r in slot.layout]
         lib = _lib.lib()
         st = slot.stream.cuda_stream
+        if self.split:
+            self._launch_split(slot, nseg, demaps, out)
+            return
         _lib.check(lib.ck_gather(slot.segs.data_ptr(), nseg, st), "server gather")
         # Every code (and constellation) takes part in every launch, with no
         # frames where a batch has none, so all batches run the one mixed
@@ -397,6 +426,32 @@ class Server:
         _lib.check(lib.ck_ldpc_decode_mixed(arr, len(entries), slot.ws.data_ptr(), slot.ws.numel(), st),
                    "server decode")  # fmt: skip
         slot.event.record(slot.stream)
+        self._busy.append(slot)
+
+    def _launch_split(self, slot: _Slot, nseg: int, demaps: list, out: dict) -> None:
+        """The batch's gather and the short codes' decode on the slot's
+        high-priority stream, the long codes' decode on its normal one; the
+        slot's event completes when both have."""
+        lib = _lib.lib()
+        hi, lo = slot.stream_hi, slot.stream
+        _lib.check(lib.ck_gather(slot.segs.data_ptr(), nseg, hi.cuda_stream), "server gather")
+        slot.gathered.record(hi)
+        got = {(name, order): (B, f_off, g_sym, g_s2) for order, g_sym, _, B, g_s2, name, f_off in demaps}
+        for stream, ws, long in ((hi, slot.ws_hi, False), (lo, slot.ws, True)):
+            if stream is lo:
+                lo.wait_event(slot.gathered)
+            entries = []
+            for name in self.codes:
+                for order in self.orders:
+                    e = got.get((name, order), (0, 0, 0, 0))
+                    entries.append((name, order, *(e if (name in self.long_codes) == long else (0, 0, 0, 0))))
+            if any(e[2] for e in entries):
+                arr = self._batch_array(entries, slot, out)
+                _lib.check(lib.ck_ldpc_decode_mixed(arr, len(entries), ws.data_ptr(), ws.numel(), stream.cuda_stream),
+                           "server decode")  # fmt: skip
+        slot.hi_done.record(hi)
+        lo.wait_event(slot.hi_done)
+        slot.event.record(lo)
         self._busy.append(slot)
 
     def _views(self, name: str, B: int, parts: list) -> tuple:

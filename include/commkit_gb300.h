@@ -429,6 +429,10 @@ typedef struct ck_ldpc_batch {
     const float* inv_s2;
     const ck_axis_maxlog* axis_re;
     const ck_axis_maxlog* axis_im;
+    /* Frames of this batch decoded at once per thread block: 0 for as many
+     * as fit.  1 gives each frame an SM of its own (a launch's blocks are
+     * sized for its largest code), so a long frame finishes sooner. */
+    int32_t frames_per_block;
 } ck_ldpc_batch;
 
 #define CK_LDPC_MAX_MIXED 12

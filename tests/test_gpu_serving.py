@@ -9,8 +9,9 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("fused", [True, False])
-def test_served_results_equal_standalone_decodes(fused):
+@pytest.mark.parametrize("fused,split,spread", [(True, True, False), (True, True, True), (True, False, False),
+                                                (False, False, False)])
+def test_served_results_equal_standalone_decodes(fused, split, spread):
     import torch
 
     import commkit_gb300 as ck
@@ -24,8 +25,8 @@ def test_served_results_equal_standalone_decodes(fused):
     codes = {n: ck.LDPCCode.quasi_cyclic(W.CODES[n].base(), lifting=W.CODES[n].z) for n in "ABC"}
     method = ck.MinSum(max_iterations=30)
     server = Server(codes, method, hbm_budget=2 << 30, max_inflight=3, device=dev, output_arena_bytes=256 << 20,
-                    fused=fused)  # fmt: skip
-    assert server.fused == fused
+                    fused=fused, priority_split=split, spread_long=spread)  # fmt: skip
+    assert server.fused == fused and server.split == split and server.long_codes == {"C"}
     done = server.serve(reqs)
     assert sorted(r.rid for r in done) == [r.rid for r in reqs]
     assert all(r.latency > 0 for r in done)
