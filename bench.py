@@ -190,34 +190,49 @@ class Clocks:
 
 
 class Dist:
-    """Replicas over torchrun ranks: a barrier and max-over-ranks timing."""
+    """Replicas over torchrun ranks: a barrier and max-over-ranks timing.
 
-    def __init__(self):
+    Every rank decodes its own frames (the workload's seed includes the
+    rank) and nothing is exchanged but the timings, so the whole-job rate
+    is the ranks' units over the slowest rank's time.  ``backend="gloo"``
+    runs the same on CPU processes (tests)."""
+
+    def __init__(self, backend: str = "nccl"):
         self.world = int(os.environ.get("WORLD_SIZE", "1"))
         self.rank = int(os.environ.get("RANK", "0"))
         self.local = int(os.environ.get("LOCAL_RANK", "0"))
         import torch
 
         self.torch = torch
-        torch.cuda.set_device(self.local)
-        self.dev = torch.device("cuda", self.local)
+        self.cuda = backend == "nccl"
+        if self.cuda:
+            torch.cuda.set_device(self.local)
+            self.dev = torch.device("cuda", self.local)
+        else:
+            self.dev = torch.device("cpu")
         if self.world > 1:
             import torch.distributed as dist
 
-            dist.init_process_group("nccl", device_id=self.dev)
+            dist.init_process_group(backend, **({"device_id": self.dev} if self.cuda else {}))
             self.dist = dist
 
     def barrier(self):
         if self.world > 1:
             self.dist.barrier()
-        self.torch.cuda.synchronize()
+        if self.cuda:
+            self.torch.cuda.synchronize()
 
     def max(self, v: float) -> float:
         if self.world == 1:
             return v
-        t = self.torch.tensor([v], device=self.dev)
+        t = self.torch.tensor([v], dtype=self.torch.float64, device=self.dev)
         self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
         return float(t.item())
+
+    def rate(self, units_per_rank: float, ms: float) -> float:
+        """Whole-job units per second: every rank's units over the slowest
+        rank's time (``ms``, already the maximum over ranks)."""
+        return self.world * units_per_rank / (ms * 1e-3)
 
     def close(self):
         if self.world > 1:
@@ -407,7 +422,7 @@ def measure_mixed(args, dist: Dist) -> dict:
     with Clocks(dev.index) as clk:
         ms = timed_flushed(dist, rx.run, args.steps, flush)
         clk.keep_busy(lambda: (flush.zero_(), rx.run()), torch.cuda.synchronize)
-    value = dist.world * info_bits * args.steps / (ms * 1e-3) / 1e9
+    value = dist.rate(info_bits * args.steps, ms) / 1e9
     res = rx.results()
 
     sym_dev = [s.to(dev) for s in sym_host]
@@ -532,28 +547,28 @@ def measure_mixed(args, dist: Dist) -> dict:
                    "launch_shapes": {n: codes[n]._plan(dev.index).get_launch() for n in names},
                    "l2": "flushed before every timed step (256 MB written outside the timed spans)",
                    "parallelism": f"replicas x{dist.world}"},
-        "plain": {"value": dist.world * info_bits * args.steps / (plain_ms * 1e-3) / 1e9,
+        "plain": {"value": dist.rate(info_bits * args.steps, plain_ms) / 1e9,
                   "ms_per_step": plain_ms / args.steps, "bit_identical_to_batched": bool(same),
                   "form": "public API: compute_llr_frames + decode, one call each per code"},
         "batched_over_plain": plain_ms / ms,
         "plain_reference_calls": {
-            "value": dist.world * info_bits * dropin_steps / (dropin_ms * 1e-3) / 1e9,
+            "value": dist.rate(info_bits * dropin_steps, dropin_ms) / 1e9,
             "ms_per_step": dropin_ms / dropin_steps, "steps": dropin_steps,
             "bit_identical_to_batched": bool(dropin_same),
             "batched_over_this": (dropin_ms / dropin_steps) / (ms / args.steps),
             "form": "the reference's drop-in calls only: compute_llr once per frame (one noise variance per call, "
                     "and every frame has its own), then decode once per code"},
-        "unfused": {"value": dist.world * info_bits * args.steps / (unf_ms * 1e-3) / 1e9,
+        "unfused": {"value": dist.rate(info_bits * args.steps, unf_ms) / 1e9,
                     "ms_per_step": unf_ms / args.steps, "bit_identical_to_fused": bool(unf_same),
                     "form": "the demapper kernels first (LLRs through HBM), then the mixed launch"},
-        "e2e": {"value": dist.world * info_bits * args.steps / (e2e_ms * 1e-3) / 1e9, "unit": UNIT,
+        "e2e": {"value": dist.rate(info_bits * args.steps, e2e_ms) / 1e9, "unit": UNIT,
                 "h2d_bytes_per_step": int(sum(s.numel() * 8 for s in sym_host)),
                 "d2h_bytes_per_step": int(sum(sum(t.numel() * t.element_size() for t in o) for o in outs)),
                 "ms_per_step": e2e_ms / args.steps,
                 "form": "MixedReceiver(host_io=True): symbols read from and results written to pinned host "
                         "memory by the kernels each step (NVLink-C2C), graph replay",
                 "bit_identical_to_device": bool(host_same),
-                "with_copies": {"value": dist.world * info_bits * args.steps / (copy_ms * 1e-3) / 1e9,
+                "with_copies": {"value": dist.rate(info_bits * args.steps, copy_ms) / 1e9,
                                 "ms_per_step": copy_ms / args.steps,
                                 "form": "copy_ in, graph replay, copy_ out (pinned host buffers)"}},
         "gpu_launches": (1 + sum(not f for f in rx.fused)) * args.steps,
@@ -632,9 +647,9 @@ def measure_single(args, dist: Dist, wname: str) -> dict:
     ksym = const.bits_per_symbol
     demap_bytes = code.n // ksym * frames * (8 + 4 * ksym)
     return {
-        "workload": w["desc"], "value": dist.world * frames * code.k * args.steps / (ms * 1e-3) / 1e9,
+        "workload": w["desc"], "value": dist.rate(frames * code.k * args.steps, ms) / 1e9,
         "unit": UNIT, "ms_per_step": ms / args.steps,
-        "e2e": {"value": dist.world * frames * code.k * args.steps / (e2e_ms * 1e-3) / 1e9,
+        "e2e": {"value": dist.rate(frames * code.k * args.steps, e2e_ms) / 1e9,
                 "h2d_bytes_per_step": int(sym_host.numel() * 8),
                 "d2h_bytes_per_step": int(sum(t.numel() * t.element_size() for t in out))},
         "launch_shape": code._plan(dev.index).get_launch(),
