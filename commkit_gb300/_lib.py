@@ -126,6 +126,7 @@ class Batch(ctypes.Structure):
         ("axis_re", ctypes.POINTER(AxisMaxlog)),
         ("axis_im", ctypes.POINTER(AxisMaxlog)),
         ("frames_per_block", ctypes.c_int32),
+        ("threads_per_frame", ctypes.c_int32),
     ]
 
 

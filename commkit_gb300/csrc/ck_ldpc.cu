@@ -652,7 +652,9 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
         }
         if (plan->max_deg > 16) R->wide = true;
         const int32_t Zp = (plan->Z + 31) / 32 * 32;
-        int32_t T = plan->launch.threads_per_frame;
+        int32_t T = b.threads_per_frame > 0 ? b.threads_per_frame : plan->launch.threads_per_frame;
+        if (b.threads_per_frame < 0)
+            return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: bad threads_per_frame", c);
         if (T == 0) {
             T = Zp;
             while (T > 512 && T % 64 == 0) T /= 2;

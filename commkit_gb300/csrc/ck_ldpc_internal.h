@@ -98,12 +98,13 @@ namespace ldpc {
 int specialised_kernel(const ck_ldpc_plan* plan, int dmax, bool r_smem, const void** out);
 // The NVRTC source of a circulant plan's specialised kernels.
 std::string specialised_source(const ck_ldpc_plan& plan, int dmax);
-// The NVRTC source of the specialised mixed kernel of n plans.
-std::string mixed_source(const ck_ldpc_plan* const* plans, const bool* special, int n, int dmax);
+// The NVRTC source of the specialised mixed kernel of n plans, batch c with
+// parts[c] threads per row slot (0: the table loop).
+std::string mixed_source(const ck_ldpc_plan* const* plans, const int* parts, int n, int dmax);
 // The code-specialised mixed kernel for these plans with threads per frame
-// T[c] (codes with T[c] == Z rounded up to whole warps run their programs,
-// the others the table loop), compiled on first use; nullptr in *out when
-// there is none.
+// T[c] (batches with T[c] == Zp or 2 Zp, Zp = Z rounded up to whole warps,
+// run their code's program, the others the table loop), compiled on first
+// use; nullptr in *out when there is none.
 int mixed_specialised_kernel(const ck_ldpc_plan* const* plans, const int32_t* T, int n, int dmax,
                              const void** out);
 // Unloads the specialised kernels that use `plan` (before it is freed).

@@ -21,6 +21,7 @@
 #include <dlfcn.h>
 #include <stdlib.h>
 
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <string>
@@ -96,10 +97,38 @@ void add(std::string& s, const char* fmt, long long a = 0, long long b = 0, long
     s += buf;
 }
 
+// The base rows of layer l that part h of H runs (H threads per row slot,
+// part = thread / Zp): balanced by edges, the heaviest row to the lighter
+// part first, then in base-row order.  The rows of a layer share no
+// variable, so any split gives the same bits.
+std::vector<int32_t> layer_part(const ck_ldpc_plan& plan, int32_t l, int H, int h) {
+    std::vector<int32_t> rows;
+    for (int32_t b = plan.h_layer[l]; b < plan.h_layer[l + 1]; ++b) rows.push_back(b);
+    if (H == 1) return rows;
+    std::vector<int32_t> order = rows;
+    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
+        return plan.h_eptr[x + 1] - plan.h_eptr[x] > plan.h_eptr[y + 1] - plan.h_eptr[y];
+    });
+    std::vector<long long> load(H, 0);
+    std::vector<int32_t> mine;
+    for (int32_t b : order) {
+        int best = 0;
+        for (int q = 1; q < H; ++q)
+            if (load[q] < load[best]) best = q;
+        load[best] += plan.h_eptr[b + 1] - plan.h_eptr[b];
+        if (best == h) mine.push_back(b);
+    }
+    std::sort(mine.begin(), mine.end());
+    return mine;
+}
+
 // The program of one circulant code, as struct `name`: every layer's base
 // rows, each as its columns (row qr0 of circulant (j, shift) is column j Z +
 // (qr0 + shift) mod Z) and its state row b Z + qr0, then the group barrier.
-std::string program_struct(const ck_ldpc_plan& plan, const char* name) {
+// With H parts (threads per frame = H Zp), part h runs its share of each
+// layer's base rows (layer_part), warp-uniformly, so a frame's layer takes
+// H times fewer rows per thread.
+std::string program_struct(const ck_ldpc_plan& plan, const char* name, int H = 1) {
     const int32_t Z = plan.Z, Zp = (Z + 31) / 32 * 32;
     // ceil(2^32 / Z): the high word of (qr0 + shift) * magic is the wrap bit.
     const unsigned long long magic = ((1ull << 32) + static_cast<unsigned long long>(Z) - 1) / static_cast<unsigned long long>(Z);
@@ -108,17 +137,19 @@ std::string program_struct(const ck_ldpc_plan& plan, const char* name) {
     s += name;
     s += " {\n";
     s += "    static constexpr bool kSpecialised = true;\n";
+    add(s, "    static constexpr int kParts = %lld;\n", H);
     s += "    template <class St>\n";
     s += "    __device__ __forceinline__ static void iteration(const St& st, const uint32_t base4_in, const uint32_t qr0_in,\n";
     s += "                                                     const float scale, const float offset, const int bar,\n";
-    s += "                                                     const int T) {\n";
+    s += "                                                     const int T, const uint32_t part_in) {\n";
     // Opaque copies of the thread's offsets, taken anew each iteration: the
     // columns and state addresses derived from them are then computed where
     // they are used instead of being hoisted out of the iteration loop and
     // held (or spilled) across it.
-    s += "        uint32_t base4, qr0;\n";
+    s += "        uint32_t base4, qr0, part;\n";
     s += "        asm volatile(\"mov.b32 %0, %1;\" : \"=r\"(base4) : \"r\"(base4_in));\n";
     s += "        asm volatile(\"mov.b32 %0, %1;\" : \"=r\"(qr0) : \"r\"(qr0_in));\n";
+    s += "        asm volatile(\"mov.b32 %0, %1;\" : \"=r\"(part) : \"r\"(part_in));\n";
     // Each row's message state in device memory is loaded one row ahead
     // (the thread's own rows: no other thread writes them, so the load may
     // cross a barrier), which hides its L2 latency behind the previous row's
@@ -129,31 +160,75 @@ std::string program_struct(const ck_ldpc_plan& plan, const char* name) {
         std::string r = std::to_string(static_cast<long long>(b) * Z) + "u + ";
         return r + (pad ? "(qr0 < " + std::to_string(Z) + "u ? qr0 : 0u)" : std::string("qr0"));
     };
-    if (plan.mb > 0) s += "        uint4 next = st.pre(" + row_of(plan.h_layer[0]) + ");\n";
+    // Each part's chain of rows, layer by layer.
+    std::vector<std::vector<std::vector<int32_t>>> parts(H);
+    std::vector<std::vector<int32_t>> chain(H);
+    for (int h = 0; h < H; ++h)
+        for (int32_t l = 0; l < plan.L; ++l) {
+            parts[h].push_back(layer_part(plan, l, H, h));
+            chain[h].insert(chain[h].end(), parts[h].back().begin(), parts[h].back().end());
+        }
+    if (H == 1) {
+        if (!chain[0].empty()) s += "        uint4 next = st.pre(" + row_of(chain[0][0]) + ");\n";
+    } else {
+        s += "        uint4 next = make_uint4(0u, 0u, 0u, 0u);\n";
+        for (int h = 0; h < H; ++h)
+            if (!chain[h].empty()) {
+                add(s, "        if (part == %lldu) next = st.pre(", h);
+                s += row_of(chain[h][0]) + ");\n";
+            }
+    }
+    std::vector<size_t> pos(H, 0);  // position in each part's chain
+    auto emit_row = [&](int h, int32_t b, const char* ind) {
+        const int32_t e0 = plan.h_eptr[b], deg = plan.h_eptr[b + 1] - e0;
+        const size_t at = pos[h]++;
+        s += ind;
+        s += "{\n";
+        s += ind;
+        s += "    const uint4 cur = st.take(next, " + row_of(b) + ");\n";
+        if (at + 1 < chain[h].size()) {
+            s += ind;
+            s += "    next = st.pre(" + row_of(chain[h][at + 1]) + ");\n";
+        }
+        if (pad) {
+            s += ind;
+            add(s, "    if (qr0 < %lldu) {\n", Z);
+        }
+        s += ind;
+        add(s, "    uint32_t c[%lld];\n", deg);
+        for (int32_t e = 0; e < deg; ++e) {
+            const int32_t first = plan.h_blk[2 * (e0 + e)];    // j Z + shift
+            const int32_t end = plan.h_blk[2 * (e0 + e) + 1];  // (j + 1) Z
+            const long long shift = Z - (end - first);
+            s += ind;
+            if (shift == 0) {
+                add(s, "    c[%lld] = base4 + %lldu;\n", e, 4ll * first);
+            } else {
+                add(s, "    c[%lld] = wrapped_base(base4, qr0, %lluu, %lluull, ", e,
+                    static_cast<long long>(magic), static_cast<long long>(magic * static_cast<unsigned long long>(shift)));
+                add(s, "%lluu) + %lldu;\n", static_cast<long long>((0x100000000ull - 4ull * Z) & 0xffffffffull),
+                    4ll * first);
+            }
+        }
+        s += ind;
+        add(s, "    st.template row_cols<%lld>(c, cur, %lldu + qr0, scale, offset);\n", deg,
+            static_cast<long long>(b) * Z);
+        if (pad) {
+            s += ind;
+            s += "    }\n";
+        }
+        s += ind;
+        s += "}\n";
+    };
     for (int32_t l = 0; l < plan.L; ++l) {
         add(s, "        // layer %lld\n", l);
-        for (int32_t b = plan.h_layer[l]; b < plan.h_layer[l + 1]; ++b) {
-            const int32_t e0 = plan.h_eptr[b], deg = plan.h_eptr[b + 1] - e0;
-            s += "        {\n            const uint4 cur = st.take(next, " + row_of(b) + ");\n";
-            if (b + 1 < plan.mb) s += "            next = st.pre(" + row_of(b + 1) + ");\n";
-            if (pad) add(s, "            if (qr0 < %lldu) {\n", Z);
-            add(s, "            uint32_t c[%lld];\n", deg);
-            for (int32_t e = 0; e < deg; ++e) {
-                const int32_t first = plan.h_blk[2 * (e0 + e)];    // j Z + shift
-                const int32_t end = plan.h_blk[2 * (e0 + e) + 1];  // (j + 1) Z
-                const long long shift = Z - (end - first);
-                if (shift == 0) {
-                    add(s, "            c[%lld] = base4 + %lldu;\n", e, 4ll * first);
-                } else {
-                    add(s, "            c[%lld] = wrapped_base(base4, qr0, %lluu, %lluull, ", e,
-                        static_cast<long long>(magic), static_cast<long long>(magic * static_cast<unsigned long long>(shift)));
-                    add(s, "%lluu) + %lldu;\n", static_cast<long long>((0x100000000ull - 4ull * Z) & 0xffffffffull),
-                        4ll * first);
-                }
+        if (H == 1) {
+            for (int32_t b : parts[0][l]) emit_row(0, b, "        ");
+        } else {
+            for (int h = 0; h < H; ++h) {
+                add(s, h == 0 ? "        if (part == %lldu) {\n" : "        } else if (part == %lldu) {\n", h);
+                for (int32_t b : parts[h][l]) emit_row(h, b, "            ");
             }
-            add(s, "            st.template row_cols<%lld>(c, cur, %lldu + qr0, scale, offset);\n", deg,
-                static_cast<long long>(b) * Z);
-            if (pad) s += "            }\n";
             s += "        }\n";
         }
         s += "        ck::group_sync(bar, T);\n";
@@ -164,35 +239,64 @@ std::string program_struct(const ck_ldpc_plan& plan, const char* name) {
     // sign bit is "< 0"), ORed over a round of base rows, one group OR per
     // round, stopping at the first unsatisfied round.  The first round is
     // one base row (an unconverged frame usually fails there), the others
-    // eight (a converged frame pays for few group ORs).
+    // eight (a converged frame pays for few group ORs).  With H parts, part
+    // h takes every H-th row of a round.
     s += "    __device__ __forceinline__ static bool syndrome(const uint32_t base4_in, const uint32_t qr0_in,\n";
-    s += "                                                    const int bar, const int T) {\n";
-    s += "        uint32_t base4, qr0;\n";
+    s += "                                                    const int bar, const int T, const uint32_t part_in) {\n";
+    s += "        uint32_t base4, qr0, part;\n";
     s += "        asm volatile(\"mov.b32 %0, %1;\" : \"=r\"(base4) : \"r\"(base4_in));\n";
     s += "        asm volatile(\"mov.b32 %0, %1;\" : \"=r\"(qr0) : \"r\"(qr0_in));\n";
+    s += "        asm volatile(\"mov.b32 %0, %1;\" : \"=r\"(part) : \"r\"(part_in));\n";
     s += "        uint32_t bad = 0u;\n";
-    for (int32_t b = 0; b < plan.mb; ++b) {
+    auto emit_parity = [&](int32_t b, const char* ind) {
         const int32_t e0 = plan.h_eptr[b], deg = plan.h_eptr[b + 1] - e0;
-        s += "        {\n            uint32_t x = 0u;\n";
-        if (pad) add(s, "            if (qr0 < %lldu) {\n", Z);
+        s += ind;
+        s += "{\n";
+        s += ind;
+        s += "    uint32_t x = 0u;\n";
+        if (pad) {
+            s += ind;
+            add(s, "    if (qr0 < %lldu) {\n", Z);
+        }
         for (int32_t e = 0; e < deg; ++e) {
             const int32_t first = plan.h_blk[2 * (e0 + e)];
             const int32_t end = plan.h_blk[2 * (e0 + e) + 1];
             const long long shift = Z - (end - first);
+            s += ind;
             if (shift == 0) {
-                add(s, "            x ^= __float_as_uint(ld_shared_f32(base4 + %lldu));\n", 4ll * first);
+                add(s, "    x ^= __float_as_uint(ld_shared_f32(base4 + %lldu));\n", 4ll * first);
             } else {
-                add(s, "            x ^= __float_as_uint(ld_shared_f32(wrapped_base(base4, qr0, %lluu, %lluull, ",
+                add(s, "    x ^= __float_as_uint(ld_shared_f32(wrapped_base(base4, qr0, %lluu, %lluull, ",
                     static_cast<long long>(magic), static_cast<long long>(magic * static_cast<unsigned long long>(shift)));
                 add(s, "%lluu) + %lldu));\n", static_cast<long long>((0x100000000ull - 4ull * Z) & 0xffffffffull),
                     4ll * first);
             }
         }
-        if (pad) s += "            }\n";
-        s += "            bad |= x >> 31;\n        }\n";
+        if (pad) {
+            s += ind;
+            s += "    }\n";
+        }
+        s += ind;
+        s += "    bad |= x >> 31;\n";
+        s += ind;
+        s += "}\n";
+    };
+    int32_t round_start = 0;
+    for (int32_t b = 0; b < plan.mb; ++b) {
         if (b == 0 || b % 8 == 0 || b + 1 == plan.mb) {
+            // rows round_start .. b form a round
+            if (H == 1) {
+                for (int32_t r = round_start; r <= b; ++r) emit_parity(r, "        ");
+            } else {
+                for (int h = 0; h < H; ++h) {
+                    add(s, h == 0 ? "        if (part == %lldu) {\n" : "        } else if (part == %lldu) {\n", h);
+                    for (int32_t r = round_start + h; r <= b; r += H) emit_parity(r, "            ");
+                }
+                s += "        }\n";
+            }
             s += "        if (ck::group_any(static_cast<int>(bad), bar, T)) return false;\n";
             if (b + 1 < plan.mb) s += "        bad = 0u;\n";
+            round_start = b + 1;
         }
     }
     s += "        return true;\n    }\n};\n";
@@ -217,21 +321,25 @@ std::string program_source(const ck_ldpc_plan& plan, int dmax) {
     return s;
 }
 
-// The mixed decoder of n codes; code c runs its program when special[c].
-std::string mixed_program_source(const ck_ldpc_plan* const* plans, const bool* special, int n, int dmax) {
+// The mixed decoder of n batches; batch c runs its code's program with
+// parts[c] threads per row slot when parts[c] > 0, else the table loop.
+std::string mixed_program_source(const ck_ldpc_plan* const* plans, const int* parts, int n, int dmax) {
     std::string s = "#include \"ck_ldpc_mixed.cuh\"\nusing namespace ck::ldpc;\nnamespace {\n";
     // A code may fill several batches (one per constellation): one program
-    // and one call site per distinct (plan, specialised), its batches as
-    // cases of the same branch.
+    // and one call site per distinct (plan, parts), its batches as cases of
+    // the same branch.
     std::vector<int> first(n);
+    std::vector<bool> special(n);
     for (int c = 0; c < n; ++c) {
+        special[c] = parts[c] > 0;
         first[c] = c;
         for (int u = 0; u < c; ++u)
-            if (plans[u] == plans[c] && special[u] == special[c]) {
+            if (plans[u] == plans[c] && parts[u] == parts[c]) {
                 first[c] = u;
                 break;
             }
-        if (first[c] == c && special[c]) s += program_struct(*plans[c], ("CodeProgram" + std::to_string(c)).c_str());
+        if (first[c] == c && special[c])
+            s += program_struct(*plans[c], ("CodeProgram" + std::to_string(c)).c_str(), parts[c]);
     }
     s += "struct CodeDispatch {\n";
     s += "    template <int DMAX>\n";
@@ -332,8 +440,8 @@ std::map<std::vector<uint64_t>, MixedJit> g_mixed;
 
 std::string specialised_source(const ck_ldpc_plan& plan, int dmax) { return program_source(plan, dmax); }
 
-std::string mixed_source(const ck_ldpc_plan* const* plans, const bool* special, int n, int dmax) {
-    return mixed_program_source(plans, special, n, dmax);
+std::string mixed_source(const ck_ldpc_plan* const* plans, const int* parts, int n, int dmax) {
+    return mixed_program_source(plans, parts, n, dmax);
 }
 
 int specialised_kernel(const ck_ldpc_plan* plan, int dmax, bool r_smem, const void** out) {
@@ -361,7 +469,7 @@ int specialised_kernel(const ck_ldpc_plan* plan, int dmax, bool r_smem, const vo
 int mixed_specialised_kernel(const ck_ldpc_plan* const* plans, const int32_t* T, int n, int dmax,
                              const void** out) {
     *out = nullptr;
-    bool special[CK_LDPC_MAX_MIXED] = {};
+    int parts[CK_LDPC_MAX_MIXED] = {};
     if (n < 1 || n > CK_LDPC_MAX_MIXED) return CK_OK;
     bool any = false, required = false;
     std::vector<uint64_t> key{static_cast<uint64_t>(dmax)};
@@ -369,10 +477,13 @@ int mixed_specialised_kernel(const ck_ldpc_plan* const* plans, const int32_t* T,
         const int mode = effective_mode(plans[c]->jit_mode);
         if (mode == CK_LDPC_SPECIALISE_OFF) return CK_OK;  // any code opting out keeps the table kernel
         required |= mode == CK_LDPC_SPECIALISE_ON;
-        special[c] = T[c] == (plans[c]->Z + 31) / 32 * 32;
-        any |= special[c];
+        // One or two threads per row slot (threads per frame Zp or 2 Zp) run
+        // the code's program; other shapes run the table loop.
+        const int32_t Zp = (plans[c]->Z + 31) / 32 * 32;
+        parts[c] = T[c] == Zp ? 1 : (T[c] == 2 * Zp ? 2 : 0);
+        any |= parts[c] > 0;
         key.push_back(plans[c]->id);
-        key.push_back(special[c] ? 1u : 0u);
+        key.push_back(static_cast<uint64_t>(parts[c]));
     }
     if (!any) return CK_OK;
     std::lock_guard<std::mutex> lock(g_mixed_mu);
@@ -382,7 +493,7 @@ int mixed_specialised_kernel(const ck_ldpc_plan* const* plans, const int32_t* T,
         static const char* const names[] = {"ck_ldpc_mixed_code"};
         const void* k = nullptr;
         const int dev = plans[0]->device;
-        if (compile_load(mixed_program_source(plans, special, n, dmax), dev, names, 1, &mj.lib, &k, &mj.why))
+        if (compile_load(mixed_program_source(plans, parts, n, dmax), dev, names, 1, &mj.lib, &k, &mj.why))
             mj.kernel = k;
         it = g_mixed.emplace(key, std::move(mj)).first;
     }

@@ -300,7 +300,7 @@ __device__ __forceinline__ void decode_body(const Params& p) {
         auto satisfied = [&]() -> bool {
             if constexpr (Prog::kSpecialised)
                 return Prog::syndrome(ck::smem_addr(a) + 4u * static_cast<uint32_t>(qr0),
-                                      static_cast<uint32_t>(qr0), bar, p.T);
+                                      static_cast<uint32_t>(qr0), bar, p.T, static_cast<uint32_t>(qb0));
             return syndrome_ok<QC>(p, a, s_eptr, s_blk, tid, bar, qr0, qb0);
         };
         // One call site of the test (it is long when generated): before the
@@ -312,7 +312,7 @@ __device__ __forceinline__ void decode_body(const Params& p) {
             if (ok || it >= p.max_iterations) break;
             if constexpr (Prog::kSpecialised) {
                 Prog::iteration(st, ck::smem_addr(a) + 4u * static_cast<uint32_t>(qr0),
-                                static_cast<uint32_t>(qr0), p.scale, p.offset, bar, p.T);
+                                static_cast<uint32_t>(qr0), p.scale, p.offset, bar, p.T, static_cast<uint32_t>(qb0));
             }
             for (int32_t l = 0; l < p.L && QC && ONE_ROW && !Prog::kSpecialised; ++l) {
                 if (qr0 < p.Z) {  // lanes past Z (Z % 32 != 0) only meet the barriers

@@ -193,7 +193,7 @@ __device__ __forceinline__ void mixed_frames(const MixedCode& K, unsigned char* 
 
     auto syndrome_ok = [&]() -> bool {
         if constexpr (Prog::kSpecialised)
-            return Prog::syndrome(a_addr + r4, static_cast<uint32_t>(qr0), bar, K.T);
+            return Prog::syndrome(a_addr + r4, static_cast<uint32_t>(qr0), bar, K.T, static_cast<uint32_t>(qb0));
         return syndrome_table();
     };
 
@@ -234,7 +234,8 @@ __device__ __forceinline__ void mixed_frames(const MixedCode& K, unsigned char* 
                 st.store(row, m1, m2, w);
             };
             if constexpr (Prog::kSpecialised)
-                Prog::iteration(st, a_addr + r4, static_cast<uint32_t>(qr0), K.scale, K.offset, bar, K.T);
+                Prog::iteration(st, a_addr + r4, static_cast<uint32_t>(qr0), K.scale, K.offset, bar, K.T,
+                                static_cast<uint32_t>(qb0));
             for (int32_t l = 0; l < K.L && !Prog::kSpecialised; ++l) {
                 const int32_t b1 = s_layer[l + 1];
                 if (!ONE_ROW || qr0 < K.Z) {

@@ -278,15 +278,15 @@ extern "C" int ck_ldpc_specialised_source(const int32_t* row_ptr, const int32_t*
                                           int32_t form, char* out, size_t capacity, size_t* length) {
     ck::clear_error();
     if (!length) return ck::fail(CK_ERR_INVALID_ARGUMENT, "length is NULL");
-    if (form != 0 && form != 1) return ck::fail(CK_ERR_INVALID_ARGUMENT, "form must be 0 or 1");
+    if (form < 0 || form > 2) return ck::fail(CK_ERR_INVALID_ARGUMENT, "form must be 0, 1 or 2");
     ck_ldpc_plan plan;
     CK_TRY(plan_host(row_ptr, cols, layer_ptr, m, N, L, &plan));
     if (!plan.qc) return ck::fail(CK_ERR_UNSUPPORTED, "the schedule has no circulant structure");
     const int dmax = plan.max_deg <= 16 ? 16 : 27;
     const ck_ldpc_plan* plans[1] = {&plan};
-    const bool special[1] = {true};
+    const int parts[1] = {form};  // form 1: one thread per row slot, 2: two
     const std::string src =
-        form == 0 ? ck::ldpc::specialised_source(plan, dmax) : ck::ldpc::mixed_source(plans, special, 1, dmax);
+        form == 0 ? ck::ldpc::specialised_source(plan, dmax) : ck::ldpc::mixed_source(plans, parts, 1, dmax);
     *length = src.size();
     if (out && capacity > 0) {
         const size_t n = std::min(capacity - 1, src.size());

@@ -202,7 +202,8 @@ class Server:
     launches before the decoder (the same bits).  ``priority_split``
     decodes the long codes' frames of a batch in their own launch, the
     others' on a higher-priority stream (the same bits).  ``spread_long``
-    gives each long frame a thread block, and so an SM, of its own.
+    gives each long frame a thread block, and so an SM, of its own, with
+    two threads per row slot (the same bits).
     """
 
     def __init__(self, codes: dict[str, LDPCCode], method: MinSum, *, hbm_budget: int = 4 << 30,
@@ -301,7 +302,9 @@ class Server:
                                 int(m.max_iterations), 1 if m.early_stop else 0, it_o, ok_o, bits_o,
                                 code.k)  # fmt: skip
             if self.spread_long and name in self.long_codes:
+                # One frame per block, on two threads per row slot.
                 arr[i].frames_per_block = 1
+                arr[i].threads_per_frame = 2 * ((code._plan(self.device.index).info["lifting"] + 31) // 32 * 32)
             if order is not None:
                 re, im, _ = self._tables[order]
                 arr[i].symbols = slot.sym_dev.data_ptr() + 8 * g_sym

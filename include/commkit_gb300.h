@@ -343,7 +343,8 @@ int ck_ldpc_plan_get_specialise(const ck_ldpc_plan* plan, int32_t* mode, int32_t
 /*
  * The CUDA source a plan of this schedule would compile for its
  * code-specialised kernels (host only, no device needed): form 0 the plain
- * decoder, form 1 a mixed decoder of this code alone.  *length gets its
+ * decoder, form 1 a mixed decoder of this code alone, form 2 the same with
+ * two threads per row slot (threads per frame 2 Zp).  *length gets its
  * size, and up to capacity - 1 bytes of it go to `out` (NUL-terminated).
  * CK_ERR_UNSUPPORTED when the schedule is not circulant.
  */
@@ -433,6 +434,10 @@ typedef struct ck_ldpc_batch {
      * as fit.  1 gives each frame an SM of its own (a launch's blocks are
      * sized for its largest code), so a long frame finishes sooner. */
     int32_t frames_per_block;
+    /* Threads per frame for this batch, 0 for the plan's launch shape.  2 Zp
+     * (Zp = Z rounded up to whole warps) runs each layer's base rows on two
+     * threads per row slot: a frame's layers take about half as long. */
+    int32_t threads_per_frame;
 } ck_ldpc_batch;
 
 #define CK_LDPC_MAX_MIXED 12

@@ -23,11 +23,11 @@ def _batch(ck, dev, name, frames, order, ebn0, seed):
 
 
 @pytest.mark.parametrize("placement", [0, 2])
-@pytest.mark.parametrize("specialise", ["table_plain", "both_auto"])
-def test_mixed_launch_matches_plain_calls(placement, specialise):
+@pytest.mark.parametrize("specialise,parts", [("table_plain", 1), ("both_auto", 1), ("both_auto", 2)])
+def test_mixed_launch_matches_plain_calls(placement, specialise, parts):
     """table_plain: plain calls on the table-driven kernel, the mixed launch
     on the code-specialised one (compiled at run time); both_auto: both
-    specialised."""
+    specialised; parts 2: the mixed launch with two threads per row slot."""
     import torch
 
     import commkit_gb300 as ck
@@ -46,6 +46,8 @@ def test_mixed_launch_matches_plain_calls(placement, specialise):
         batches.append((llr, code, method))
         plain.append(ck.decode(llr, code=code, method=method))
         code._plan(0).set_specialise(_lib.CK_LDPC_SPECIALISE_AUTO)
+        if parts == 2:
+            code._plan(0).set_launch(2 * ((code._plan(0).info["lifting"] + 31) // 32 * 32), 0, placement)
     mixed = ck.decode_mixed(batches)
     for (llr, code, method), p, m in zip(batches, plain, mixed, strict=True):
         frames = llr.shape[0]

@@ -87,6 +87,11 @@ def test_specialised_source_compiles(name):
     assert "ck_ldpc_mixed_code" in mixed and "CodeProgram0" in mixed
     st, log = compile_nvrtc(mixed)
     assert st == 0, log[:3000]
+    # Two threads per row slot: every row body once, split between the parts.
+    split = source(*sched, m, n, form=2)
+    assert "kParts = 2" in split and split.count("st.template row_cols<") == bodies
+    st, log = compile_nvrtc(split)
+    assert st == 0, log[:3000]
 
 
 def test_csr_schedule_has_no_specialised_source():
