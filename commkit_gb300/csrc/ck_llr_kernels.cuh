@@ -13,8 +13,10 @@
 //    512 B in and 32*2k*4 B out per step, contiguous, no shared-memory
 //    staging (the reference stages every tile through shared memory to
 //    coalesce k-strided stores);
-//  * two symbol pairs are in flight per thread per step, and the grid is a
-//    multiple of the SM count, so the memory system sees enough requests;
+//  * two symbol pairs are in flight per thread per step, and the grid is
+//    the SM count times the blocks resident per SM (occupancy query), so
+//    the memory system sees enough requests and no block runs in a second
+//    wave;
 //  * the per-axis tables (levels, labels, opposite levels, bit positions)
 //    live in shared memory, indexed by the data-dependent snapped level;
 //  * the bits-per-axis count is a template parameter, so every per-bit
@@ -43,6 +45,7 @@ int num_sms();
 
 
 constexpr int kThreads = 256;
+constexpr int kOccupancyDevices = 64;  // launch shapes cached per device
 constexpr float kExactFloor = 1e-26f;
 
 __device__ __forceinline__ float4 ld_stream(const float4* p) { return __ldcs(p); }
@@ -253,9 +256,12 @@ __device__ __forceinline__ void store_scattered(const T& tab, float* out, uint32
 
 // Main kernel: two symbols per 16-byte load, two loads in flight per thread.
 // PAIRS = false is the fallback for buffers that are not 16-byte aligned:
-// one symbol per thread and scalar stores.
+// one symbol per thread and scalar stores.  The closed form is held to 32
+// registers, so 8 blocks (64 warps) share an SM and keep more loads in
+// flight (38-40 registers left 6 blocks: 64-QAM 33.0 -> 31.0 us at 2^22
+// symbols, 16-QAM unchanged, a few bytes of spill outside the main loop).
 template <int KA, int METHOD, bool PAIRS>
-__global__ void __launch_bounds__(kThreads) llr_kernel(const float2* __restrict__ x, uint32_t n,
+__global__ void __launch_bounds__(kThreads, METHOD == 0 ? 8 : 1) llr_kernel(const float2* __restrict__ x, uint32_t n,
                                                        const typename AxisArg<METHOD>::type re,
                                                        const typename AxisArg<METHOD>::type im,
                                                        const NoiseScale noise,
@@ -355,13 +361,27 @@ int launch_ka(const void* x, uint32_t n, const AX& re, const AX& im, const Noise
                          (reinterpret_cast<uintptr_t>(out) % 16 == 0);
     const uint32_t work = aligned ? (n / 2 + 1) : n;
     const uint32_t want = (work + kThreads - 1) / kThreads;
-    const uint32_t cap = static_cast<uint32_t>(num_sms()) * 8u;  // 8 blocks of 256 per SM
+    using Kernel = void (*)(const float2*, uint32_t, const typename AxisArg<METHOD>::type,
+                            const typename AxisArg<METHOD>::type, const NoiseScale, float*);
+    const Kernel kernel = aligned ? llr_kernel<KA, METHOD, true> : llr_kernel<KA, METHOD, false>;
+    // The grid-stride loop gives every block the same share, so the grid is
+    // the blocks that are resident at once (registers decide: 38-40
+    // registers leave 6 blocks of 256 per SM, and a grid of 8 per SM ran its
+    // last quarter as a second, thin wave).  Cached per device and form.
+    static int per_sm_cache[2][kOccupancyDevices] = {};
+    int dev = 0;
+    CK_CUDA(cudaGetDevice(&dev));
+    int per_sm = dev < kOccupancyDevices ? per_sm_cache[aligned][dev] : 0;
+    if (per_sm == 0) {
+        CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(kernel),
+                                                              kThreads, 0));
+        if (per_sm < 1) return ck::fail(CK_ERR_UNSUPPORTED, "LLR block does not fit an SM");
+        if (dev < kOccupancyDevices) per_sm_cache[aligned][dev] = per_sm;
+    }
+    const uint32_t cap = static_cast<uint32_t>(num_sms()) * static_cast<uint32_t>(per_sm);
     const uint32_t blocks = want < cap ? (want > 0 ? want : 1) : cap;
     const float2* xs = static_cast<const float2*>(x);
-    if (aligned)
-        llr_kernel<KA, METHOD, true><<<blocks, kThreads, 0, stream>>>(xs, n, re, im, noise, out);
-    else
-        llr_kernel<KA, METHOD, false><<<blocks, kThreads, 0, stream>>>(xs, n, re, im, noise, out);
+    kernel<<<blocks, kThreads, 0, stream>>>(xs, n, re, im, noise, out);
     return ck::cuda_check(cudaGetLastError(), "LLR kernel launch");
 }
 
