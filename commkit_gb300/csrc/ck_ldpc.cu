@@ -373,13 +373,27 @@ int check_device(const ck_ldpc_plan* plan) {
 
 // Argument checks shared by the decode entry points (the reference's
 // wrapper checks, commkit/_cuda/coding.py:27-67, plus this ABI's own).
+// The min-sum parameters the reference's MinSum accepts
+// (commkit/coding/ldpc.py:345-347): scale finite in (0, 1], offset finite
+// and >= 0.  A C caller gets the same refusal as a Python one, before any
+// launch.
+int check_min_sum_params(float scale, float offset) {
+    if (!(scale > 0.0f && scale <= 1.0f))
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "scale must be in (0, 1], got %g", static_cast<double>(scale));
+    if (!(offset >= 0.0f && offset <= 3.4028234663852886e38f))
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "offset must be finite and >= 0, got %g",
+                        static_cast<double>(offset));
+    return CK_OK;
+}
+
 int check_decode_args(const ck_ldpc_plan* plan, const float* llr_in, const float* llr_out,
-                      int64_t B, int32_t n_in, int32_t rule, int32_t max_iterations,
-                      const int32_t* iters, const uint8_t* valid, const int8_t* bits,
-                      int32_t k_bits) {
+                      int64_t B, int32_t n_in, int32_t rule, float scale, float offset,
+                      int32_t max_iterations, const int32_t* iters, const uint8_t* valid,
+                      const int8_t* bits, int32_t k_bits) {
     if (!plan) return ck::fail(CK_ERR_INVALID_ARGUMENT, "plan is NULL");
     if (rule != CK_LDPC_MIN_SUM && rule != CK_LDPC_SUM_PRODUCT)
         return ck::fail(CK_ERR_INVALID_ARGUMENT, "unknown check rule %d", rule);
+    if (rule == CK_LDPC_MIN_SUM) CK_TRY(check_min_sum_params(scale, offset));
     if (B < 0 || B >= (int64_t(1) << 31))
         return ck::fail(CK_ERR_INVALID_ARGUMENT, "B must be in [0, 2**31), got %lld",
                         static_cast<long long>(B));
@@ -470,8 +484,8 @@ extern "C" int ck_ldpc_decode(const ck_ldpc_plan* plan, const float* llr_in, flo
                               uint8_t* valid, int8_t* bits, int32_t k_bits, void* workspace,
                               size_t workspace_bytes, void* stream) {
     ck::clear_error();
-    CK_TRY(check_decode_args(plan, llr_in, llr_out, B, n_in, rule, max_iterations, iters, valid,
-                             bits, k_bits));
+    CK_TRY(check_decode_args(plan, llr_in, llr_out, B, n_in, rule, scale, offset, max_iterations,
+                             iters, valid, bits, k_bits));
     if (B == 0) return CK_OK;
     CK_TRY(check_device(plan));
     Resolved r;
@@ -525,8 +539,8 @@ int ck::ldpc_decode_in_scratch(const ck_ldpc_plan* plan, const float* llr_in, fl
                                int32_t max_iterations, int32_t early_stop, int32_t* iters,
                                uint8_t* valid, int8_t* bits, int32_t k_bits, void* scratch,
                                size_t scratch_bytes, cudaStream_t s) {
-    CK_TRY(check_decode_args(plan, llr_in, llr_out, B, n_in, rule, max_iterations, iters, valid,
-                             bits, k_bits));
+    CK_TRY(check_decode_args(plan, llr_in, llr_out, B, n_in, rule, scale, offset, max_iterations,
+                             iters, valid, bits, k_bits));
     if (B == 0) return CK_OK;
     if (reinterpret_cast<uintptr_t>(scratch) % 256)
         return ck::fail(CK_ERR_INVALID_ARGUMENT, "scratch must be 256-byte aligned");
@@ -622,6 +636,7 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
                             plan->device, dev);
         if (!plan->qc) return ck::fail(CK_ERR_UNSUPPORTED, "batch %d: mixed launches take quasi-cyclic codes", c);
         if (b.rule != CK_LDPC_MIN_SUM) return ck::fail(CK_ERR_UNSUPPORTED, "only the min-sum rule is implemented");
+        CK_TRY(check_min_sum_params(b.scale, b.offset));
         if (b.B < 0 || b.B >= (int64_t(1) << 31)) return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: bad B", c);
         if (b.n_in < 1 || b.n_in > plan->N) return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: bad n_in", c);
         if (b.max_iterations < 0) return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: bad max_iterations", c);

@@ -131,3 +131,23 @@ def test_mixed_launch_rejects_sum_product(torch_dev, ck):
     x = torch.zeros((2, code.n), dtype=torch.float32, device=dev)
     with pytest.raises(NotImplementedError):
         ck.decode_mixed([(x, code, ck.SumProduct())])
+
+
+@pytest.mark.parametrize("scale,offset", [(0.0, 0.0), (1.5, 0.0), (float("nan"), 0.0), (0.875, -0.1),
+                                          (0.875, float("inf"))])
+def test_min_sum_launcher_rejects_parameters_minsum_refuses(torch_dev, ck, scale, offset):
+    """The C ABI takes the min-sum parameters the reference's MinSum accepts
+    (commkit/coding/ldpc.py:345-347: scale in (0, 1], offset finite and
+    >= 0) and raises ValueError through the launcher for the others, before
+    any launch; ``app`` is left as it was."""
+    torch, dev = torch_dev
+    from commkit_gb300 import _cuda
+
+    code = _qc_code(ck, "A")
+    row_ptr, cols, layer_ptr = (torch.from_numpy(a.copy()).to(dev) for a in code._schedule)
+    launch = _cuda.get_kernel("ldpc_layered")
+    llrs = np.ones((2, code.num_variables), dtype=np.float32)
+    app = torch.from_numpy(llrs).to(dev)
+    with pytest.raises(ValueError, match="scale|offset"):
+        launch(app, row_ptr, cols, layer_ptr, scale=scale, offset=offset, max_iterations=5, early_stop=True)
+    np.testing.assert_array_equal(app.cpu().numpy(), llrs)
