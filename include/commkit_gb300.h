@@ -369,8 +369,10 @@ int ck_ldpc_workspace_size(const ck_ldpc_plan* plan, int64_t B, int32_t rule, si
  *           variables, punctured, start at LLR 0)
  *   llr_out (B, n_in) float32 a-posteriori LLRs; may equal llr_in (in place,
  *           the reference's `app` with n_in = N)
- *   rule    CK_LDPC_MIN_SUM (`scale`, `offset` as MinSum) or
- *           CK_LDPC_SUM_PRODUCT (`scale`, `offset` ignored)
+ *   rule    CK_LDPC_MIN_SUM (`scale`, `offset` as MinSum; scale in (0, 1]
+ *           and offset finite and >= 0, as MinSum checks them at
+ *           commkit/coding/ldpc.py:345-347, else CK_ERR_INVALID_ARGUMENT)
+ *           or CK_LDPC_SUM_PRODUCT (`scale`, `offset` ignored)
  *   iters   (B,) int32 iterations run (-1 if a device wait gave up)
  *   valid   (B,) uint8 1 when every check is satisfied
  *   bits    (B, k_bits) int8 hard decisions of the first k_bits variables,
