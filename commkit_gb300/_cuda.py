@@ -166,31 +166,42 @@ def _llr_separable_factory() -> Callable:
 
 
 class _PlanCache:
-    """Plans keyed by the identity of the schedule's device arrays.
+    """Plans keyed by the schedule's device arrays.
 
     The reference caches those arrays per code and device
     (``commkit/backend.py:265-287``), so the same objects come back on
     every call; the first call copies them to the host once to build the
-    plan.  Entries die with the arrays.
+    plan.  The key holds each array's identity, device pointer, size and
+    device, and entries die with the arrays; arrays that cannot be weakly
+    referenced (so an entry could outlive them and a new array reuse their
+    identity) get a plan per call, uncached.
     """
 
     def __init__(self) -> None:
-        self._plans: dict[tuple[int, int, int], Any] = {}
+        self._plans: dict[tuple, Any] = {}
+
+    @staticmethod
+    def _key_of(a: Any) -> tuple:
+        d = _device.wrap(a)
+        return (id(a), d.ptr, d.size, d.device)
 
     def get(self, row_ptr: Any, cols: Any, layer_ptr: Any, n_var: int) -> Any:
         from .coding import _Plan
 
-        key = (id(row_ptr), id(cols), id(layer_ptr), n_var)
+        arrays = (row_ptr, cols, layer_ptr)
+        key = (*(self._key_of(a) for a in arrays), n_var)
         plan = self._plans.get(key)
         if plan is None:
-            host = [_to_host(a) for a in (row_ptr, cols, layer_ptr)]
+            host = [_to_host(a) for a in arrays]
             plan = _Plan(*host, host[0].size - 1, n_var)
+            try:
+                for a in arrays:
+                    weakref.ref(a)
+            except TypeError:
+                return plan
             self._plans[key] = plan
-            for a in (row_ptr, cols, layer_ptr):
-                try:
-                    weakref.finalize(a, self._plans.pop, key, None)
-                except TypeError:
-                    pass
+            for a in arrays:
+                weakref.finalize(a, self._plans.pop, key, None)
         return plan
 
 

@@ -18,6 +18,20 @@ typedef unsigned long long uint64_t;
 
 namespace ck {
 
+namespace ldpc {
+// Largest row degree of the decoder's packed min-sum record (27 sign bits
+// and a 5-bit argmin in one word).  Codes with longer rows run the
+// any-degree kernels (row-degree bound 0): a generic row loop and, for
+// min-sum, the wide message state.
+constexpr int kPackedDegree = 27;
+
+// The row-degree bound of the decoder kernels for a code whose longest row
+// has max_deg edges: 8 (CSR codes only), 16, 27, or 0 for any degree.
+__host__ __device__ constexpr int kernel_dmax(bool qc, int max_deg) {
+    return max_deg > kPackedDegree ? 0 : (max_deg > 16 ? 27 : ((!qc && max_deg <= 8) ? 8 : 16));
+}
+}  // namespace ldpc
+
 // q = n / d for 0 <= n < 2^31 and a run-time divisor 1 <= d < 2^31, by a
 // multiply-high and a shift (the round-up method of Granlund and
 // Montgomery, "Division by invariant integers using multiplication", 1994).

@@ -61,24 +61,39 @@ static_assert(kMaxMixed == CK_LDPC_MAX_MIXED, "mixed-launch code count");
 namespace ck {
 namespace ldpc {
 
-struct MinSumPick {
-    template <bool QC, int DMAX, bool ONE_ROW>
+// The packed state for row-degree bounds up to 27, the wide one for any
+// degree (DMAX = 0).
+template <int DMAX, template <bool> class State>
+struct MinSumPickOf {
+    template <bool QC, bool ONE_ROW>
     static KernelFn get(bool app_smem, bool r_smem) {
-        if (app_smem && r_smem) return decode_kernel<MinSumState, QC, DMAX, true, true, ONE_ROW>;
-        if (app_smem) return decode_kernel<MinSumState, QC, DMAX, true, false, ONE_ROW>;
-        if constexpr (!QC) return decode_kernel<MinSumState, QC, DMAX, false, false, false>;
+        if (app_smem && r_smem) return decode_kernel<State, QC, DMAX, true, true, ONE_ROW>;
+        if (app_smem) return decode_kernel<State, QC, DMAX, true, false, ONE_ROW>;
+        if constexpr (!QC) return decode_kernel<State, QC, DMAX, false, false, false>;
         return nullptr;
     }
 };
+struct MinSumPick {
+    template <bool QC, int DMAX, bool ONE_ROW>
+    static KernelFn get(bool app_smem, bool r_smem) {
+        if constexpr (DMAX == 0)
+            return MinSumPickOf<0, WideMinSumState>::template get<QC, ONE_ROW>(app_smem, r_smem);
+        else
+            return MinSumPickOf<DMAX, MinSumState>::template get<QC, ONE_ROW>(app_smem, r_smem);
+    }
+};
 
-KernelFn min_sum_kernel(bool qc, int dmax, bool app_smem, bool r_smem, bool one_row) {
-    return pick_shape<MinSumPick>(qc, dmax, app_smem, r_smem, one_row);
+KernelFn min_sum_kernel(bool qc, int max_deg, bool app_smem, bool r_smem, bool one_row) {
+    return pick_shape<MinSumPick>(qc, max_deg, app_smem, r_smem, one_row);
 }
 
-KernelFn min_sum_cluster_kernel(int dmax) {
-    if (dmax <= 8) return decode_cluster_kernel<MinSumState, 8>;
-    if (dmax <= 16) return decode_cluster_kernel<MinSumState, 16>;
-    return decode_cluster_kernel<MinSumState, 27>;
+KernelFn min_sum_cluster_kernel(int max_deg) {
+    switch (kernel_dmax(false, max_deg)) {
+        case 8: return decode_cluster_kernel<MinSumState, 8>;
+        case 16: return decode_cluster_kernel<MinSumState, 16>;
+        case 27: return decode_cluster_kernel<MinSumState, 27>;
+        default: return decode_cluster_kernel<WideMinSumState, 0>;
+    }
 }
 
 }  // namespace ldpc
@@ -104,6 +119,7 @@ struct Resolved {
     int cluster_per_sm;
     int cluster;
     int plain_grid;  // the plain kernel's grid for the same frames
+    int32_t sign_words;  // wide min-sum state: sign words per row (0: packed or sum-product)
 };
 
 constexpr int kMaxCluster = 8;  // the portable cluster size
@@ -119,10 +135,12 @@ int device_limits(int dev, int* sms, int* smem_optin) {
 
 // Launch shape, shared-memory layout, grid and workspace of a decode of B
 // frames by `rule`; a pure function of the plan, its launch setting, the
-// rule and B.
-int resolve_shape(const ck_ldpc_plan* plan, int32_t rule, Resolved* r, int* per_sm_out, int* sms_out);
+// rule and B.  may_compile false: a code-specialised kernel only if one is
+// compiled already (no NVRTC, no module load), and nothing cached.
+int resolve_shape(const ck_ldpc_plan* plan, int32_t rule, Resolved* r, int* per_sm_out, int* sms_out,
+                  bool may_compile);
 
-int resolve(const ck_ldpc_plan* plan, int32_t rule, int64_t B, Resolved* r) {
+int resolve(const ck_ldpc_plan* plan, int32_t rule, int64_t B, Resolved* r, bool may_compile = true) {
     if (rule != CK_LDPC_MIN_SUM && rule != CK_LDPC_SUM_PRODUCT)
         return ck::fail(CK_ERR_INVALID_ARGUMENT, "unknown check rule %d", rule);
     static_assert(sizeof(Resolved) <= sizeof(plan->shape_cache[0].resolved), "shape cache too small");
@@ -135,8 +153,10 @@ int resolve(const ck_ldpc_plan* plan, int32_t rule, int64_t B, Resolved* r) {
             memcpy(static_cast<void*>(r), c.resolved, sizeof(Resolved));
             per_sm = c.per_sm;
             sms = c.sms;
+        } else if (!may_compile) {
+            CK_TRY(resolve_shape(plan, rule, r, &per_sm, &sms, false));
         } else {
-            CK_TRY(resolve_shape(plan, rule, r, &per_sm, &sms));
+            CK_TRY(resolve_shape(plan, rule, r, &per_sm, &sms, true));
             memcpy(c.resolved, static_cast<const void*>(r), sizeof(Resolved));
             c.launch = plan->launch;
             c.jit_mode = plan->jit_mode;
@@ -193,7 +213,8 @@ int resolve(const ck_ldpc_plan* plan, int32_t rule, int64_t B, Resolved* r) {
 }
 
 // Everything of a decode's launch that does not depend on the frame count.
-int resolve_shape(const ck_ldpc_plan* plan, int32_t rule, Resolved* r, int* per_sm_out, int* sms_out) {
+int resolve_shape(const ck_ldpc_plan* plan, int32_t rule, Resolved* r, int* per_sm_out, int* sms_out,
+                  bool may_compile) {
     const bool sp = rule == CK_LDPC_SUM_PRODUCT;
     int sms = 0, optin = 0;
     CK_TRY(device_limits(plan->device, &sms, &optin));
@@ -205,11 +226,13 @@ int resolve_shape(const ck_ldpc_plan* plan, int32_t rule, Resolved* r, int* per_
     const uint32_t ctrl = 128;
     const uint32_t app_bytes = align_up(static_cast<uint32_t>(plan->N) * 4, 128);
     // Message state per frame: min-sum keeps a 16-byte record per row in
-    // shared memory (12 bytes in device memory), sum-product one float per
-    // edge in either.
+    // shared memory (12 bytes in device memory), or for rows above 27 edges
+    // the wide state's 3 + sign_words words per row in either; sum-product
+    // one float per edge in either.
+    const int32_t sign_words = (!sp && plan->max_deg > kPackedDegree) ? (plan->max_deg + 31) / 32 : 0;
     const uint32_t r_stride = align_up(static_cast<uint32_t>(sp ? plan->E : plan->m), 32);
-    const uint32_t r_bytes = r_stride * (sp ? 4 : 16);      // in shared memory
-    const uint32_t r_bytes_dev = r_stride * (sp ? 4 : 12);  // in device memory
+    const uint32_t r_bytes = r_stride * (sp ? 4 : (sign_words ? 4 * (3 + sign_words) : 16));  // in shared memory
+    const uint32_t r_bytes_dev = r_stride * (sp ? 4 : (sign_words ? 4 * (3 + sign_words) : 12));  // in device memory
     // Per group: its copy of the circulant table with shared addresses.
     const uint32_t gblk_bytes = plan->qc ? align_up(static_cast<uint32_t>(plan->nnzb) * 8, 128) : 0;
     const uint32_t budget = static_cast<uint32_t>(optin) > tables ? optin - tables : 0;
@@ -254,7 +277,7 @@ int resolve_shape(const ck_ldpc_plan* plan, int32_t rule, Resolved* r, int* per_
                         "threads_per_frame %d must divide or be a multiple of %d (the lifting %d "
                         "rounded up to whole warps)",
                         T, Zp, plan->Z);
-    const int32_t max_threads = max_block_threads(plan->qc, plan->max_deg <= 16 ? 16 : 27);
+    const int32_t max_threads = max_block_threads(plan->qc, kernel_dmax(plan->qc, plan->max_deg));
     if (T > max_threads)
         return ck::fail(CK_ERR_INVALID_ARGUMENT,
                         "threads_per_frame %d above %d for row degree %d", T, max_threads,
@@ -272,10 +295,14 @@ int resolve_shape(const ck_ldpc_plan* plan, int32_t rule, Resolved* r, int* per_
                               : min_sum_kernel(plan->qc, plan->max_deg, app_smem, r_smem, one_row);
     if (!table) return ck::fail(CK_ERR_UNSUPPORTED, "no decoder kernel for this code shape");
     const void* kernel = reinterpret_cast<const void*>(table);
-    if (!sp && plan->qc && T == Zp && app_smem) {
-        // The code-specialised kernel, where the plan has one.
+    if (!sp && plan->qc && T == Zp && app_smem && plan->max_deg <= kPackedDegree) {
+        // The code-specialised kernel, where the plan has one (codes with
+        // rows above 27 edges have none: they run the any-degree kernels).
         const void* special = nullptr;
-        CK_TRY(specialised_kernel(plan, plan->max_deg <= 16 ? 16 : 27, r_smem, &special));
+        if (may_compile)
+            CK_TRY(specialised_kernel(plan, kernel_dmax(true, plan->max_deg), r_smem, &special));
+        else
+            CK_TRY(specialised_kernel_ready(plan, r_smem, &special));
         if (special) kernel = special;
     }
     CK_TRY(ck::allow_max_smem(kernel, plan->device, optin));
@@ -312,6 +339,7 @@ int resolve_shape(const ck_ldpc_plan* plan, int32_t rule, Resolved* r, int* per_
     r->r_stride = r_stride;
     r->smem = tables + static_cast<uint32_t>(G) * group;
     r->app_stride = static_cast<int32_t>(app_bytes / 4);
+    r->sign_words = sign_words;
 
     int per_sm = 0;
     CK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, r->kernel, T * G, r->smem));
@@ -461,6 +489,7 @@ Params make_params(const ck_ldpc_plan* plan, const Resolved& r, const float* llr
     p.g_r = reinterpret_cast<uint32_t*>(wsb + r.r_ws_off);
     p.g_app = reinterpret_cast<float*>(wsb + r.app_ws_off);
     p.app_stride = r.app_stride;
+    p.sign_words = r.sign_words;
     return p;
 }
 
@@ -529,11 +558,13 @@ extern "C" int ck_ldpc_workspace_status(const void* workspace, void* stream) {
 }
 
 // Decode into caller-provided scratch of a fixed capacity (the allocation-free
-// entry point of ck_ldpc_static.cu): the same kernel and launch shape as
+// entry point of ck_ldpc_static.cu): the same kernels and launch shape as
 // ck_ldpc_decode, with the persistent grid cut down to the frame slots whose
 // device-memory state fits in `scratch_bytes`.  Frames beyond the slots wait
 // in the device queue, so any B fits; a code whose one slot does not fit is
-// rejected.
+// rejected.  It never compiles a code-specialised kernel (that loads a module,
+// which allocates): it uses one only when an earlier ck_ldpc_decode of the
+// plan compiled it, else the table-driven kernel, with the same results.
 int ck::ldpc_decode_in_scratch(const ck_ldpc_plan* plan, const float* llr_in, float* llr_out,
                                int64_t B, int32_t n_in, int32_t rule, float scale, float offset,
                                int32_t max_iterations, int32_t early_stop, int32_t* iters,
@@ -546,7 +577,7 @@ int ck::ldpc_decode_in_scratch(const ck_ldpc_plan* plan, const float* llr_in, fl
         return ck::fail(CK_ERR_INVALID_ARGUMENT, "scratch must be 256-byte aligned");
     CK_TRY(check_device(plan));
     Resolved r;
-    CK_TRY(resolve(plan, rule, B, &r));
+    CK_TRY(resolve(plan, rule, B, &r, false));
     // The static scratch serves the plain kernel's frame slots.
     r.cluster = 1;
     r.grid = r.plain_grid;
@@ -594,6 +625,7 @@ struct MixedResolved {
     size_t ws_bytes;
     uint32_t block_words;  // device-memory message state per block, shared by the codes
     bool wide;  // some code has rows above degree 16
+    bool any_degree;  // some code has rows above degree 27: the any-degree kernel, wide state for all
 };
 
 // Occupancy per (kernel, device, block shape), remembered: the request
@@ -627,6 +659,9 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
     R->block_threads = 32;
     R->smem = 0;
     R->wide = false;
+    R->any_degree = false;
+    for (int c = 0; c < n; ++c)
+        if (batches[c].plan && batches[c].plan->max_deg > kPackedDegree) R->any_degree = true;
     for (int c = 0; c < n; ++c) {
         const ck_ldpc_batch& b = batches[c];
         const ck_ldpc_plan* plan = b.plan;
@@ -685,7 +720,11 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
         const uint32_t gblk = align_up(static_cast<uint32_t>(plan->nnzb) * 8, 128);
         const uint32_t app = align_up(static_cast<uint32_t>(plan->N) * 4, 128);
         const uint32_t r_stride = align_up(static_cast<uint32_t>(plan->m), 32);
-        const uint32_t rsm = r_stride * 16;
+        // Message state words per row: the packed record (16 bytes in shared
+        // memory, 3 words in device memory), or in an any-degree launch every
+        // code's wide state, 3 + sign_words words in either.
+        const int32_t sign_words = R->any_degree ? std::max(1, (plan->max_deg + 31) / 32) : 0;
+        const uint32_t rsm = r_stride * (sign_words ? 4u * static_cast<uint32_t>(3 + sign_words) : 16u);
         // 1 KB stays free for the kernel's static shared variable.
         const uint32_t budget = static_cast<uint32_t>(optin) > tables + 1024 ? optin - tables - 1024 : 0;
         const int32_t max_threads = R->wide ? 512 : kMixedThreads;
@@ -737,6 +776,7 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
         K.r_off = ctrl + gblk + app;
         K.r_stride = r_stride;
         K.weight = static_cast<float>(plan->E);
+        K.sign_words = sign_words;
         K.ka = ka;
         K.axes_off = axes_off;
         if (ka) {
@@ -757,8 +797,9 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
     if (R->wide && R->block_threads > 512)
         return ck::fail(CK_ERR_UNSUPPORTED, "mixed launch of %d threads with rows above degree 16",
                         R->block_threads);
-    const void* kernel = reinterpret_cast<const void*>(R->wide ? ldpc_mixed_kernel<27> : ldpc_mixed_kernel<16>);
-    {
+    const void* kernel = reinterpret_cast<const void*>(
+        R->any_degree ? ldpc_mixed_kernel<0> : (R->wide ? ldpc_mixed_kernel<27> : ldpc_mixed_kernel<16>));
+    if (!R->any_degree) {
         // The code-specialised mixed kernel, where the plans have one.
         const ck_ldpc_plan* plans[kMaxMixed];
         int32_t threads[kMaxMixed];
@@ -801,7 +842,8 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
     uint32_t block_words = 0;
     for (int c = 0; c < n; ++c)
         if (!R->p.code[c].r_smem && R->p.code[c].B > 0)  // a code without frames never runs
-            block_words = std::max<uint32_t>(block_words, static_cast<uint32_t>(R->p.code[c].G) * 3u *
+            block_words = std::max<uint32_t>(block_words, static_cast<uint32_t>(R->p.code[c].G) *
+                                                              static_cast<uint32_t>(3 + R->p.code[c].sign_words) *
                                                               R->p.code[c].r_stride);
     R->block_words = (block_words + 63u) / 64u * 64u;
     for (int c = 0; c < n; ++c) R->p.code[c].block_words = R->block_words;

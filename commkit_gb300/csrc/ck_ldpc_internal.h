@@ -11,9 +11,6 @@
 
 namespace ck {
 
-// Largest check-row degree: the compressed check-to-variable state of a row
-// keeps its sign bits and the argmin in one 32-bit word (27 + 5 bits).
-constexpr int32_t kMaxRowDegree = 27;
 // Circulant tables held in shared memory.
 constexpr int32_t kMaxBaseRows = 1024;
 constexpr int32_t kMaxBlocks = 2048;
@@ -96,6 +93,11 @@ namespace ldpc {
 // the plan has none (specialisation off, NVRTC missing or the compilation
 // failed); an error only when the plan requires specialisation.
 int specialised_kernel(const ck_ldpc_plan* plan, int dmax, bool r_smem, const void** out);
+// The same kernel only if an earlier call already compiled it (nullptr in
+// *out otherwise): never compiles or loads code, for the allocation-free
+// entry point.  An error only when the plan requires specialisation and has
+// no compiled kernel.
+int specialised_kernel_ready(const ck_ldpc_plan* plan, bool r_smem, const void** out);
 // The NVRTC source of a circulant plan's specialised kernels.
 std::string specialised_source(const ck_ldpc_plan& plan, int dmax);
 // The NVRTC source of the specialised mixed kernel of n plans, batch c with

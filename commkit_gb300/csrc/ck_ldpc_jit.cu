@@ -466,6 +466,25 @@ int specialised_kernel(const ck_ldpc_plan* plan, int dmax, bool r_smem, const vo
     return CK_OK;
 }
 
+int specialised_kernel_ready(const ck_ldpc_plan* plan, bool r_smem, const void** out) {
+    *out = nullptr;
+    const int mode = effective_mode(plan->jit_mode);
+    if (mode == CK_LDPC_SPECIALISE_OFF) return CK_OK;
+    std::lock_guard<std::mutex> lock(plan->jit_mu);
+    const ck_ldpc_plan::Jit& j = plan->jit;
+    if (j.tried && j.lib) {
+        *out = j.kernel[r_smem ? 1 : 0];
+        return CK_OK;
+    }
+    if (mode == CK_LDPC_SPECIALISE_ON)
+        return ck::fail(CK_ERR_UNSUPPORTED,
+                        j.tried ? "code-specialised decoder unavailable: %s"
+                                : "the code-specialised decoder is not compiled yet%s: decode once through "
+                                  "ck_ldpc_decode first",
+                        j.why.c_str());
+    return CK_OK;
+}
+
 int mixed_specialised_kernel(const ck_ldpc_plan* const* plans, const int32_t* T, int n, int dmax,
                              const void** out) {
     *out = nullptr;

@@ -64,6 +64,9 @@ struct Params {
     uint32_t* g_r;  // check-message state slots in device memory (rule's layout)
     float* g_app;  // posterior slots in device memory (N per slot)
     int32_t app_stride;
+    // Min-sum codes with rows above kPackedDegree edges: sign words per row
+    // of the wide message state (0 otherwise).
+    int32_t sign_words;
 };
 
 __device__ __forceinline__ float flip_sign(float v, uint32_t bit) {
@@ -180,10 +183,35 @@ __device__ __forceinline__ bool syndrome_ok(const Params& p, const float* a, con
     return true;
 }
 
-// Threads per block the kernels are built for (registers scale inversely).
+// Threads per block the kernels are built for (registers scale inversely;
+// the any-degree kernels keep no per-edge registers).
 __host__ __device__ constexpr int max_block_threads(bool qc, int dmax) {
     return dmax > 16 ? 512 : (qc ? 768 : 1024);
 }
+
+// Posterior access of the any-degree row loops: col(e) gives edge e's
+// handle, ld/st read and write the posterior there.  Circulant rows address
+// the group's shared-memory posterior through its shared-address table
+// (gblk, r4 = 4 r, Z4 = 4 Z, as qc_row_fixed); CSR rows index `a`.
+struct QcSmemPost {
+    const int2* gblk;
+    uint32_t r4, Z4;
+    __device__ __forceinline__ uint32_t col(uint32_t e) const {
+        const int2 b = gblk[e];
+        const uint32_t c = r4 + static_cast<uint32_t>(b.x);
+        return c >= static_cast<uint32_t>(b.y) ? c - Z4 : c;
+    }
+    __device__ __forceinline__ float ld(uint32_t c) const { return ld_shared_f32(c); }
+    __device__ __forceinline__ void st(uint32_t c, float v) const { st_shared_f32(c, v); }
+};
+template <class ColOf>
+struct CsrPost {
+    float* a;
+    const ColOf& col_of;
+    __device__ __forceinline__ uint32_t col(uint32_t e) const { return static_cast<uint32_t>(col_of(static_cast<int>(e))); }
+    __device__ __forceinline__ float ld(uint32_t c) const { return a[c]; }
+    __device__ __forceinline__ void st(uint32_t c, float v) const { a[c] = v; }
+};
 
 // The layer loop of the table-driven kernels.
 struct TableProgram {
@@ -380,29 +408,36 @@ __global__ void __launch_bounds__(max_block_threads(QC, DMAX))
 #ifndef __CUDACC_RTC__
 using KernelFn = void (*)(Params);
 
-// The decoder kernel of a rule for a code shape (quasi-cyclic or CSR, the
-// row-degree bound, where the posterior and the message state live);
-// nullptr when no such kernel exists.
-KernelFn min_sum_kernel(bool qc, int dmax, bool app_smem, bool r_smem, bool one_row);
-KernelFn sum_product_kernel(bool qc, int dmax, bool app_smem, bool r_smem, bool one_row);
+// The decoder kernel of a rule for a code shape (quasi-cyclic or CSR, its
+// longest row, where the posterior and the message state live); nullptr
+// when no such kernel exists.
+KernelFn min_sum_kernel(bool qc, int max_deg, bool app_smem, bool r_smem, bool one_row);
+KernelFn sum_product_kernel(bool qc, int max_deg, bool app_smem, bool r_smem, bool one_row);
 // The cluster kernel of a rule for CSR codes (posterior and messages in
-// device memory).
-KernelFn min_sum_cluster_kernel(int dmax);
-KernelFn sum_product_cluster_kernel(int dmax);
+// device memory) whose longest row has max_deg edges.
+KernelFn min_sum_cluster_kernel(int max_deg);
+KernelFn sum_product_cluster_kernel(int max_deg);
 
-// Kernels are built for these row-degree bounds (CSR codes also for 8).
+// Kernels are built for these row-degree bounds: 16, 27 and any (0), CSR
+// codes also 8 (kernel_dmax).
 template <class Pick>
-KernelFn pick_shape(bool qc, int dmax, bool app_smem, bool r_smem, bool one_row) {
+KernelFn pick_shape(bool qc, int max_deg, bool app_smem, bool r_smem, bool one_row) {
     if (!app_smem && (qc || r_smem)) return nullptr;  // circulant rows address shared memory
-    if (!qc && dmax <= 8) return Pick::template get<false, 8, false>(app_smem, r_smem);
-    if (!qc)
-        return dmax <= 16 ? Pick::template get<false, 16, false>(app_smem, r_smem)
-                          : Pick::template get<false, 27, false>(app_smem, r_smem);
-    if (one_row)
-        return dmax <= 16 ? Pick::template get<true, 16, true>(app_smem, r_smem)
-                          : Pick::template get<true, 27, true>(app_smem, r_smem);
-    return dmax <= 16 ? Pick::template get<true, 16, false>(app_smem, r_smem)
-                      : Pick::template get<true, 27, false>(app_smem, r_smem);
+    const int d = kernel_dmax(qc, max_deg);
+    if (!qc) {
+        if (d == 8) return Pick::template get<false, 8, false>(app_smem, r_smem);
+        if (d == 16) return Pick::template get<false, 16, false>(app_smem, r_smem);
+        if (d == 27) return Pick::template get<false, 27, false>(app_smem, r_smem);
+        return Pick::template get<false, 0, false>(app_smem, r_smem);
+    }
+    if (one_row) {
+        if (d == 16) return Pick::template get<true, 16, true>(app_smem, r_smem);
+        if (d == 27) return Pick::template get<true, 27, true>(app_smem, r_smem);
+        return Pick::template get<true, 0, true>(app_smem, r_smem);
+    }
+    if (d == 16) return Pick::template get<true, 16, false>(app_smem, r_smem);
+    if (d == 27) return Pick::template get<true, 27, false>(app_smem, r_smem);
+    return Pick::template get<true, 0, false>(app_smem, r_smem);
 }
 
 #endif  // __CUDACC_RTC__

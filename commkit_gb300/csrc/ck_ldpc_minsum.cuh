@@ -222,6 +222,10 @@ struct MinSumState {
         : rs(rs_),
           g12(reinterpret_cast<uint2*>(g_r + static_cast<size_t>(slot) * 3 * r_stride)),
           g3(g_r + static_cast<size_t>(slot) * 3 * r_stride + 2 * r_stride) {}
+    // The mixed kernel's form (the same state; sign_words is unused).
+    __device__ __forceinline__ MinSumState(unsigned char* rsm, uint32_t* g_r, uint32_t slot, uint32_t r_stride,
+                                           int32_t)
+        : MinSumState(reinterpret_cast<uint4*>(rsm), g_r, slot, r_stride) {}
 
     __device__ __forceinline__ void zero(const Params& p, int first, int stride) const {
         zero_rows(p.m, first, stride);
@@ -252,10 +256,15 @@ struct MinSumState {
     template <int DMAX>
     __device__ __forceinline__ void qc_row(const Params& p, const int2* gblk, int deg, uint32_t row,
                                            int32_t, int32_t, uint32_t r4, uint32_t Z4) const {
+        qc_row_k<DMAX>(gblk, deg, row, r4, Z4, p.scale, p.offset);
+    }
+    template <int DMAX>
+    __device__ __forceinline__ void qc_row_k(const int2* gblk, int deg, uint32_t row, uint32_t r4, uint32_t Z4,
+                                             float scale, float offset) const {
         const uint4 s = load(row);
         float m1 = __uint_as_float(s.x), m2 = __uint_as_float(s.y);
         uint32_t w = s.z;
-        ck::ldpc::qc_row<DMAX>(gblk, deg, r4, Z4, m1, m2, w, p.scale, p.offset);
+        ck::ldpc::qc_row<DMAX>(gblk, deg, r4, Z4, m1, m2, w, scale, offset);
         store(row, m1, m2, w);
     }
     // Load-ahead for the code-specialised programs: pre(row) starts loading
@@ -287,6 +296,144 @@ struct MinSumState {
         min_sum_row<DMAX>(a, deg, col_of, m1, m2, w, p.scale, p.offset);
         store(row, m1, m2, w);
     }
+};
+
+
+
+// Min-sum check-message state of codes with rows above kPackedDegree edges
+// (the any-degree kernels, row-degree bound 0).  Per row: (min1', min2') as
+// a pair, the argmin as a whole word, and the row's sign bits in
+// sign_words words (bit j of word w is edge 32 w + j).  Each of these is an
+// array of r_stride entries, so rows on consecutive lanes touch consecutive
+// words: (3 + sign_words) r_stride words per frame slot, in the group's
+// shared memory or in the slot's device memory.  Still lossless: the
+// message of row i edge e is sign_e * (e == argmin ? min2' : min1').
+template <bool R_SMEM>
+struct WideMinSumState {
+    uint32_t* w;  // the slot's words
+    uint32_t r_stride;
+    int32_t nw;
+
+    __device__ __forceinline__ WideMinSumState(const Params& p, unsigned char* gbase, uint32_t slot)
+        : WideMinSumState(gbase + p.r_off, p.g_r, slot, p.r_stride, p.sign_words) {}
+    __device__ __forceinline__ WideMinSumState(unsigned char* rsm, uint32_t* g_r, uint32_t slot,
+                                               uint32_t r_stride_, int32_t sign_words)
+        : w(R_SMEM ? reinterpret_cast<uint32_t*>(rsm)
+                   : g_r + static_cast<size_t>(slot) * static_cast<uint32_t>(3 + sign_words) * r_stride_),
+          r_stride(r_stride_),
+          nw(sign_words) {}
+
+    __device__ __forceinline__ uint32_t ld(uint32_t i) const { return R_SMEM ? w[i] : __ldcg(w + i); }
+    __device__ __forceinline__ void st(uint32_t i, uint32_t v) const {
+        if (R_SMEM)
+            w[i] = v;
+        else
+            __stcg(w + i, v);
+    }
+    __device__ __forceinline__ uint2 ld2(uint32_t row) const {
+        const uint2* m = reinterpret_cast<const uint2*>(w);
+        return R_SMEM ? m[row] : __ldcg(m + row);
+    }
+    __device__ __forceinline__ void st2(uint32_t row, float m1, float m2) const {
+        uint2* m = reinterpret_cast<uint2*>(w);
+        const uint2 v = make_uint2(__float_as_uint(m1), __float_as_uint(m2));
+        if (R_SMEM)
+            m[row] = v;
+        else
+            __stcg(m + row, v);
+    }
+
+    __device__ __forceinline__ void zero(const Params& p, int first, int stride) const {
+        zero_rows(p.m, first, stride);
+    }
+    __device__ __forceinline__ void zero_rows(int32_t m, int first, int stride) const {
+        for (int i = first; i < m; i += stride) {
+            st2(static_cast<uint32_t>(i), 0.0f, 0.0f);
+            for (int32_t k = 0; k <= nw; ++k) st((2u + static_cast<uint32_t>(k)) * r_stride + i, 0u);
+        }
+    }
+
+    // One row of any degree: the reference's two passes
+    // (commkit/_cuda/src/ldpc.cu:45-72) edge by edge, with Q recomputed in
+    // the second pass from the unchanged posterior and the old state (the
+    // same float operations, so the same Q), and the new sign bits written
+    // a word at a time after that word's old bits have been read.
+    template <class Post>
+    __device__ __forceinline__ void any_row(const Post& post, const int deg, const uint32_t row, const float scale,
+                                            const float offset) const {
+        const uint2 om = ld2(row);
+        const float om1 = __uint_as_float(om.x), om2 = __uint_as_float(om.y);
+        const uint32_t oidx = ld(2u * r_stride + row);
+        float min1 = ck::inf_f(), min2 = ck::inf_f();
+        uint32_t idx = 0xffffffffu;  // no edge, the reference's -1
+        uint32_t par = 0u;
+        for (int w0 = 0; w0 < deg; w0 += 32) {
+            const uint32_t os = ld((3u + static_cast<uint32_t>(w0 >> 5)) * r_stride + row);
+            const int n = min(32, deg - w0);
+            for (int j = 0; j < n; ++j) {
+                const uint32_t e = static_cast<uint32_t>(w0 + j);
+                const float r_old = flip_sign(e == oidx ? om2 : om1, (os >> j) & 1u);
+                const float q = __fsub_rn(post.ld(post.col(e)), r_old);
+                par ^= q < 0.0f ? 1u : 0u;
+                const float mag = fabsf(q);
+                if (mag < min1) {
+                    min2 = min1;
+                    min1 = mag;
+                    idx = e;
+                } else if (mag < min2) {
+                    min2 = mag;
+                }
+            }
+        }
+        const float n1 = fmaxf(__fsub_rn(__fmul_rn(scale, min1), offset), 0.0f);
+        const float n2 = fmaxf(__fsub_rn(__fmul_rn(scale, min2), offset), 0.0f);
+        for (int w0 = 0; w0 < deg; w0 += 32) {
+            const uint32_t wi = (3u + static_cast<uint32_t>(w0 >> 5)) * r_stride + row;
+            const uint32_t os = ld(wi);
+            uint32_t ns = 0u;
+            const int n = min(32, deg - w0);
+            for (int j = 0; j < n; ++j) {
+                const uint32_t e = static_cast<uint32_t>(w0 + j);
+                const uint32_t c = post.col(e);
+                const float r_old = flip_sign(e == oidx ? om2 : om1, (os >> j) & 1u);
+                const float q = __fsub_rn(post.ld(c), r_old);
+                const uint32_t sgn = par ^ (q < 0.0f ? 1u : 0u);
+                const float rn = flip_sign(e == idx ? n2 : n1, sgn);
+                post.st(c, __fadd_rn(q, rn));
+                ns |= sgn << j;
+            }
+            st(wi, ns);
+        }
+        st2(row, n1, n2);
+        st(2u * r_stride + row, idx);
+    }
+
+    template <int DMAX>
+    __device__ __forceinline__ void qc_row(const Params& p, const int2* gblk, int deg, uint32_t row,
+                                           int32_t, int32_t, uint32_t r4, uint32_t Z4) const {
+        any_row(QcSmemPost{gblk, r4, Z4}, deg, row, p.scale, p.offset);
+    }
+    template <int DMAX>
+    __device__ __forceinline__ void qc_row_k(const int2* gblk, int deg, uint32_t row, uint32_t r4, uint32_t Z4,
+                                             float scale, float offset) const {
+        any_row(QcSmemPost{gblk, r4, Z4}, deg, row, scale, offset);
+    }
+    template <int DMAX, class ColOf>
+    __device__ __forceinline__ void csr_row(const Params& p, float* a, uint32_t row, int deg, int32_t,
+                                            const ColOf& col_of) const {
+        any_row(CsrPost<ColOf>{a, col_of}, deg, row, p.scale, p.offset);
+    }
+};
+
+// The min-sum state of the kernels with row-degree bound DMAX: the packed
+// record, or the wide one for any degree (DMAX = 0).
+template <int DMAX, bool R_SMEM>
+struct MinSumFor {
+    using type = MinSumState<R_SMEM>;
+};
+template <bool R_SMEM>
+struct MinSumFor<0, R_SMEM> {
+    using type = WideMinSumState<R_SMEM>;
 };
 
 

@@ -47,6 +47,10 @@ struct MixedCode {
     uint32_t block_words;
     uint32_t* counter;
     float weight;  // edges per frame
+    // Any-degree launches (row-degree bound 0): sign words per row of the
+    // code's wide message state, 3 + sign_words words per row; 0 otherwise
+    // (the packed record, 3 words per row in device memory).
+    int32_t sign_words;
     // Fused demapping (sym != null): frame f's channel LLRs are the
     // closed-form max-log LLRs of its n_in / (2 ka) symbols at
     // sym + f * n_in / (2 ka), with 1/sigma^2 = inv_s2[f]; llr_in is unused.
@@ -160,9 +164,9 @@ __device__ __forceinline__ void mixed_frames(const MixedCode& K, unsigned char* 
     unsigned char* gbase = smem + K.tables_bytes + static_cast<uint32_t>(g) * K.group_bytes;
     volatile uint32_t* s_frame = reinterpret_cast<volatile uint32_t*>(gbase + 8);
     float* a = reinterpret_cast<float*>(gbase + K.app_off);
-    const MinSumState<R_SMEM> st(reinterpret_cast<uint4*>(gbase + K.r_off),
-                                 K.g_r + static_cast<size_t>(blockIdx.x) * K.block_words, static_cast<uint32_t>(g),
-                                 K.r_stride);
+    using State = typename MinSumFor<DMAX, R_SMEM>::type;
+    const State st(gbase + K.r_off, K.g_r + static_cast<size_t>(blockIdx.x) * K.block_words,
+                   static_cast<uint32_t>(g), K.r_stride, K.sign_words);
     int2* gblk = reinterpret_cast<int2*>(gbase + K.gblk_off);
     const uint32_t a_addr = ck::smem_addr(a);
     for (int i = tid; i < K.nnzb; i += K.T)
@@ -226,12 +230,8 @@ __device__ __forceinline__ void mixed_frames(const MixedCode& K, unsigned char* 
             auto do_row = [&](int32_t b, int32_t e0, int deg, int32_t r) {
                 const uint32_t row = static_cast<uint32_t>(b) * static_cast<uint32_t>(K.Z) +
                                      static_cast<uint32_t>(r);
-                const uint4 s = st.load(row);
-                float m1 = __uint_as_float(s.x), m2 = __uint_as_float(s.y);
-                uint32_t w = s.z;
-                qc_row<DMAX>(gblk + e0, deg, r4 + 4u * static_cast<uint32_t>(r - qr0), Z4, m1, m2, w,
-                             K.scale, K.offset);
-                st.store(row, m1, m2, w);
+                st.template qc_row_k<DMAX>(gblk + e0, deg, row, r4 + 4u * static_cast<uint32_t>(r - qr0), Z4,
+                                           K.scale, K.offset);
             };
             if constexpr (Prog::kSpecialised)
                 Prog::iteration(st, a_addr + r4, static_cast<uint32_t>(qr0), K.scale, K.offset, bar, K.T,

@@ -209,10 +209,6 @@ int plan_host(const int32_t* row_ptr, const int32_t* cols, const int32_t* layer_
             if (cols[e] <= cols[e - 1])
                 return ck::fail(CK_ERR_INVALID_ARGUMENT,
                                 "the columns of row %d must be increasing", r);
-    if (max_deg > ck::kMaxRowDegree)
-        return ck::fail(CK_ERR_UNSUPPORTED, "row degree %d above the decoder's limit of %d",
-                        max_deg, ck::kMaxRowDegree);
-
     plan->m = m;
     plan->N = N;
     plan->E = E;
@@ -282,7 +278,11 @@ extern "C" int ck_ldpc_specialised_source(const int32_t* row_ptr, const int32_t*
     ck_ldpc_plan plan;
     CK_TRY(plan_host(row_ptr, cols, layer_ptr, m, N, L, &plan));
     if (!plan.qc) return ck::fail(CK_ERR_UNSUPPORTED, "the schedule has no circulant structure");
-    const int dmax = plan.max_deg <= 16 ? 16 : 27;
+    if (plan.max_deg > ck::ldpc::kPackedDegree)
+        return ck::fail(CK_ERR_UNSUPPORTED,
+                        "rows of %d edges: codes with rows above %d edges run the any-degree kernels, "
+                        "which have no code-specialised form", plan.max_deg, ck::ldpc::kPackedDegree);
+    const int dmax = ck::ldpc::kernel_dmax(true, plan.max_deg);
     const ck_ldpc_plan* plans[1] = {&plan};
     const int parts[1] = {form};  // form 1: one thread per row slot, 2: two
     const std::string src =

@@ -51,6 +51,39 @@ struct SumProductState {
             __stcg(r + i, v);
     }
 
+    // One row of any degree (the any-degree kernels, DMAX = 0): the
+    // reference's kernel loop as it stands (commkit/_cuda/src/ldpc.cu:74-91),
+    // Q and phi(|Q|) recomputed in the second pass; edge e's message at
+    // msg(e).
+    template <class Post, class Msg>
+    __device__ __forceinline__ void any_row(const Post& post, const int deg, const Msg& msg) const {
+        float total = 0.0f;
+        bool neg = false;
+        for (int e = 0; e < deg; ++e) {
+            const float qe = __fsub_rn(post.ld(post.col(static_cast<uint32_t>(e))), ld(msg(e)));
+            neg ^= qe < 0.0f;
+            total = __fadd_rn(total, phi(fabsf(qe)));
+        }
+        for (int e = 0; e < deg; ++e) {
+            const uint32_t c = post.col(static_cast<uint32_t>(e));
+            const float qe = __fsub_rn(post.ld(c), ld(msg(e)));
+            const float mag = phi(__fsub_rn(total, phi(fabsf(qe))));
+            const float rn = (neg != (qe < 0.0f)) ? -mag : mag;
+            post.st(c, __fadd_rn(qe, rn));
+            st(msg(e), rn);
+        }
+    }
+    // Message addresses: circulant c of a base row keeps row r's message at
+    // c Z + r; a CSR edge at its index.
+    struct QcMsg {
+        uint32_t base, Z;
+        __device__ __forceinline__ uint32_t operator()(int e) const { return base + static_cast<uint32_t>(e) * Z; }
+    };
+    struct CsrMsg {
+        int32_t e0;
+        __device__ __forceinline__ uint32_t operator()(int e) const { return static_cast<uint32_t>(e0 + e); }
+    };
+
     // Row r of base row b: circulants e0 .. e0 + deg of the table, their
     // columns from the group's shared-address copy `gblk`.
     template <int DMAX>
@@ -60,6 +93,17 @@ struct SumProductState {
                                            const uint32_t Z4) const {
         const uint32_t Z = static_cast<uint32_t>(p.Z);
         const uint32_t base = static_cast<uint32_t>(e0) * Z + static_cast<uint32_t>(rr);
+        if constexpr (DMAX == 0) {
+            any_row(QcSmemPost{gblk, r4, Z4}, deg, QcMsg{base, Z});
+        } else {
+            qc_row_fixed<DMAX>(gblk, deg, base, Z, r4, Z4);
+        }
+    }
+
+    template <int DMAX>
+    __device__ __forceinline__ void qc_row_fixed(const int2* __restrict__ gblk, const int deg,
+                                                 const uint32_t base, const uint32_t Z,
+                                                 const uint32_t r4, const uint32_t Z4) const {
         float q[DMAX], ph[DMAX];
         float total = 0.0f;
         bool neg = false;
@@ -94,6 +138,16 @@ struct SumProductState {
     __device__ __forceinline__ void csr_row(const Params&, float* __restrict__ a, uint32_t,
                                             const int deg, const int32_t e0,
                                             const ColOf& col_of) const {
+        if constexpr (DMAX == 0) {
+            any_row(CsrPost<ColOf>{a, col_of}, deg, CsrMsg{e0});
+        } else {
+            csr_row_fixed<DMAX>(a, deg, e0, col_of);
+        }
+    }
+
+    template <int DMAX, class ColOf>
+    __device__ __forceinline__ void csr_row_fixed(float* __restrict__ a, const int deg, const int32_t e0,
+                                                  const ColOf& col_of) const {
         float q[DMAX], ph[DMAX];
         int col[DMAX];  // loaded once, all before the first posterior load
         float total = 0.0f;
@@ -135,14 +189,17 @@ struct SumProductPick {
 
 }  // namespace sp
 
-KernelFn sum_product_kernel(bool qc, int dmax, bool app_smem, bool r_smem, bool one_row) {
-    return pick_shape<sp::SumProductPick>(qc, dmax, app_smem, r_smem, one_row);
+KernelFn sum_product_kernel(bool qc, int max_deg, bool app_smem, bool r_smem, bool one_row) {
+    return pick_shape<sp::SumProductPick>(qc, max_deg, app_smem, r_smem, one_row);
 }
 
-KernelFn sum_product_cluster_kernel(int dmax) {
-    if (dmax <= 8) return decode_cluster_kernel<sp::SumProductState, 8>;
-    if (dmax <= 16) return decode_cluster_kernel<sp::SumProductState, 16>;
-    return decode_cluster_kernel<sp::SumProductState, 27>;
+KernelFn sum_product_cluster_kernel(int max_deg) {
+    switch (kernel_dmax(false, max_deg)) {
+        case 8: return decode_cluster_kernel<sp::SumProductState, 8>;
+        case 16: return decode_cluster_kernel<sp::SumProductState, 16>;
+        case 27: return decode_cluster_kernel<sp::SumProductState, 27>;
+        default: return decode_cluster_kernel<sp::SumProductState, 0>;
+    }
 }
 
 }  // namespace ldpc

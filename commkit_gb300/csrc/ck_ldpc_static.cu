@@ -29,6 +29,16 @@
 //    shared memory use only the 256-byte header.
 //  * Plans (ck_ldpc_plan_create) allocate their tables when they are
 //    created, so create them before the allocation-free phase.
+//  * It never compiles a code-specialised kernel (NVRTC and the module load
+//    allocate): a plan whose specialised kernel an earlier ck_ldpc_decode
+//    compiled runs it, any other runs the table-driven kernel, with the
+//    same results.
+//  * A frame whose bulk LLR copy timed out comes back with iters = -1 and
+//    valid = 0, the only timeout signal here (the status word sits in the
+//    shared array and the next call clears it).
+//  * The address is cached per device ordinal for the life of the process:
+//    after cudaDeviceReset the module is reloaded elsewhere, so the entry
+//    point must not be used again in that process.
 #include <mutex>
 
 #include "ck_ldpc_internal.h"

@@ -483,7 +483,14 @@ int ck_ldpc_decode_mixed(const ck_ldpc_batch* batches, int32_t num_batches, void
  * serialise them on one stream.  The grid is limited to the frames whose
  * state fits (any B works); a code whose one block of frames needs more
  * scratch than the array holds returns CK_ERR_UNSUPPORTED.  Results are
- * identical to ck_ldpc_decode's.
+ * identical to ck_ldpc_decode's.  The call never compiles a code-specialised
+ * kernel (loading one allocates): it runs one only when an earlier
+ * ck_ldpc_decode of the plan compiled it, else the table-driven kernel, with
+ * the same results (a plan set to CK_LDPC_SPECIALISE_ON without a compiled
+ * kernel is refused).  A frame whose LLR copy timed out reports iters = -1
+ * and valid = 0; that is the only timeout signal on this path.  The cached
+ * address does not survive cudaDeviceReset: do not use the entry point after
+ * resetting the device in the same process.
  */
 int ck_ldpc_decode_static(const ck_ldpc_plan* plan, const float* llr_in, float* llr_out,
                           int64_t B, int32_t n_in, int32_t rule, float scale, float offset,

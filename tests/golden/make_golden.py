@@ -40,6 +40,10 @@ Every output here is the reference's own result on seeded inputs:
   reference's public calls on this path (``--only=api``);
 * ``ldpc_nonfinite.npz``: min-sum on LLRs with infinities and a NaN,
   DVB-S2 short 1/2 and PON (``--only=nonfinite``);
+* ``ldpc_wide.npz``: codes with rows above 27 edges (DVB-S2 normal 9/10,
+  rows of 30; two seeded codes with rows of 64, circulant and not): the
+  reference's schedules and its min-sum and sum-product decodes
+  (``--only=wide``);
 * ``ldpc_generator.npz``: three codes whose parity part is not invertible
   (a cycle-free code, a random code with a redundant check, a circulant
   code whose block columns have weight two), with the reference's ``k``,
@@ -585,8 +589,108 @@ def generator_case(ref: str) -> dict:
     return out
 
 
+def wide_codes() -> dict:
+    """``name -> (checks, variables, m, N)`` of two seeded codes with rows of
+    64 edges, beyond the packed min-sum record's 27: a circulant code (4 x 66
+    base matrix, Z = 32, the 62 information block columns all present with
+    shifts of ``default_rng(41)``, a dual-diagonal parity part of identities)
+    and a code without circulant structure (64 checks on 1024 bits, each
+    check on 38 to 62 random information bits of ``default_rng(42)`` plus a
+    dual-diagonal parity part)."""
+    out = {}
+    rng = np.random.default_rng(41)
+    mb, nb, z = 4, 66, 32
+    base = -np.ones((mb, nb), np.int64)
+    base[:, : nb - mb] = rng.integers(0, z, size=(mb, nb - mb))
+    for i in range(mb):
+        base[i, nb - mb + i] = 0
+        if i > 0:
+            base[i, nb - mb + i - 1] = 0
+    bi, bj = np.nonzero(base >= 0)
+    lift = np.arange(z)
+    rr = (bi[:, None] * z + lift).ravel()
+    cc = (bj[:, None] * z + (lift + base[bi, bj][:, None]) % z).ravel()
+    out["w64qc"] = (rr, cc, mb * z, nb * z)
+    rng = np.random.default_rng(42)
+    m, n = 64, 1024
+    rows, cols = [], []
+    for i in range(m):
+        info = np.sort(rng.choice(n - m, size=int(rng.integers(38, 63)), replace=False))
+        par = [n - m + i] if i == 0 else [n - m + i - 1, n - m + i]
+        c = np.concatenate([info, par])
+        rows.append(np.full(c.size, i))
+        cols.append(c)
+    out["w64csr"] = (np.concatenate(rows), np.concatenate(cols), m, n)
+    return out
+
+
+# LLR means of the wide-row cases (the all-zero word, consistent Gaussian
+# LLRs: standard deviation sqrt(2 mean)), chosen so that some frames
+# converge in a few iterations and others run to the limit.
+WIDE_MEANS = {"w64qc": (8.0, 10.0, 10.0, 12.0), "w64csr": (9.0, 10.0, 10.0, 11.0), "dvbs2n910": (8.0, 8.5, 9.0)}
+
+
+def wide_llrs(name: str, n: int) -> np.ndarray:
+    """The seeded input LLRs of a wide-row case (``default_rng(43)``)."""
+    means = np.asarray(WIDE_MEANS[name], np.float64)[:, None]
+    rng = np.random.default_rng(43)
+    return (means + np.sqrt(2.0 * means) * rng.standard_normal((means.shape[0], n))).astype(np.float32)
+
+
+def wide_case(ref: str, name: str) -> dict:
+    """The reference on a code with rows above 27 edges: DVB-S2 normal 9/10
+    (``LDPCCode.dvbs2("9/10")``, rows of 30 edges) or one of
+    :func:`wide_codes`.  Its schedule, and its ``MinSum()``,
+    ``MinSum(0.75, 0.05, 12, early_stop=False)`` and ``SumProduct`` (10
+    iterations, with and without early stop) decodes of :func:`wide_llrs`."""
+    _import_reference(ref)
+    from commkit.coding import LDPCCode, MinSum, SumProduct, decode
+
+    if name == "dvbs2n910":
+        code = LDPCCode.dvbs2("9/10")
+    else:
+        rows, cols, m, n = wide_codes()[name]
+        code = LDPCCode(np.asarray(rows, np.int64), np.asarray(cols, np.int64), m, n)
+    row_ptr, cols_s, layer_ptr = code._schedule
+    llrs = wide_llrs(name, code.n)
+    out = {
+        f"{name}_checks": code.checks.astype(np.int32), f"{name}_variables": code.variables.astype(np.int32),
+        f"{name}_m": np.int64(code.num_checks), f"{name}_N": np.int64(code.num_variables),
+        f"{name}_n": np.int64(code.n), f"{name}_k": np.int64(code.k),
+        f"{name}_max_degree": np.int64(np.diff(row_ptr).max()),
+        f"{name}_layer_ptr": layer_ptr.astype(np.int32),
+        f"{name}_schedule_digest": digest(np.concatenate([row_ptr, cols_s]).astype(np.int32)),
+        f"{name}_llrs_digest": digest(llrs),
+    }  # fmt: skip
+    methods = {
+        "ms": MinSum(),
+        "ms2": MinSum(scale=0.75, offset=0.05, max_iterations=12, early_stop=False),
+        "sp0": SumProduct(max_iterations=10, early_stop=False),
+        "sp1": SumProduct(max_iterations=10, early_stop=True),
+    }
+    for tag, method in methods.items():
+        case = _decode_case(ref, code, llrs, method)
+        out.update({f"{name}_{tag}_{k}": v for k, v in case.items()})
+        if tag.startswith("sp") or llrs.size <= 8192:
+            res = decode(llrs.reshape(-1), code=code, method=method)
+            out[f"{name}_{tag}_post"] = np.asarray(res.llrs, np.float32).reshape(llrs.shape[0], -1)
+    return out
+
+
 def main(ref: str, only: str | None = None) -> None:
     t0 = time.time()
+    if only == "wide":
+        import multiprocessing as mp
+
+        names = ("w64qc", "w64csr", "dvbs2n910")
+        with ProcessPoolExecutor(max_workers=len(names), mp_context=mp.get_context("spawn")) as pool:
+            parts = [f.result() for f in [pool.submit(wide_case, ref, nm) for nm in names]]
+        wide = {}
+        for part in parts:
+            wide.update(part)
+        np.savez_compressed(HERE / "ldpc_wide.npz", **wide)
+        print(f"wide-row fixtures written in {time.time() - t0:.0f} s")
+        return
     if only == "generator":
         import multiprocessing as mp
 
@@ -675,4 +779,6 @@ def main(ref: str, only: str | None = None) -> None:
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
     only = next((a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")), None)
-    main(args[0] if args else "/root/reference", only)
+    if len(args) != 1:
+        sys.exit("usage: python tests/golden/make_golden.py REFERENCE_SOURCE_TREE [--only=PART]")
+    main(args[0], only)

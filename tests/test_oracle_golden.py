@@ -216,3 +216,33 @@ def test_dvbs2_normal_oracle_and_encoder():
     assert digest(llrs) == d["dvbs2n_llrs_digest"]
     bits, post, valid, iters = oracle.decode(llrs, (row_ptr, cols, N), k=k, max_iterations=50)
     _check_case(d, "dvbs2n", bits, post, valid, iters)
+
+
+@pytest.mark.parametrize("name", ["w64qc", "w64csr", "dvbs2n910"])
+def test_wide_rows_oracle_matches_reference(name):
+    """Codes with rows above 27 edges (``ldpc_wide.npz``: DVB-S2 normal 9/10,
+    and seeded codes with rows of 64): the oracle's schedule and its min-sum
+    (bit-exact) and sum-product decodes against the reference's."""
+    from tests.conftest import GOLDEN
+    from tests.golden.make_golden import wide_llrs
+
+    g = dict(np.load(GOLDEN / "ldpc_wide.npz"))
+    m, N, n, k = (int(g[f"{name}_{s}"]) for s in ("m", "N", "n", "k"))
+    row_ptr, cols, layer_ptr = oracle.schedule(g[f"{name}_checks"], g[f"{name}_variables"], m, N)
+    np.testing.assert_array_equal(layer_ptr, g[f"{name}_layer_ptr"])
+    assert digest(np.concatenate([row_ptr, cols]).astype(np.int32)) == g[f"{name}_schedule_digest"]
+    assert np.diff(row_ptr).max() == int(g[f"{name}_max_degree"]) > 27
+    llrs = wide_llrs(name, n)
+    assert digest(llrs) == g[f"{name}_llrs_digest"]
+    for tag, kw in (("ms", {}), ("ms2", dict(scale=0.75, offset=0.05, max_iterations=12, early_stop=False))):
+        bits, post, valid, iters = oracle.decode(llrs, (row_ptr, cols, N), k=k, **kw)
+        key = f"{name}_{tag}"
+        np.testing.assert_array_equal(iters, g[key + "_iters"])
+        np.testing.assert_array_equal(valid, g[key + "_valid"])
+        np.testing.assert_array_equal(np.packbits(bits.astype(np.uint8), axis=1), g[key + "_bits_packed"])
+        np.testing.assert_array_equal(post[0], g[key + "_post_first"])
+        assert digest(post) == g[key + "_post_digest"]
+    for tag, es in (("sp0", False), ("sp1", True)):
+        bits, post, valid, iters = oracle.decode(llrs, (row_ptr, cols, N), k=k, sum_product=True,
+                                                 max_iterations=10, early_stop=es)  # fmt: skip
+        check_sum_product(g, f"{name}_{tag}", bits, post, valid, iters, saturated=True)
