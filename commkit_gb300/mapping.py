@@ -421,19 +421,24 @@ def _check_method(method: str) -> None:
 
 
 def _opposite_levels(labels: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
-    """``lo``/``hi`` ``(k_a, L)`` int32 (``commkit/mapping/_demap.py:82-106``):
-    the nearest level below / above with the other bit value, -1 for none."""
+    """For each bit b and level s of an axis, the nearest level below
+    (``lo[b, s]``) and above (``hi[b, s]``) whose bit b differs from level
+    s's, -1 where there is none: ``(k_a, L)`` int32, the closed-form
+    max-log's opposite levels (``commkit/mapping/_demap.py:82-106``).
+
+    One upward and one downward scan per bit: when a level's bit equals the
+    bit of the level just below it, both share their nearest differing
+    level below; otherwise that is the level just below (and likewise
+    upwards)."""
     L, k = labels.shape
-    lo = np.empty((k, L), np.int32)
-    hi = np.empty((k, L), np.int32)
+    lo = np.full((k, L), -1, np.int32)
+    hi = np.full((k, L), -1, np.int32)
     for b in range(k):
-        col = labels[:, b]
-        change = col[1:] != col[:-1]
-        run = np.concatenate([[0], np.cumsum(change)])
-        starts = np.concatenate([[0], np.flatnonzero(change) + 1])
-        ends = np.concatenate([np.flatnonzero(change), [L - 1]])
-        lo[b] = starts[run] - 1
-        hi[b] = np.where(ends[run] + 1 < L, ends[run] + 1, -1)
+        bit = labels[:, b]
+        for s in range(1, L):
+            lo[b, s] = s - 1 if bit[s] != bit[s - 1] else lo[b, s - 1]
+        for s in range(L - 2, -1, -1):
+            hi[b, s] = s + 1 if bit[s] != bit[s + 1] else hi[b, s + 1]
     return lo, hi
 
 

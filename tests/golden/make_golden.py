@@ -44,6 +44,11 @@ Every output here is the reference's own result on seeded inputs:
   rows of 30; two seeded codes with rows of 64, circulant and not): the
   reference's schedules and its min-sum and sum-product decodes
   (``--only=wide``);
+* ``registry_calls.npz``: the reference's own launcher calls, recorded at
+  its kernel registry while its ``compute_llr`` and ``decode`` run their GPU
+  route on stand-in CuPy arrays (the tables, ``inv_s2`` from ``esn0_db``,
+  schedules and padded posteriors its host code builds), with its CPU
+  results on the same inputs (``--only=registry``);
 * ``ldpc_generator.npz``: three codes whose parity part is not invertible
   (a cycle-free code, a random code with a redundant check, a circulant
   code whose block columns have weight two), with the reference's ``k``,
@@ -677,8 +682,220 @@ def wide_case(ref: str, name: str) -> dict:
     return out
 
 
+def _cupy_stand_in():
+    """A NumPy-backed stand-in for CuPy, used only to record launcher calls:
+    its arrays are a NumPy subclass whose type lives in a module named
+    ``cupy``, which is how the reference's ``dispatch`` recognises device data
+    (``commkit/backend.py:75-81``), so the reference's host code takes its GPU
+    route and builds its launcher arguments (``commkit/mapping/_demap.py:
+    184-220, 298-352``, ``commkit/coding/ldpc.py:539-588``) on the host."""
+    if "cupy" in sys.modules:
+        return sys.modules["cupy"]
+    cp = types.ModuleType("cupy")
+
+    class ndarray(np.ndarray):
+        pass
+
+    ndarray.__module__ = "cupy"
+
+    def view(a):
+        return np.asarray(a).view(ndarray)
+
+    cp.ndarray = ndarray
+    for name in ("float32", "float64", "complex64", "complex128", "int8", "uint8", "int32", "int64", "bool_",
+                 "dtype", "newaxis", "inf", "nan", "pi"):  # fmt: skip
+        setattr(cp, name, getattr(np, name))
+    for name in ("asarray", "empty", "zeros", "ones", "arange", "full", "concatenate", "stack", "where",
+                 "empty_like", "zeros_like", "ascontiguousarray", "abs", "log2", "sqrt", "exp", "log"):  # fmt: skip
+        setattr(cp, name, (lambda f: lambda *a, **k: view(f(*a, **k)))(getattr(np, name)))
+    cp.cuda = types.SimpleNamespace(Device=lambda *a: types.SimpleNamespace(id=0))
+    cp.view = view
+    sys.modules["cupy"] = cp
+    cupyx = types.ModuleType("cupyx")
+    sp = types.ModuleType("cupyx.scipy")
+    cupyx.scipy = sp
+    sys.modules["cupyx"] = cupyx
+    sys.modules["cupyx.scipy"] = sp
+    for sub in ("ndimage", "signal", "special"):
+        m = types.ModuleType(f"cupyx.scipy.{sub}")
+        setattr(sp, sub, m)
+        sys.modules[f"cupyx.scipy.{sub}"] = m
+    return cp
+
+
+def _recording_registry(cuda_module, calls: list):
+    """Replaces the four launcher factories of the reference's real registry
+    (``commkit._cuda._KERNEL_FACTORIES``) by recorders: each call's name,
+    specialisation, positional arrays (host copies; tuples kept as tuples)
+    and keyword arguments go to ``calls``, and the launcher returns zeros of
+    its output shape.  Returns the previous factories."""
+    cp = sys.modules["cupy"]
+
+    def host(a):
+        if isinstance(a, tuple):
+            return tuple(host(t) for t in a)
+        return np.array(a) if isinstance(a, np.ndarray) else a
+
+    def factory_for(name):
+        def factory(**spec):
+            def launch(*args, **kwargs):
+                calls.append((name, dict(spec), [host(a) for a in args], dict(kwargs)))
+                if name == "ldpc_layered":
+                    B = args[0].shape[0]
+                    return cp.zeros(B, dtype=np.int32), cp.zeros(B, dtype=np.bool_)
+                n = args[0].shape[0]
+                k = kwargs["k"] if name == "llr" else args[1][-1].size + args[2][-1].size
+                return cp.zeros((n, k), dtype=np.float32)
+
+            return launch
+
+        return factory
+
+    saved = {}
+    for name in ("llr", "llr_separable_maxlog", "llr_separable", "ldpc_layered"):
+        saved[name] = cuda_module._KERNEL_FACTORIES[name]
+        cuda_module._KERNEL_FACTORIES[name] = factory_for(name)
+    return saved
+
+
+# (tag, constellation, method, Es/N0 dB, symbols): demapper calls recorded
+# from the reference's GPU route; Es/N0 goes in as esn0_db, so the recorded
+# inv_s2 also pins the reference's noise-variance rule (_demap.py:48-68,312).
+REGISTRY_LLR_CASES = (
+    ("qam16_maxlog", ("qam", 16), "maxlog", 12.0, 2048),
+    ("qam64_maxlog", ("qam", 64), "maxlog", 17.5, 2048),
+    ("qam16_exact", ("qam", 16), "exact", 9.0, 2048),
+    ("qam64_exact", ("qam", 64), "exact", 15.0, 2048),
+    ("shaped16_maxlog", ("shaped", 16), "maxlog", 10.0, 1024),
+    ("shaped16_exact", ("shaped", 16), "exact", 10.0, 1024),
+    ("psk8_maxlog", ("psk", 8), "maxlog", 11.0, 1024),
+    ("psk8_exact", ("psk", 8), "exact", 11.0, 1024),
+    ("cross32_exact", ("qam", 32), "exact", 14.0, 1024),
+)
+# (tag, code, method kind, method arguments, frames, LLR mean)
+REGISTRY_LDPC_CASES = (
+    ("codeA_ms", "A", "ms", {"max_iterations": 20}, 6, 2.2),
+    ("dvbs2s_ms", "dvbs2s", "ms", {"scale": 0.75, "offset": 0.05, "max_iterations": 12}, 4, 1.8),
+    ("dvbs2s_sp", "dvbs2s", "sp", {"max_iterations": 5}, 4, 0.8),
+    ("pon_ms", "pon", "ms", {"max_iterations": 15, "early_stop": False}, 3, 3.0),
+)
+
+
+def registry_ldpc_llrs(frames: int, n: int, mean: float) -> np.ndarray:
+    """Input LLRs of a recorded decode: ``mean + 1.5 N(0,1)`` of
+    ``default_rng(70)``, the all-zero word."""
+    rng = np.random.default_rng(70)
+    return (mean + 1.5 * rng.standard_normal((frames, n))).astype(np.float32)
+
+
+def _registry_constellation(Constellation, kind):
+    family, order = kind
+    if family == "qam":
+        return Constellation.qam(order)
+    if family == "psk":
+        return Constellation.psk(order)
+    return Constellation.qam(order).shaped(entropy=3.5)
+
+
+def registry_case(ref: str) -> dict:
+    """The reference's own launcher calls, recorded at its kernel registry:
+    its ``compute_llr`` and ``decode`` run on stand-in CuPy arrays
+    (:func:`_cupy_stand_in`) with recorders in place of the four launchers
+    (:func:`_recording_registry`), so each recorded argument tuple is what the
+    reference's host code builds for its CUDA kernels (tables from
+    ``_device_tables``, ``inv_s2``, the schedule and the zero-padded
+    posterior).  Beside each, the reference's CPU result for the same
+    input, to compare the launchers' output with."""
+    _import_reference(ref)
+    cp = _cupy_stand_in()
+    import commkit._cuda as cuda_module
+    from commkit.coding import LDPCCode, MinSum, SumProduct, decode
+    from commkit.mapping import Constellation, compute_llr
+
+    from commkit_gb300 import workloads as W
+
+    out = {}
+    calls: list = []
+    saved = _recording_registry(cuda_module, calls)
+    try:
+        for i, (tag, kind, method, esn0, n) in enumerate(REGISTRY_LLR_CASES):
+            c = _registry_constellation(Constellation, kind)
+            rng = np.random.default_rng(60 + i)
+            idx = rng.integers(0, c.points.size, size=n)
+            nv = float(c.power()) / 10 ** (esn0 / 10)
+            noise = np.sqrt(nv / 2) * (rng.standard_normal(n) + 1j * rng.standard_normal(n))
+            x = (c.points[idx] + noise).astype(np.complex64)
+            del calls[:]
+            compute_llr(cp.view(x), esn0_db=esn0, constellation=c, method=method)
+            assert len(calls) == 1, calls
+            name, spec, args, kwargs = calls[0]
+            out[f"{tag}_name"] = np.array(name)
+            out[f"{tag}_x"] = args[0]
+            for j, a in enumerate(args[1:]):
+                if isinstance(a, tuple):
+                    for t, arr in enumerate(a):
+                        out[f"{tag}_arg{j}_{t}"] = arr
+                    out[f"{tag}_arg{j}_len"] = np.int64(len(a))
+                else:
+                    out[f"{tag}_arg{j}"] = a
+            out[f"{tag}_nargs"] = np.int64(len(args) - 1)
+            for key, v in kwargs.items():
+                out[f"{tag}_kw_{key}"] = np.asarray(v)
+            out[f"{tag}_kwnames"] = np.array(sorted(kwargs))
+            out[f"{tag}_esn0_db"] = np.float64(esn0)
+            out[f"{tag}_want"] = np.asarray(
+                compute_llr(x, esn0_db=esn0, constellation=c, method=method), np.float32).reshape(n, -1)  # fmt: skip
+        for tag, which, kind, kw, frames, mean in REGISTRY_LDPC_CASES:
+            if which == "A":
+                code = LDPCCode.quasi_cyclic(W.CODE_A.base(), lifting=W.CODE_A.z)
+            elif which == "dvbs2s":
+                code = LDPCCode.dvbs2("1/2", frame="short")
+            else:
+                code = LDPCCode.pon()
+            method = MinSum(**kw) if kind == "ms" else SumProduct(**kw)
+            llrs = registry_ldpc_llrs(frames, code.n, mean)
+            del calls[:]
+            decode(cp.view(llrs.reshape(-1)), code=code, method=method)
+            assert len(calls) == 1, calls
+            name, spec, args, kwargs = calls[0]
+            out[f"{tag}_name"] = np.array(name)
+            out[f"{tag}_sum_product"] = np.bool_(spec["sum_product"])
+            # The posterior the reference builds (zeros, then the LLRs) is kept
+            # as a digest: the tests rebuild it from registry_ldpc_llrs().
+            assert np.array_equal(args[0][:, : code.n], llrs) and not args[0][:, code.n :].any()
+            out[f"{tag}_app_digest"] = digest(args[0])
+            out[f"{tag}_N"] = np.int64(args[0].shape[1])
+            out[f"{tag}_row_ptr"], out[f"{tag}_cols"], out[f"{tag}_layer_ptr"] = args[1], args[2], args[3]
+            for key, v in kwargs.items():
+                out[f"{tag}_kw_{key}"] = np.asarray(v)
+            out[f"{tag}_kwnames"] = np.array(sorted(kwargs))
+            out[f"{tag}_n"] = np.int64(code.n)
+            res = decode(llrs.reshape(-1), code=code, method=method)
+            post = np.asarray(res.llrs, np.float32).reshape(frames, -1)
+            if kind == "sp":
+                out[f"{tag}_want_post"] = post
+            else:
+                out[f"{tag}_want_post_digest"] = digest(post)
+                out[f"{tag}_want_post_first"] = post[0].copy()
+            out[f"{tag}_want_iters"] = np.asarray(res.iterations, np.int32).reshape(-1)
+            out[f"{tag}_want_valid"] = np.asarray(res.valid, bool).reshape(-1)
+    finally:
+        cuda_module._KERNEL_FACTORIES.update(saved)
+    out["llr_tags"] = np.array([c[0] for c in REGISTRY_LLR_CASES])
+    out["ldpc_tags"] = np.array([c[0] for c in REGISTRY_LDPC_CASES])
+    return out
+
+
 def main(ref: str, only: str | None = None) -> None:
     t0 = time.time()
+    if only == "registry":
+        import multiprocessing as mp
+
+        with ProcessPoolExecutor(max_workers=1, mp_context=mp.get_context("spawn")) as pool:
+            res = pool.submit(registry_case, ref).result()
+        np.savez_compressed(HERE / "registry_calls.npz", **res)
+        print(f"registry fixtures written in {time.time() - t0:.0f} s")
+        return
     if only == "wide":
         import multiprocessing as mp
 
