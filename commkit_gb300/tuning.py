@@ -9,8 +9,12 @@ and a digest of the code's schedule.  :func:`apply_cached` (called when a
 plan is created) sets a cached shape on the plan, so tuned codes decode with
 their best shape from then on.
 
-The timing batch is fixed work: random LLRs, no early stop, a few
-iterations, enough frames to fill every SM several times.
+The timing batch is what a receiver meets: frames in the code's waterfall
+region, decoded with early stop, so iteration counts are as uneven as in
+service and the persistent queue's balancing is part of what is timed.  By
+default it is the all-zero codeword under consistent Gaussian LLRs (mean mu,
+variance 2 mu, the LLRs of BPSK over AWGN), with mu found by bisection where
+half the frames fail to decode; a caller may pass its own batch instead.
 
 Cache file: ``$COMMKIT_GB300_TUNING`` or ``~/.cache/commkit_gb300/tuning.json``.
 """
@@ -105,11 +109,47 @@ def candidates(plan_info: dict) -> list[tuple[int, int, int]]:
     return sorted(shapes)
 
 
-def tune(code: Any, *, device: int = 0, frames: int | None = None, iterations: int = 6,
-         reps: int = 3, store: bool = True) -> dict:  # fmt: skip
+def waterfall_llrs(code: Any, frames: int, *, device: int = 0, iterations: int = 50, seed: int = 0):
+    """``frames`` LLR frames of the all-zero codeword in ``code``'s waterfall
+    region: consistent Gaussian LLRs ``mu + sqrt(2 mu) N(0, 1)`` with ``mu``
+    bisected (on a smaller batch, min-sum with early stop) to where about half
+    the frames fail.  Returns ``(llrs (frames, n) float32 on the device, mu)``."""
+    import torch
+
+    from .coding import MinSum, decode
+
+    dev = torch.device("cuda", device)
+    method = MinSum(max_iterations=iterations)
+    probe = max(64, min(frames, 512))
+    noise = np.random.default_rng(seed).standard_normal((probe, code.n))
+
+    def fer(mu: float) -> float:
+        llr = torch.from_numpy((mu + np.sqrt(2.0 * mu) * noise).astype(np.float32)).to(dev)
+        return float((~decode(llr, code=code, method=method).valid).float().mean())
+
+    lo, hi = 0.25, 1.0
+    while fer(hi) > 0.5 and hi < 1024.0:
+        lo, hi = hi, 2.0 * hi
+    for _ in range(7):
+        mid = 0.5 * (lo + hi)
+        if fer(mid) > 0.5:
+            lo = mid
+        else:
+            hi = mid
+    mu = 0.5 * (lo + hi)
+    rng = np.random.default_rng(seed + 1)
+    llr = (mu + np.sqrt(2.0 * mu) * rng.standard_normal((frames, code.n))).astype(np.float32)
+    return torch.from_numpy(llr).to(dev), mu
+
+
+def tune(code: Any, *, device: int = 0, frames: int | None = None, iterations: int = 50,
+         reps: int = 3, store: bool = True, llrs: Any = None) -> dict:  # fmt: skip
     """Time the candidate shapes of ``code`` on ``device``; returns the best
     ``{"threads_per_frame", "frames_per_block", "placement", "ms", "edge_updates_per_s"}``
-    (stored in the cache when ``store``) and leaves it set on the plan."""
+    (stored in the cache when ``store``) and leaves it set on the plan.
+    ``llrs``: the timing batch ``(frames, n)`` on the device, else
+    :func:`waterfall_llrs`; decoded with min-sum, ``iterations`` at most,
+    early stop."""
     import torch
 
     from .coding import MinSum, decode
@@ -118,11 +158,15 @@ def tune(code: Any, *, device: int = 0, frames: int | None = None, iterations: i
     plan = code._plan(device)
     info = plan.info
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    if frames is None:
-        frames = int(max(sms * 4, min(8192, (1 << 27) // max(1, code.num_variables))))
-    rng = np.random.default_rng(0)
-    llr = torch.from_numpy((1.0 + 2.0 * rng.standard_normal((frames, code.n))).astype(np.float32)).to(dev)
-    method = MinSum(max_iterations=iterations, early_stop=False)
+    if llrs is None:
+        if frames is None:
+            frames = int(max(sms * 4, min(2048, (1 << 27) // max(1, code.num_variables))))
+        plan.set_launch(0, 0, 0)
+        llr, _ = waterfall_llrs(code, frames, device=device, iterations=iterations)
+    else:
+        llr = llrs.reshape(-1, code.n)
+        frames = int(llr.shape[0])
+    method = MinSum(max_iterations=iterations, early_stop=True)
     ws = None
     results = []
     for t, g, place in candidates(info):
@@ -142,15 +186,17 @@ def tune(code: Any, *, device: int = 0, frames: int | None = None, iterations: i
         e1.record()
         torch.cuda.synchronize(dev)
         ms = e0.elapsed_time(e1) / reps
-        results.append((ms, t, g, place))
+        its = int(decode(llr, code=code, method=method, workspace=ws).iterations.sum())
+        results.append((ms, t, g, place, its))
     if not results:
         plan.set_launch(0, 0, 0)
         raise RuntimeError("tune(): no launch shape fits this code")
-    ms, t, g, place = min(results)
+    ms, t, g, place, its = min(results)
     best = {
         "threads_per_frame": t, "frames_per_block": g, "placement": place, "ms": ms,
-        "edge_updates_per_s": frames * iterations * info["num_edges"] / (ms * 1e-3),
-        "tried": len(results),
+        "edge_updates_per_s": its * info["num_edges"] / (ms * 1e-3),
+        "tried": len(results), "batch": {"frames": frames, "max_iterations": iterations, "early_stop": True,
+                                        "mean_iterations": its / frames},
     }  # fmt: skip
     plan.set_launch(t, g, place)
     if store:

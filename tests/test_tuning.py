@@ -53,3 +53,19 @@ def test_tune_picks_a_shape_and_keeps_results(tmp_path, monkeypatch):
     code2 = ck.LDPCCode.quasi_cyclic(W.CODE_B.base(), lifting=96)
     assert code2._plan(0).get_launch() == (best["threads_per_frame"], best["frames_per_block"], best["placement"])
     code._plan(0).set_launch(0, 0, 0)
+
+
+@pytest.mark.gpu
+def test_tuning_batch_sits_in_the_waterfall():
+    """The default timing batch: frames near the code's waterfall, decoded
+    with early stop, so iteration counts are uneven as in service."""
+    import commkit_gb300 as ck
+
+    code = ck.LDPCCode.quasi_cyclic(W.CODE_A.base(), lifting=54)
+    llr, mu = tuning.waterfall_llrs(code, 512, device=0, iterations=50)
+    assert llr.shape == (512, code.n) and mu > 0
+    res = ck.decode(llr, code=code, method=ck.MinSum(max_iterations=50))
+    fer = float((~res.valid).float().mean())
+    its = res.iterations.cpu().numpy()
+    assert 0.2 < fer < 0.8, fer
+    assert its.min() < 25 and its.max() == 50
