@@ -838,6 +838,34 @@ def measure_montecarlo(dist: Dist) -> dict:
                         "MinSum 50 it, fixed blocks per point, wall clock of the public call", "results": out}
 
 
+def measure_host_overhead(dist: Dist, calls: int = 2000) -> dict:
+    """Host time per public call, the GPU not waited for (the kernels queue
+    behind the calls): ``compute_llr`` of 4096 16-QAM symbols and ``decode``
+    of one code-A frame, each with its outputs allocated by the call, as a
+    drop-in user who calls per frame runs them."""
+    import commkit_gb300 as ck
+    from commkit_gb300 import workloads as W
+
+    torch, dev = dist.torch, dist.dev
+    c = ck.Constellation.qam(16)
+    x = torch.from_numpy((np.random.default_rng(3).standard_normal(8192).astype(np.float32)).view(np.complex64)).to(dev)
+    code = ck.LDPCCode.quasi_cyclic(W.CODE_A.base(), lifting=W.CODE_A.z)
+    llr = torch.from_numpy((2.0 + np.random.default_rng(4).standard_normal(code.n)).astype(np.float32)).to(dev)
+    method = ck.MinSum(max_iterations=20)
+    out = {}
+    for name, fn in (("compute_llr_4096_symbols", lambda: ck.compute_llr(x, noise_var=0.1, constellation=c)),
+                     ("decode_1_frame_code_A", lambda: ck.decode(llr, code=code, method=method))):  # fmt: skip
+        for _ in range(200):
+            fn()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(calls):
+            fn()
+        out[name] = (time.perf_counter() - t0) / calls * 1e6
+        torch.cuda.synchronize(dev)
+    return {"unit": "us per call (host)", "calls": calls, "results": out}
+
+
 def measure_dvbs2(dist: Dist, steps: int = 10, warmup: int = 3) -> dict:
     """The reference's own LDPC benchmark (``benchmarks/bench_coding.py:37-38,
     55-56,75-86``): 64 DVB-S2 normal-frame rate-1/2 codewords over QPSK at
@@ -1022,6 +1050,7 @@ def main() -> None:
                             ("2", lambda: measure_demapper(dist)),
                             ("2_mpoint", lambda: measure_mpoint(dist)),
                             ("reference_ldpc_benchmark", lambda: measure_dvbs2(dist)),
+                            ("host_overhead", lambda: measure_host_overhead(dist)),
                             ("f1_montecarlo", lambda: measure_montecarlo(dist)),
                             ("5", lambda: measure_served(args, dist))):  # fmt: skip
                 try:

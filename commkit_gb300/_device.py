@@ -70,7 +70,10 @@ class DeviceArray:
 
     @property
     def size(self) -> int:
-        return int(np.prod(self.shape, dtype=np.int64))
+        n = 1
+        for d in self.shape:
+            n *= int(d)
+        return n
 
     @property
     def ndim(self) -> int:

@@ -175,8 +175,11 @@ class LDPCCode:
 
     @property
     def _leading_info(self) -> bool:
-        """True when the information columns are the first k."""
-        return self.k == 0 or int(self._info[-1]) == self.k - 1
+        """True when the information columns are the first k (remembered)."""
+        lead = self.__dict__.get("_leading_memo")
+        if lead is None:
+            lead = self.__dict__["_leading_memo"] = self.k == 0 or int(self._info[-1]) == self.k - 1
+        return lead
 
     @property
     def rate(self) -> float:
@@ -418,6 +421,7 @@ class _Plan:
                    placement: int = 0) -> None:  # fmt: skip
         cfg = _lib.Launch(threads_per_frame, frames_per_block, placement)
         _lib.check(_lib.lib().ck_ldpc_plan_set_launch(self.handle, ctypes.byref(cfg)), "set_launch")
+        self.__dict__.pop("_ws_need", None)  # workspace sizes depend on the launch shape
 
     def get_launch(self) -> tuple[int, int, int]:
         cfg = _lib.Launch()
@@ -437,6 +441,28 @@ class _Plan:
         _lib.check(lib.ck_ldpc_plan_get_specialise(self.handle, ctypes.byref(mode), ctypes.byref(state)),
                    "get_specialise")  # fmt: skip
         return mode.value, state.value, (_lib.last_error() if state.value < 0 else "")
+
+    def stream_workspace(self, like: _device.DeviceArray, stream: int, rows: int, rule: int):
+        """A decode workspace for ``rows`` frames kept per (stream, rule) and
+        reused by later calls on that stream (grown when a call needs more),
+        so a decode allocates nothing but its outputs; and the lock that
+        serialises its use by host threads (a decode resets the workspace's
+        frame counter and launches on the stream, and two threads
+        interleaving those on one workspace would corrupt both).  Work on
+        one stream runs in order, so calls never overlap on the device."""
+        import threading
+
+        cache = self.__dict__.setdefault("_stream_ws", {})
+        key = (stream, rule)
+        entry = cache.get(key)
+        size_key = (rows, rule)
+        need = self.__dict__.setdefault("_ws_need", {}).get(size_key)
+        if need is None:
+            need = self._ws_need[size_key] = self.workspace_size(rows, rule)
+        if entry is None or entry[0].numel() < need:
+            lock = entry[1] if entry is not None else threading.Lock()
+            entry = cache[key] = (_device.empty(like, (max(need, 256),), np.uint8), lock)
+        return entry
 
     def workspace_size(self, frames: int, rule: int = _lib.CK_LDPC_MIN_SUM) -> int:
         size = ctypes.c_size_t(0)
@@ -509,6 +535,8 @@ def decode(llrs: Any, *, code: LDPCCode, method: MinSum | SumProduct | None = No
         raise TypeError(f"decode(): code must be an LDPCCode, got {type(code).__name__}.")
     method = _resolve_method(method)
     x0 = _device.wrap(llrs, "llrs")
+    if workspace is None and x0.kind == "torch" and x0.dtype == np.float32 and x0.contiguous and code._leading_info:
+        return _decode_torch(llrs, x0, code, method)
     x = _as_llrs(llrs, x0)
     was_1d = x0.ndim == 1
     x2 = x.reshape(1, -1) if was_1d else x
@@ -536,30 +564,28 @@ def decode(llrs: Any, *, code: LDPCCode, method: MinSum | SumProduct | None = No
     iters = _device.empty(xd, (rows,), np.int32)
     valid_u8 = _device.empty(xd, (rows,), np.uint8)
     if rows:
+        ptr = (lambda a: a.data_ptr()) if xd.kind == "torch" else (lambda a: _device.wrap(a).ptr)
         with _device.on_device(xd):
             plan = code._plan(xd.device)
             stream = _device.stream_of(xd)
-            ws_ptr, ws_bytes = 0, 0
             rule, scale, offset = _rule_args(method)
+            lock = None
             if workspace is None:
-                need = plan.workspace_size(rows, rule)
-                workspace = _device.empty(xd, (need,), np.uint8)
+                workspace, lock = plan.stream_workspace(xd, stream, rows, rule)
             wsd = _device.wrap(workspace, "workspace")
-            ws_ptr, ws_bytes = wsd.ptr, wsd.size
-            st = _lib.lib().ck_ldpc_decode(
-                plan.handle, xd.ptr, _device.wrap(out_llrs).ptr, rows, code.n,
-                rule, scale, offset,
-                int(method.max_iterations), 1 if method.early_stop else 0,
-                _device.wrap(iters).ptr, _device.wrap(valid_u8).ptr,
-                _device.wrap(bits).ptr if leading else None, k if leading else 0,
-                ws_ptr, ws_bytes, stream,
-            )  # fmt: skip
+            args = (plan.handle, xd.ptr, ptr(out_llrs), rows, code.n, rule, scale, offset,
+                    int(method.max_iterations), 1 if method.early_stop else 0, ptr(iters), ptr(valid_u8),
+                    ptr(bits) if leading else None, k if leading else 0, wsd.ptr, wsd.size, stream)  # fmt: skip
+            if lock is None:
+                st = _lib.lib().ck_ldpc_decode(*args)
+            else:
+                with lock:  # the workspace's counter reset and launch, enqueued as a pair
+                    st = _lib.lib().ck_ldpc_decode(*args)
             _lib.check(st, "decode()")
             if not leading:
                 # Hard decisions at the information columns (ldpc.py:582-586).
                 st = _lib.lib().ck_ldpc_column_signs(
-                    _device.wrap(out_llrs).ptr, rows, code.n, _device.wrap(_info_columns(code, xd)).ptr, k,
-                    _device.wrap(bits).ptr, stream,
+                    ptr(out_llrs), rows, code.n, _device.wrap(_info_columns(code, xd)).ptr, k, ptr(bits), stream,
                 )  # fmt: skip
                 _lib.check(st, "decode() bits")
     valid = valid_u8.view(_bool_dtype(xd))
@@ -570,6 +596,48 @@ def decode(llrs: Any, *, code: LDPCCode, method: MinSum | SumProduct | None = No
 
     return DecodeResult(bits=shaped(bits, k), llrs=shaped(out_llrs, code.n),
                         valid=shaped(valid, 1), iterations=shaped(iters, 1), checked=True)  # fmt: skip
+
+
+def _decode_torch(llrs: Any, x0: _device.DeviceArray, code: LDPCCode, method: MinSum | SumProduct) -> DecodeResult:
+    """``decode`` of contiguous float32 torch LLRs of a code whose information
+    bits lead its codeword, with the plan's per-stream workspace: the outputs
+    are allocated in their final shapes and every pointer comes straight from
+    the tensors, so the host work is little more than the four allocations
+    and the launch (the same kernel and results as the general path)."""
+    import torch
+
+    shape = x0.shape
+    if len(shape) not in (1, 2):
+        raise ValueError(f"decode(): llrs must be 1-D or 2-D, got {len(shape)}-D.")
+    n, k = code.n, code.k
+    last = shape[-1]
+    if last % n:
+        raise ValueError(
+            f"decode(): the last axis of llrs ({last}) must be a multiple of the block length {n}."
+        )  # fmt: skip
+    nb = last // n
+    C = 1 if len(shape) == 1 else shape[0]
+    rows = C * nb
+    dev = llrs.device
+    lead = () if len(shape) == 1 else (C,)
+    out_llrs = torch.empty(lead + (nb * n,), dtype=torch.float32, device=dev)
+    bits = torch.empty(lead + (nb * k,), dtype=torch.int8, device=dev)
+    iters = torch.empty(lead + (nb,), dtype=torch.int32, device=dev)
+    valid = torch.empty(lead + (nb,), dtype=torch.bool, device=dev)
+    if rows:
+        with _device.on_device(x0):
+            plan = code._plan(x0.device)
+            stream = _device.stream_of(x0)
+            rule, scale, offset = _rule_args(method)
+            ws, lock = plan.stream_workspace(x0, stream, rows, rule)
+            with lock:
+                st = _lib.lib().ck_ldpc_decode(
+                    plan.handle, x0.ptr, out_llrs.data_ptr(), rows, n, rule, scale, offset,
+                    int(method.max_iterations), 1 if method.early_stop else 0, iters.data_ptr(),
+                    valid.data_ptr(), bits.data_ptr(), k, ws.data_ptr(), ws.numel(), stream,
+                )  # fmt: skip
+            _lib.check(st, "decode()")
+    return DecodeResult(bits=bits, llrs=out_llrs, valid=valid, iterations=iters, checked=True)
 
 
 def _encoder_tables(code: LDPCCode, like: _device.DeviceArray) -> tuple:

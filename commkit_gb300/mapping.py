@@ -330,7 +330,10 @@ class Constellation:
         separable lattices per axis, every other constellation over all its
         points."""
         nv = _finite(noise_var, "Constellation.llr(): noise_var", low=0.0)
-        x = _device.wrap(symbols, "symbols")
+        return self._llr(symbols, _device.wrap(symbols, "symbols"), nv, method)
+
+    def _llr(self, symbols: Any, x: _device.DeviceArray, nv: float, method: str) -> Any:
+        """``llr`` on already wrapped symbols (``compute_llr`` wraps once)."""
         if x.dtype.kind != "c":
             # Real noise of variance s2: the in-phase part of circular noise of 2 s2.
             nv = 2.0 * nv
@@ -477,12 +480,21 @@ def _table_kind(c: Constellation, method: str) -> str:
     """Which kernel serves ``c`` (``commkit/mapping/_demap.py:112-118,
     298-352``, ``constellation.py:327-332``): the closed form for max-log of
     a uniform separable lattice, the per-axis level metrics for other
-    separable lattices, every point otherwise."""
-    if c._axes is None:
-        return "points"
-    if method == "maxlog" and all(a.pmf is None and a.levels.size >= 2 for a in c._axes):
-        return "maxlog"
-    return "levels"
+    separable lattices, every point otherwise.  Remembered on the
+    (immutable) instance per method."""
+    memo = c.__dict__.get("_table_kinds")
+    if memo is None:
+        memo = c.__dict__["_table_kinds"] = {}
+    kind = memo.get(method)
+    if kind is None:
+        if c._axes is None:
+            kind = "points"
+        elif method == "maxlog" and all(a.pmf is None and a.levels.size >= 2 for a in c._axes):
+            kind = "maxlog"
+        else:
+            kind = "levels"
+        memo[method] = kind
+    return kind
 
 
 def device_tables(constellation: Constellation, kind: str, like: _device.DeviceArray):
@@ -499,6 +511,23 @@ def device_tables(constellation: Constellation, kind: str, like: _device.DeviceA
         dev = torch.device("cuda", like.device)
         t = per[key] = tuple(torch.from_numpy(a.copy()).to(dev) for a in host_tables(constellation, kind))
     return t
+
+
+def _axis_args(constellation: Constellation, kind: str, like: _device.DeviceArray) -> tuple:
+    """The two axes' C-ABI structs of ``device_tables`` and pointers to them
+    (``ctypes.byref``), built once per table kind and device and kept with
+    the tables, so a call passes them as they are."""
+    per = constellation.__dict__.get("_axis_args")
+    if per is None:
+        per = constellation.__dict__["_axis_args"] = {}
+    key = (kind, like.device)
+    args = per.get(key)
+    if args is None:
+        tables = device_tables(constellation, kind, like)
+        half = len(tables) // 2
+        re, im = _axis_struct(tables[:half], kind), _axis_struct(tables[half:], kind)
+        args = per[key] = (re, im, ctypes.byref(re), ctypes.byref(im), tables)
+    return args
 
 
 def _axis_struct(tables, kind: str):
@@ -537,29 +566,36 @@ def _llr_separable_gpu(symbols: Any, x: _device.DeviceArray, c: Constellation, n
     """``commkit/mapping/_demap.py:298-352`` on the sm_103a kernels."""
     _check_method(method)
     k = c.bits_per_symbol
-    flat = _as_complex64(symbols, x, "compute_llr() / Constellation.llr()")
-    fx = _device.wrap(flat, "symbols")
-    n = fx.size
+    if x.kind == "torch" and x.contiguous and x.dtype == np.complex64:
+        # The common case: the symbols as they are, no copy and no new wrap.
+        ptr, n = x.ptr, x.size
+    else:
+        flat = _as_complex64(symbols, x, "compute_llr() / Constellation.llr()")
+        fx = _device.wrap(flat, "symbols")
+        ptr, n = fx.ptr, fx.size
     if n >= 2**31:
         raise ValueError(f"at most 2**31 - 1 symbols per call, got {n}")
-    out = _device.empty(x, (n, k), np.float32)
-    od = _device.wrap(out, "out")
+    # The output in its final shape, (..., N * k): the same memory as (n, k).
+    shape = tuple(x.shape[:-1]) + (x.shape[-1] * k,) if x.ndim else (k,)
+    if x.kind == "torch":
+        torch = _device._torch()
+        out = torch.empty(shape, dtype=torch.float32, device=symbols.device)
+        out_ptr = out.data_ptr()
+    else:
+        out = _device.empty(x, shape, np.float32)
+        out_ptr = _device.wrap(out, "out").ptr
     kind = _table_kind(c, method)
     with _device.on_device(x):
-        tables = device_tables(c, kind, x)
-        half = len(tables) // 2
-        re, im = _axis_struct(tables[:half], kind), _axis_struct(tables[half:], kind)
+        _, _, re_ref, im_ref, _ = _axis_args(c, kind, x)
         stream = _device.stream_of(x)
         lib = _lib.lib()
         if kind == "maxlog":
-            st = lib.ck_llr_separable_maxlog(fx.ptr, n, ctypes.byref(re), ctypes.byref(im),
-                                             inv_s2(nv), od.ptr, stream)  # fmt: skip
+            st = lib.ck_llr_separable_maxlog(ptr, n, re_ref, im_ref, inv_s2(nv), out_ptr, stream)
         else:
-            st = lib.ck_llr_separable(fx.ptr, n, ctypes.byref(re), ctypes.byref(im), inv_s2(nv),
-                                      1 if method == "exact" else 0, od.ptr, stream)  # fmt: skip
+            st = lib.ck_llr_separable(ptr, n, re_ref, im_ref, inv_s2(nv), 1 if method == "exact" else 0,
+                                      out_ptr, stream)  # fmt: skip
         _lib.check(st, "compute_llr()")
-    shape = tuple(x.shape[:-1]) + (x.shape[-1] * k,) if x.ndim else (k,)
-    return out.reshape(shape)
+    return out
 
 
 def _llr_points_gpu(symbols: Any, x: _device.DeviceArray, c: Constellation, nv: float,
@@ -601,7 +637,7 @@ def compute_llr(symbols: Any, *, noise_var: float | None = None, esn0_db: float 
         raise ValueError("compute_llr(): constellation is required for array input.")
     x = _device.wrap(symbols, "symbols")
     nv = _noise_variance(noise_var, esn0_db, constellation, x.dtype.kind != "c", "compute_llr()")
-    return constellation.llr(symbols, noise_var=nv, method=method)
+    return constellation._llr(symbols, x, nv, method)
 
 
 def inv_s2_frames(noise_var: Any) -> np.ndarray:
