@@ -71,7 +71,22 @@ struct LevelAxis {
     float logp[L];
     int32_t lab[L];
     int32_t pos[KA];
+    // Per-level records of the exact method: level, log prior, then the
+    // half weights, 1 in slot 2 + b where level j's bit b is 0 and in slot
+    // 2 + KA + b where it is 1, else 0; padded to 16 bytes.
+    static constexpr int R = (2 + 2 * KA + 3) / 4 * 4;
+    alignas(16) float rec[L][R];
+    uint32_t half1[KA];  // per bit: bit j set where level j's bit is 1
 };
+
+// A 16-byte shared-memory load that the compiler may neither hoist out of a
+// loop nor merge with another (volatile), so table records are read where
+// they are used instead of being held in registers across the symbol loop.
+__device__ __forceinline__ float4 lds4(uint32_t addr) {
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr));
+    return v;
+}
 
 template <int KA>
 __device__ __forceinline__ float level_metric(const LevelAxis<KA>& t, int j, float x,
@@ -120,6 +135,7 @@ __device__ __forceinline__ void axis_levels(float x, const LevelAxis<KA>& t, flo
         for (int b = 0; b < KA; ++b) o[b] = __fsub_rn(p0[b], p1[b]);
         return;
     }
+    // (The exact method of axes up to 16 levels runs axis_exact below.)
     // Pass 2: the half-sums of e_j = exp(m_j - peak), ascending j.
     float s0[KA], s1[KA];
 #pragma unroll
@@ -159,6 +175,105 @@ __device__ __forceinline__ void axis_levels(float x, const LevelAxis<KA>& t, flo
     }
 }
 
+// e^x for x <= 0 (also -inf and NaN), accurate to a few units in the last
+// place: 2^(x log2 e) with the product x log2 e carried beyond float
+// precision (the argument split of Cody and Waite, "Software Manual for the
+// Elementary Functions", 1980: a float head y = rn(x L2E), its exact residual
+// from a fused multiply-add, plus x times the tail of log2 e), then 2^y from
+// the hardware's ex2 and the factor 2^r = 1 + r ln 2 (|r| is below an ulp of
+// y, so the next term is far below float precision).  The argument is first
+// held at -200 or above, NaN kept (e^-200 is 0 in float), so -inf gives 0.
+__device__ __forceinline__ float exp_split(float x) {
+    constexpr float kL2E = 1.44269502162933349609375f;  // log2(e) rounded to float
+    constexpr float kL2ELo = 1.925963033500011e-8f;      // log2(e) - kL2E
+    constexpr float kLn2 = 0.693147180559945309f;
+    float xc;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(xc) : "f"(x), "f"(-200.0f));
+    const float y = __fmul_rn(xc, kL2E);
+    const float r = __fmaf_rn(xc, kL2ELo, __fmaf_rn(xc, kL2E, -y));
+    float p;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(p) : "f"(y));
+    return __fmaf_rn(p, __fmul_rn(r, kLn2), p);
+}
+
+// The exact method (the reference's log-sum-exp, commkit/mapping/
+// _numba_llr.py:35-81) for axes of up to 16 levels, shaped for issue rate:
+// the level metrics stay in registers; the half-sums run in the reference's
+// order (ascending level) as fused multiply-adds with a 0/1 weight per level
+// and half, each exact (e * 1 + s rounds once as e + s does, e * 0 + s is
+// s), so no per-level branch on the label; exp is exp_split and log the
+// hardware's lg2 times ln 2 (__logf), within the 1e-5 relative / 1e-6
+// absolute tolerance against the reference.  A half-sum below 1e-26 is
+// redone relative to that half's own largest metric, as the reference does,
+// over the half's levels only (a level of the other half may lie far above
+// that maximum).  The peak is the largest metric: the reference's "first,
+// then any strictly greater" equals fmaxf here, since the metrics are either
+// all NaN (a NaN symbol) or none.
+template <int KA>
+__device__ __forceinline__ void axis_exact(float x, const LevelAxis<KA>& t, float inv_s2, float* o) {
+    constexpr int L = 1 << KA, R = LevelAxis<KA>::R;
+    const uint32_t base = ck::smem_addr(&t.rec[0][0]);
+    // Level j's record, R words from its shared address.
+    auto record = [&](int j, float (&r)[R]) {
+#pragma unroll
+        for (int q = 0; q < R / 4; ++q) {
+            const float4 v = lds4(base + static_cast<uint32_t>((j * R + 4 * q) * 4));
+            r[4 * q] = v.x;
+            r[4 * q + 1] = v.y;
+            r[4 * q + 2] = v.z;
+            r[4 * q + 3] = v.w;
+        }
+    };
+    float m[L];
+    float peak = 0.0f;
+#pragma unroll
+    for (int j = 0; j < L; ++j) {
+        float r[R];
+        record(j, r);
+        m[j] = __fadd_rn(neg_sq_scaled(__fsub_rn(x, r[0]), inv_s2), r[1]);
+        peak = j == 0 ? m[j] : fmaxf(peak, m[j]);
+    }
+    float s0[KA], s1[KA];
+#pragma unroll
+    for (int b = 0; b < KA; ++b) s0[b] = s1[b] = 0.0f;
+#pragma unroll
+    for (int j = 0; j < L; ++j) {
+        float r[R];
+        record(j, r);
+        const float e = exp_split(__fsub_rn(m[j], peak));
+#pragma unroll
+        for (int b = 0; b < KA; ++b) {
+            s0[b] = __fmaf_rn(e, r[2 + b], s0[b]);
+            s1[b] = __fmaf_rn(e, r[2 + KA + b], s1[b]);
+        }
+    }
+#pragma unroll
+    for (int b = 0; b < KA; ++b) {
+        float l[2];
+#pragma unroll
+        for (int v = 0; v < 2; ++v) {
+            const float sv = v ? s1[b] : s0[b];
+            if (sv >= kExactFloor) {
+                l[v] = __logf(sv);
+                continue;
+            }
+            // Underflowed half (rare): its largest metric p, then the sum
+            // relative to p over its own levels, ascending.
+            const uint32_t mask = v ? t.half1[b] : ~t.half1[b];
+            float p = -ck::inf_f();
+#pragma unroll
+            for (int j = 0; j < L; ++j)
+                if ((mask >> j) & 1u) p = fmaxf(p, m[j]);
+            float acc = 0.0f;
+#pragma unroll
+            for (int j = 0; j < L; ++j)
+                if ((mask >> j) & 1u) acc = __fadd_rn(acc, exp_split(__fsub_rn(m[j], p)));
+            l[v] = __fadd_rn(__logf(acc), __fsub_rn(p, peak));
+        }
+        o[b] = __fsub_rn(l[0], l[1]);
+    }
+}
+
 template <int KA>
 __device__ __forceinline__ void load_level_axis(LevelAxis<KA>& t, const ck_axis_levels& a) {
     constexpr int L = 1 << KA;
@@ -166,8 +281,24 @@ __device__ __forceinline__ void load_level_axis(LevelAxis<KA>& t, const ck_axis_
         t.lev[i] = a.levels[i];
         t.logp[i] = a.logp[i];
         t.lab[i] = a.labels[i];
+        constexpr int R = LevelAxis<KA>::R;
+        t.rec[i][0] = a.levels[i];
+        t.rec[i][1] = a.logp[i];
+#pragma unroll
+        for (int b = 0; b < KA; ++b) {
+            const bool one = (a.labels[i] >> (KA - 1 - b)) & 1;
+            t.rec[i][2 + b] = one ? 0.0f : 1.0f;
+            t.rec[i][2 + KA + b] = one ? 1.0f : 0.0f;
+        }
+#pragma unroll
+        for (int w = 2 + 2 * KA; w < R; ++w) t.rec[i][w] = 0.0f;
     }
-    for (int i = threadIdx.x; i < KA; i += blockDim.x) t.pos[i] = a.pos[i];
+    for (int i = threadIdx.x; i < KA; i += blockDim.x) {
+        t.pos[i] = a.pos[i];
+        uint32_t h = 0u;
+        for (int j = 0; j < L && j < 32; ++j) h |= static_cast<uint32_t>((a.labels[j] >> (KA - 1 - i)) & 1) << j;
+        t.half1[i] = h;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -183,8 +314,9 @@ struct NoiseScale {
     __device__ __forceinline__ float at(uint32_t i) const {
         return frames ? __ldg(frames + frame_len.div(i)) : value;
     }
-    // Symbols i and i + 1: one division; the second is in the next frame
-    // only when i + 1 starts it.
+    // Symbols i and i + 1 (i even): one division; with frames of even
+    // length both are in one frame, else the second is in the next frame
+    // when i + 1 starts it.
     __device__ __forceinline__ void pair(uint32_t i, float& a, float& b) const {
         if (!frames) {
             a = b = value;
@@ -192,7 +324,10 @@ struct NoiseScale {
         }
         const uint32_t f = frame_len.div(i);
         a = __ldg(frames + f);
-        b = i + 1 == (f + 1) * frame_len.d ? __ldg(frames + f + 1) : a;
+        if (frame_len.d & 1u)
+            b = i + 1 == (f + 1) * frame_len.d ? __ldg(frames + f + 1) : a;
+        else
+            b = a;
     }
 };
 
@@ -226,8 +361,13 @@ struct Tables<KA, 1> {  // level metrics, max-log
 template <int KA>
 struct Tables<KA, 2> : Tables<KA, 1> {  // level metrics, exact
     __device__ __forceinline__ void symbol(float2 x, float s2, float* o) const {
-        axis_levels<KA, true>(x.x, this->re, s2, o);
-        axis_levels<KA, true>(x.y, this->im, s2, o + KA);
+        if constexpr (KA <= 4) {
+            axis_exact<KA>(x.x, this->re, s2, o);
+            axis_exact<KA>(x.y, this->im, s2, o + KA);
+        } else {
+            axis_levels<KA, true>(x.x, this->re, s2, o);
+            axis_levels<KA, true>(x.y, this->im, s2, o + KA);
+        }
     }
 };
 
@@ -256,12 +396,13 @@ __device__ __forceinline__ void store_scattered(const T& tab, float* out, uint32
 
 // Main kernel: two symbols per 16-byte load, two loads in flight per thread.
 // PAIRS = false is the fallback for buffers that are not 16-byte aligned:
-// one symbol per thread and scalar stores.  The closed form is held to 32
-// registers, so 8 blocks (64 warps) share an SM and keep more loads in
-// flight (38-40 registers left 6 blocks: 64-QAM 33.0 -> 31.0 us at 2^22
-// symbols, 16-QAM unchanged, a few bytes of spill outside the main loop).
+// one symbol per thread and scalar stores.  The closed form is held to 64
+// registers (4 blocks of 256 per SM): measured at 2^22 symbols against 8,
+// 6 and 4 blocks per SM, with and without the next pairs loaded ahead of
+// the arithmetic, this was fastest (16-QAM 24.8 -> 22.0 us, 64-QAM 33.1 ->
+// 28.5 us against 8 blocks; the load-ahead gained nothing).
 template <int KA, int METHOD, bool PAIRS>
-__global__ void __launch_bounds__(kThreads, METHOD == 0 ? 8 : 1) llr_kernel(const float2* __restrict__ x, uint32_t n,
+__global__ void __launch_bounds__(kThreads, METHOD == 0 ? 4 : (METHOD == 2 && KA <= 4 ? 2 : 1)) llr_kernel(const float2* __restrict__ x, uint32_t n,
                                                        const typename AxisArg<METHOD>::type re,
                                                        const typename AxisArg<METHOD>::type im,
                                                        const NoiseScale noise,
@@ -273,6 +414,13 @@ __global__ void __launch_bounds__(kThreads, METHOD == 0 ? 8 : 1) llr_kernel(cons
     const uint32_t npairs = n >> 1;
     const float4* x4 = reinterpret_cast<const float4*>(x);
     const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    // The closed form's first two symbol pairs are requested before the
+    // tables are staged, so the two latencies overlap.
+    float4 va = zero4, vb = zero4;
+    if (PAIRS && METHOD == 0) {
+        if (t0 < npairs) va = ld_stream(x4 + t0);
+        if (t0 + stride < npairs) vb = ld_stream(x4 + t0 + stride);
+    }
     tab.load(re, im);
     __syncthreads();
     bool standard = true;
@@ -314,8 +462,6 @@ __global__ void __launch_bounds__(kThreads, METHOD == 0 ? 8 : 1) llr_kernel(cons
         for (uint32_t p = t0; p < npairs; p += 2 * stride) {
             const uint32_t pb = p + stride;
             const bool two = pb < npairs;
-            const float4 va = ld_stream(x4 + p);
-            const float4 vb = two ? ld_stream(x4 + pb) : zero4;
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 if (h == 1 && !two) break;
@@ -337,6 +483,9 @@ __global__ void __launch_bounds__(kThreads, METHOD == 0 ? 8 : 1) llr_kernel(cons
                     store_scattered<KA>(tab, out, 2 * pp + 1, o + K);
                 }
             }
+            const uint32_t q = p + 2 * stride;
+            va = q < npairs ? ld_stream(x4 + q) : zero4;
+            vb = q + stride < npairs ? ld_stream(x4 + q + stride) : zero4;
         }
         // Odd count: the last symbol.
         if ((n & 1u) && t0 == 0) {
