@@ -77,7 +77,19 @@ struct LevelAxis {
     static constexpr int R = (2 + 2 * KA + 3) / 4 * 4;
     alignas(16) float rec[L][R];
     uint32_t half1[KA];  // per bit: bit j set where level j's bit is 1
+    // (level, log prior) pairs, and whether the labels are the binary
+    // reflected Gray code of the level index (label j = j ^ (j >> 1), as
+    // the axes of the reference's square QAM and of its shaped forms have):
+    // then the halves of every bit are known at compile time.
+    alignas(16) float2 lp[L];
+    int32_t gray;
 };
+
+__device__ __forceinline__ float2 lds2(uint32_t addr) {
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
+    return v;
+}
 
 // A 16-byte shared-memory load that the compiler may neither hoist out of a
 // loop nor merge with another (volatile), so table records are read where
@@ -274,6 +286,135 @@ __device__ __forceinline__ void axis_exact(float x, const LevelAxis<KA>& t, floa
     }
 }
 
+// Packed pairs of floats for the FMA pipe's two-lane forms (add, sub, mul,
+// fma .rn.f32x2, sm_100 and later): each lane rounds as the scalar _rn
+// operation does, so results are bit for bit those of two scalar ops, at
+// half the instruction count.
+__device__ __forceinline__ uint64_t pk2(float lo, float hi) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void upk2(uint64_t v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+    uint64_t r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
+    uint64_t r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+    uint64_t r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+// exp_split of two arguments, its multiply-adds in the two-lane forms: the
+// same operations, so the same bits.
+__device__ __forceinline__ void exp_split2(float x0, float x1, float& e0, float& e1) {
+    constexpr float kL2E = 1.44269502162933349609375f;
+    constexpr float kL2ELo = 1.925963033500011e-8f;
+    constexpr float kLn2 = 0.693147180559945309f;
+    float c0, c1;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(c0) : "f"(x0), "f"(-200.0f));
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(c1) : "f"(x1), "f"(-200.0f));
+    const uint64_t xc = pk2(c0, c1);
+    const uint64_t y = mul2(xc, pk2(kL2E, kL2E));
+    float y0, y1;
+    upk2(y, y0, y1);
+    const uint64_t r = fma2(xc, pk2(kL2ELo, kL2ELo), fma2(xc, pk2(kL2E, kL2E), pk2(-y0, -y1)));
+    float p0, p1;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(p0) : "f"(y0));
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(p1) : "f"(y1));
+    const uint64_t p = pk2(p0, p1);
+    upk2(fma2(p, mul2(r, pk2(kLn2, kLn2)), p), e0, e1);
+}
+
+// Bit b (axis order, MSB first) of level j's Gray label.
+template <int KA>
+__host__ __device__ constexpr int gray_bit(int j, int b) {
+    return ((j ^ (j >> 1)) >> (KA - 1 - b)) & 1;
+}
+
+// axis_exact for Gray-labelled axes: the same operations in the same order,
+// with each bit's halves known at compile time, so the half-sums are plain
+// additions over their own levels (ascending, each starting from its first
+// term, as 0 + e is e), the underflow redo likewise, and no weights.
+template <int KA>
+__device__ __forceinline__ void axis_exact_gray(float x, const LevelAxis<KA>& t, float inv_s2, float* o) {
+    constexpr int L = 1 << KA;  // even: L >= 2
+    const uint32_t base = ck::smem_addr(&t.lp[0]);
+    // Metrics two levels at a time: -(d*d)*s2 + logp with d = x - level,
+    // rounded as the scalar steps (-(d*d) times s2 is d*d times -s2).
+    float m[L];
+    const uint64_t x2 = pk2(x, x), ns2 = pk2(-inv_s2, -inv_s2);
+#pragma unroll
+    for (int j = 0; j < L; j += 2) {
+        const float4 v = lds4(base + 8u * static_cast<uint32_t>(j));  // (lev j, logp j, lev j+1, logp j+1)
+        const uint64_t d = sub2(x2, pk2(v.x, v.z));
+        upk2(add2(mul2(mul2(d, d), ns2), pk2(v.y, v.w)), m[j], m[j + 1]);
+    }
+    float peak = m[0];
+#pragma unroll
+    for (int j = 1; j < L; ++j) peak = fmaxf(peak, m[j]);
+    float e[L];
+#pragma unroll
+    for (int j = 0; j < L; j += 2) {
+        float a, b;
+        upk2(sub2(pk2(m[j], m[j + 1]), pk2(peak, peak)), a, b);
+        exp_split2(a, b, e[j], e[j + 1]);
+    }
+#pragma unroll
+    for (int b = 0; b < KA; ++b) {
+        float sum[2] = {0.0f, 0.0f};
+        bool seen[2] = {false, false};
+#pragma unroll
+        for (int j = 0; j < L; ++j) {
+            const int v = gray_bit<KA>(j, b);
+            sum[v] = seen[v] ? __fadd_rn(sum[v], e[j]) : e[j];
+            seen[v] = true;
+        }
+        float l[2];
+#pragma unroll
+        for (int v = 0; v < 2; ++v) {
+            if (sum[v] >= kExactFloor) {
+                l[v] = __logf(sum[v]);
+                continue;
+            }
+            // Underflowed half (rare): relative to its own largest metric.
+            float p = 0.0f;
+            bool first = true;
+#pragma unroll
+            for (int j = 0; j < L; ++j) {
+                if (gray_bit<KA>(j, b) != v) continue;
+                p = first ? m[j] : fmaxf(p, m[j]);
+                first = false;
+            }
+            float acc = 0.0f;
+            first = true;
+#pragma unroll
+            for (int j = 0; j < L; ++j) {
+                if (gray_bit<KA>(j, b) != v) continue;
+                const float ej = exp_split(__fsub_rn(m[j], p));
+                acc = first ? ej : __fadd_rn(acc, ej);
+                first = false;
+            }
+            l[v] = __fadd_rn(__logf(acc), __fsub_rn(p, peak));
+        }
+        o[b] = __fsub_rn(l[0], l[1]);
+    }
+}
+
 template <int KA>
 __device__ __forceinline__ void load_level_axis(LevelAxis<KA>& t, const ck_axis_levels& a) {
     constexpr int L = 1 << KA;
@@ -282,6 +423,7 @@ __device__ __forceinline__ void load_level_axis(LevelAxis<KA>& t, const ck_axis_
         t.logp[i] = a.logp[i];
         t.lab[i] = a.labels[i];
         constexpr int R = LevelAxis<KA>::R;
+        t.lp[i] = make_float2(a.levels[i], a.logp[i]);
         t.rec[i][0] = a.levels[i];
         t.rec[i][1] = a.logp[i];
 #pragma unroll
@@ -292,6 +434,11 @@ __device__ __forceinline__ void load_level_axis(LevelAxis<KA>& t, const ck_axis_
         }
 #pragma unroll
         for (int w = 2 + 2 * KA; w < R; ++w) t.rec[i][w] = 0.0f;
+    }
+    if (threadIdx.x == 0) {
+        int32_t g = 1;
+        for (int j = 0; j < L; ++j) g &= a.labels[j] == (j ^ (j >> 1)) ? 1 : 0;
+        t.gray = g;
     }
     for (int i = threadIdx.x; i < KA; i += blockDim.x) {
         t.pos[i] = a.pos[i];
@@ -362,8 +509,13 @@ template <int KA>
 struct Tables<KA, 2> : Tables<KA, 1> {  // level metrics, exact
     __device__ __forceinline__ void symbol(float2 x, float s2, float* o) const {
         if constexpr (KA <= 4) {
-            axis_exact<KA>(x.x, this->re, s2, o);
-            axis_exact<KA>(x.y, this->im, s2, o + KA);
+            if (this->re.gray & this->im.gray) {  // block-uniform
+                axis_exact_gray<KA>(x.x, this->re, s2, o);
+                axis_exact_gray<KA>(x.y, this->im, s2, o + KA);
+            } else {
+                axis_exact<KA>(x.x, this->re, s2, o);
+                axis_exact<KA>(x.y, this->im, s2, o + KA);
+            }
         } else {
             axis_levels<KA, true>(x.x, this->re, s2, o);
             axis_levels<KA, true>(x.y, this->im, s2, o + KA);
