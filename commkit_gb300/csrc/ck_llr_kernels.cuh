@@ -552,9 +552,12 @@ __device__ __forceinline__ void store_scattered(const T& tab, float* out, uint32
 // registers (4 blocks of 256 per SM): measured at 2^22 symbols against 8,
 // 6 and 4 blocks per SM, with and without the next pairs loaded ahead of
 // the arithmetic, this was fastest (16-QAM 24.8 -> 22.0 us, 64-QAM 33.1 ->
-// 28.5 us against 8 blocks; the load-ahead gained nothing).
+// 28.5 us against 8 blocks; the load-ahead gained nothing).  The exact
+// form is held to 4 blocks up to 64-QAM as well (64 registers, no spills:
+// 64-QAM 67.9 -> 63.9 us against 3 blocks at 77 registers), to 2 for
+// 256-QAM.
 template <int KA, int METHOD, bool PAIRS>
-__global__ void __launch_bounds__(kThreads, METHOD == 0 ? 4 : (METHOD == 2 && KA <= 4 ? 2 : 1)) llr_kernel(const float2* __restrict__ x, uint32_t n,
+__global__ void __launch_bounds__(kThreads, METHOD == 0 || (METHOD == 2 && KA <= 3) ? 4 : (METHOD == 2 && KA == 4 ? 2 : 1)) llr_kernel(const float2* __restrict__ x, uint32_t n,
                                                        const typename AxisArg<METHOD>::type re,
                                                        const typename AxisArg<METHOD>::type im,
                                                        const NoiseScale noise,
