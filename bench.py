@@ -1010,8 +1010,11 @@ def measure_served(args, dist: Dist) -> dict:
                                                                 if r.code == c], 99))
                                         for c in "ABC" if any(r.code == c for r in done)},
             }  # fmt: skip
+    feed = {policy: measure_feed(codes, pool, sat_rate, duration, info_bits, dev, policy)
+            for policy in ("oldest", "shortest")}
     return {
         "workload": WORKLOADS["served"]["desc"],
+        "feed": feed,
         "saturation": {"gbps": info_bits(backlog) / sat_s / 1e9, "requests_per_s": sat_rate,
                        "requests": len(backlog), "frames": int(sum(r.frames for r in backlog)),
                        "method": "overload at 3x a backlog estimate for 0.5 s, completed / wall until drained"},
@@ -1020,6 +1023,45 @@ def measure_served(args, dist: Dist) -> dict:
                    "spread_long": server.spread_long},
         "pool_build_s": t_build, "clocks": clk.summary(),
     }  # fmt: skip
+
+
+def _latency_summary(done, wall: float, info_bits) -> dict:
+    lat = np.array([r.latency for r in done]) * 1e3
+    return {"requests": len(done), "frames": int(sum(r.frames for r in done)),
+            "gbps": info_bits(done) / wall / 1e9, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()),
+            "p99_ms_by_code": {c: float(np.percentile([r.latency * 1e3 for r in done if r.code == c], 99))
+                               for c in "ABC" if any(r.code == c for r in done)}}  # fmt: skip
+
+
+def measure_feed(codes, pool, sat_rate: float, duration: float, info_bits, dev, policy: str) -> dict:
+    """Config 5 through the continuous feed (``serving.FeedServer``): the
+    same request streams (the same seeds and rates, as fractions of the
+    batched server's saturation) published into one running decoder, whose
+    blocks take the oldest queue first or the shortest code's first."""
+    import commkit_gb300 as ck
+    from commkit_gb300.serving import FeedServer, poisson_requests
+
+    server = FeedServer(codes, ck.MinSum(max_iterations=WORKLOADS["served"]["max_it"]), device=dev,
+                        output_arena_bytes=2 << 30, idle_us=20000, policy=policy)  # fmt: skip
+    server.serve(poisson_requests(1e5, 0.002, pool, seed=1))  # warm-up (compiles and loads the kernel)
+    over = poisson_requests(3.0 * sat_rate, 0.5, pool, seed=3)
+    t0 = time.perf_counter()
+    done = server.serve(over)
+    sat_s = time.perf_counter() - t0
+    sweep = {}
+    with Clocks(dev.index) as clk:
+        for load in (0.1, 0.3, 0.5, 0.7, 0.9):
+            reqs = poisson_requests(load * sat_rate, duration, pool, seed=int(load * 100))
+            t0 = time.perf_counter()
+            got = server.serve(reqs)
+            sweep[f"{int(round(load * 100))}%"] = _latency_summary(got, time.perf_counter() - t0, info_bits)
+    launches = server.launches
+    server.close()
+    return {"what": "one persistent decoder fed from pinned descriptor rings (ck_ldpc_feed_launch); loads are "
+                    "fractions of the batched server's saturation",
+            "saturation_gbps": info_bits(done) / sat_s / 1e9, "latency_vs_load": sweep,
+            "p99_ms_at_70pct": sweep["70%"]["p99_ms"], "launches": launches, "clocks": clk.summary()}  # fmt: skip
 
 
 def main() -> None:

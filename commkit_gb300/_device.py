@@ -206,7 +206,10 @@ class on_device:
 
     def __enter__(self):
         t = _torch()
-        cur = t.cuda.current_device()
+        # torch's own getter without the Python wrapper's lazy-init checks
+        # (a CUDA tensor exists, so CUDA is initialised).
+        get = getattr(t._C, "_cuda_getDevice", None)
+        cur = get() if get is not None else t.cuda.current_device()
         if cur != self.dev:
             self.prev = cur
             t.cuda.set_device(self.dev)

@@ -32,6 +32,8 @@ CK_LDPC_SPECIALISE_AUTO = 0
 CK_LDPC_SPECIALISE_OFF = 1
 CK_LDPC_SPECIALISE_ON = 2
 CK_LDPC_MAX_MIXED = 12
+CK_LDPC_FEED_OLDEST = 0
+CK_LDPC_FEED_SHORTEST = 1
 CK_LDPC_STATIC_SCRATCH_BYTES = 64 * 1024 * 1024
 
 # Every symbol the header declares; tests check the library exports them.
@@ -69,6 +71,11 @@ EXPORTS = (
     "ck_ldpc_decode_static",
     "ck_ldpc_mixed_workspace_size",
     "ck_ldpc_decode_mixed",
+    "ck_host_publish",
+    "ck_ldpc_feed_workspace_size",
+    "ck_ldpc_feed_reset",
+    "ck_ldpc_feed_launch",
+    "ck_ldpc_feed_publish",
 )
 
 
@@ -128,6 +135,30 @@ class Batch(ctypes.Structure):
         ("axis_im", ctypes.POINTER(AxisMaxlog)),
         ("frames_per_block", ctypes.c_int32),
         ("threads_per_frame", ctypes.c_int32),
+    ]
+
+
+class FeedFrame(ctypes.Structure):
+    """ck_ldpc_feed_frame: one frame of a continuous feed."""
+
+    _fields_ = [
+        ("symbols", ctypes.c_void_p),
+        ("llr_out", ctypes.c_void_p),
+        ("bits", ctypes.c_void_p),
+        ("iters", ctypes.c_void_p),
+        ("valid", ctypes.c_void_p),
+        ("inv_s2", ctypes.c_float),
+        ("seq", ctypes.c_uint32),
+    ]
+
+
+class FeedRing(ctypes.Structure):
+    """ck_ldpc_feed_ring: a feed queue's descriptors and published count."""
+
+    _fields_ = [
+        ("frames", ctypes.c_void_p),
+        ("published", ctypes.c_void_p),
+        ("capacity", ctypes.c_uint32),
     ]
 
 
@@ -192,6 +223,13 @@ def _declare(lib: ctypes.CDLL) -> None:
         "ck_ldpc_decode_mixed": ([ctypes.POINTER(Batch), i32, p, ctypes.c_size_t, p], ctypes.c_int),
         "ck_ldpc_decode_static": (
             [p, p, p, i64, i32, i32, f32, f32, i32, i32, p, p, p, i32, p], ctypes.c_int),
+        "ck_host_publish": ([p, ctypes.c_uint32], None),
+        "ck_ldpc_feed_workspace_size": ([ctypes.POINTER(Batch), i32, size_p], ctypes.c_int),
+        "ck_ldpc_feed_reset": ([p, p], ctypes.c_int),
+        "ck_ldpc_feed_launch": ([ctypes.POINTER(Batch), ctypes.POINTER(FeedRing), i32, p, ctypes.c_uint32, i32, p,
+                                 ctypes.c_size_t, p], ctypes.c_int),
+        "ck_ldpc_feed_publish": ([p, ctypes.c_uint32, p, p, ctypes.c_uint32, i32, p, i64, p, i32, p, i32, p, f32,
+                                  ctypes.c_uint32], ctypes.c_int),
     }  # fmt: skip
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)

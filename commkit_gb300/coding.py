@@ -487,12 +487,20 @@ def _resolve_method(method: Any) -> MinSum | SumProduct:
     return method
 
 
-def _rule_args(method: MinSum | SumProduct) -> tuple[int, np.float32, np.float32]:
+def _rule_args(method: MinSum | SumProduct) -> tuple[int, float, float]:
     """(rule, scale, offset) of the C ABI; sum-product has neither parameter
-    (``commkit/coding/ldpc.py:547-549`` passes 1 and 0)."""
-    if isinstance(method, SumProduct):
-        return _lib.CK_LDPC_SUM_PRODUCT, np.float32(1.0), np.float32(0.0)
-    return _lib.CK_LDPC_MIN_SUM, np.float32(method.scale), np.float32(method.offset)
+    (``commkit/coding/ldpc.py:547-549`` passes 1 and 0).  The parameters are
+    rounded to float32 and kept as Python floats, which the C call takes as
+    the same float32 values (ctypes converts a NumPy scalar several
+    microseconds slower); remembered on the (frozen) method object."""
+    args = method.__dict__.get("_c_args")
+    if args is None:
+        if isinstance(method, SumProduct):
+            args = (_lib.CK_LDPC_SUM_PRODUCT, 1.0, 0.0)
+        else:
+            args = (_lib.CK_LDPC_MIN_SUM, float(np.float32(method.scale)), float(np.float32(method.offset)))
+        method.__dict__["_c_args"] = args
+    return args
 
 
 def _as_llrs(llrs: Any, x: _device.DeviceArray):
@@ -618,12 +626,13 @@ def _decode_torch(llrs: Any, x0: _device.DeviceArray, code: LDPCCode, method: Mi
     nb = last // n
     C = 1 if len(shape) == 1 else shape[0]
     rows = C * nb
-    dev = llrs.device
     lead = () if len(shape) == 1 else (C,)
-    out_llrs = torch.empty(lead + (nb * n,), dtype=torch.float32, device=dev)
-    bits = torch.empty(lead + (nb * k,), dtype=torch.int8, device=dev)
-    iters = torch.empty(lead + (nb,), dtype=torch.int32, device=dev)
-    valid = torch.empty(lead + (nb,), dtype=torch.bool, device=dev)
+    # empty_like / new_empty: the input's device and layout without parsing
+    # a device argument (the allocations are most of this call's host time).
+    out_llrs = torch.empty_like(llrs)
+    bits = llrs.new_empty(lead + (nb * k,), dtype=torch.int8)
+    iters = llrs.new_empty(lead + (nb,), dtype=torch.int32)
+    valid = llrs.new_empty(lead + (nb,), dtype=torch.bool)
     if rows:
         with _device.on_device(x0):
             plan = code._plan(x0.device)
@@ -806,8 +815,7 @@ def decode_mixed(batches, *, workspace: Any = None, outputs: list | None = None)
             for i, (x, xd, code, method, B, out, bits, iters, valid) in enumerate(items):
                 plan = code._plan(xd.device)
                 arr[i] = _lib.Batch(plan.handle, xd.ptr, _device.wrap(out).ptr, B, code.n,
-                                    _lib.CK_LDPC_MIN_SUM, np.float32(method.scale),
-                                    np.float32(method.offset), int(method.max_iterations),
+                                    *_rule_args(method), int(method.max_iterations),
                                     1 if method.early_stop else 0, _device.wrap(iters).ptr,
                                     _device.wrap(valid).ptr, _device.wrap(bits).ptr, code.k)  # fmt: skip
             lib = _lib.lib()

@@ -37,6 +37,7 @@
 // change a bit; rows of one layer share no variable, and layers run in the
 // schedule's order, as in the reference.
 #include <math_constants.h>
+#include <stddef.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -647,7 +648,10 @@ int mixed_occupancy(const void* kernel, int dev, int threads, uint32_t smem, int
     return CK_OK;
 }
 
-int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
+// feed: the queues of a continuous feed (ck_ldpc_feed_launch): every queue
+// may run (its frames come later), the grid is every resident block, and
+// the per-frame arrays come from the rings instead.
+int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R, bool feed = false) {
     if (!batches || n < 1 || n > kMaxMixed)
         return ck::fail(CK_ERR_INVALID_ARGUMENT, "1 to %d batches per mixed launch, got %d", kMaxMixed, n);
     int dev = -1;
@@ -678,13 +682,16 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
         if (b.frames_per_block < 0) return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: bad frames_per_block", c);
         if (b.bits && (b.k_bits < 0 || b.k_bits > b.n_in))
             return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: bad k_bits", c);
-        if (b.B > 0 && ((!b.llr_in && !b.symbols) || !b.llr_out || !b.iters || !b.valid))
+        if (!feed && b.B > 0 && ((!b.llr_in && !b.symbols) || !b.llr_out || !b.iters || !b.valid))
             return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: missing arrays", c);
+        if (feed && !b.symbols)
+            return ck::fail(CK_ERR_INVALID_ARGUMENT, "queue %d: a feed demaps in the decoder (symbols must be set)",
+                            c);
         int32_t ka = 0;
         if (b.symbols) {
             // Fused demapping: closed-form max-log tables of a square
             // separable constellation, 1 to 4 bits per axis.
-            if (!b.inv_s2 || !b.axis_re || !b.axis_im)
+            if ((!feed && !b.inv_s2) || !b.axis_re || !b.axis_im)
                 return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: symbols need inv_s2 and both axes", c);
             ka = b.axis_re->k;
             if (ka < 1 || ka > 4 || b.axis_im->k != ka || b.axis_re->L != (1 << ka) || b.axis_im->L != (1 << ka))
@@ -693,7 +700,7 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
             if (b.n_in % (2 * ka))
                 return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: n_in %d is not a multiple of %d bits per "
                                 "symbol", c, b.n_in, 2 * ka);
-            if (reinterpret_cast<uintptr_t>(b.symbols) % 8)
+            if (!feed && reinterpret_cast<uintptr_t>(b.symbols) % 8)
                 return ck::fail(CK_ERR_INVALID_ARGUMENT, "batch %d: symbols must be 8-byte aligned", c);
             const ck_axis_maxlog* ax[2] = {b.axis_re, b.axis_im};
             for (int a = 0; a < 2; ++a)
@@ -714,8 +721,10 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
         const uint32_t code_tables = align_up(static_cast<uint32_t>(plan->L + 1 + plan->mb + 1) * 4, 8) +
                                      static_cast<uint32_t>(plan->nnzb) * 8;
         const uint32_t axes_off = align_up(code_tables, 16);
-        const uint32_t tables =
-            align_up(ka ? axes_off + static_cast<uint32_t>(sizeof(ck::ldpc::MixedAxes<4>)) : code_tables, 128);
+        // Then one word of the block's frame bookkeeping (busy_off).
+        const uint32_t busy_off =
+            align_up(ka ? axes_off + static_cast<uint32_t>(sizeof(ck::ldpc::MixedAxes<4>)) : code_tables, 4);
+        const uint32_t tables = align_up(busy_off + 4, 128);
         const uint32_t ctrl = 128;
         const uint32_t gblk = align_up(static_cast<uint32_t>(plan->nnzb) * 8, 128);
         const uint32_t app = align_up(static_cast<uint32_t>(plan->N) * 4, 128);
@@ -779,6 +788,7 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
         K.sign_words = sign_words;
         K.ka = ka;
         K.axes_off = axes_off;
+        K.busy_off = busy_off;
         if (ka) {
             K.sym = static_cast<const float2*>(b.symbols);
             K.inv_s2 = b.inv_s2;
@@ -819,7 +829,8 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
     int64_t need = 0;
     for (int c = 0; c < n; ++c)
         need += (R->p.code[c].B + R->p.code[c].G - 1) / R->p.code[c].G;
-    R->grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(need, int64_t(sms) * per_sm)));
+    R->grid = feed ? sms * per_sm
+                   : static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(need, int64_t(sms) * per_sm)));
     // Starting split of the blocks in proportion to each code's work
     // (frames x edges x iteration budget), at least one block per code with frames.
     double total = 0.0, work[kMaxMixed] = {};
@@ -841,7 +852,7 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R) {
     // sized for the largest (G groups x 3 r_stride words), in 256-byte units.
     uint32_t block_words = 0;
     for (int c = 0; c < n; ++c)
-        if (!R->p.code[c].r_smem && R->p.code[c].B > 0)  // a code without frames never runs
+        if (!R->p.code[c].r_smem && (feed || R->p.code[c].B > 0))  // a code without frames never runs
             block_words = std::max<uint32_t>(block_words, static_cast<uint32_t>(R->p.code[c].G) *
                                                               static_cast<uint32_t>(3 + R->p.code[c].sign_words) *
                                                               R->p.code[c].r_stride);
@@ -901,6 +912,73 @@ extern "C" int ck_ldpc_decode_mixed(const ck_ldpc_batch* batches, int32_t num_ba
         if (status == CK_OK) status = st;
     }
     return status;
+}
+
+static_assert(sizeof(ck_ldpc_feed_frame) == sizeof(ck::ldpc::FeedFrame), "feed frame layout");
+static_assert(offsetof(ck_ldpc_feed_frame, inv_s2) == offsetof(ck::ldpc::FeedFrame, inv_s2), "feed frame layout");
+static_assert(offsetof(ck_ldpc_feed_frame, seq) == offsetof(ck::ldpc::FeedFrame, seq), "feed frame layout");
+
+extern "C" int ck_ldpc_feed_workspace_size(const ck_ldpc_batch* queues, int32_t num_queues, size_t* bytes) {
+    ck::clear_error();
+    if (!bytes) return ck::fail(CK_ERR_INVALID_ARGUMENT, "bytes is NULL");
+    MixedResolved R;
+    CK_TRY(resolve_mixed(queues, num_queues, &R, true));
+    *bytes = R.ws_bytes;
+    return CK_OK;
+}
+
+extern "C" int ck_ldpc_feed_reset(void* workspace, void* stream) {
+    ck::clear_error();
+    if (!workspace) return ck::fail(CK_ERR_INVALID_ARGUMENT, "workspace is NULL");
+    return ck::cuda_check(cudaMemsetAsync(workspace, 0, kHeaderBytes, static_cast<cudaStream_t>(stream)),
+                          "cudaMemsetAsync");
+}
+
+extern "C" int ck_ldpc_feed_launch(const ck_ldpc_batch* queues, const ck_ldpc_feed_ring* rings,
+                                   int32_t num_queues, const uint32_t* stop, uint32_t idle_us, int32_t policy,
+                                   void* workspace, size_t workspace_bytes, void* stream) {
+    ck::clear_error();
+    if (!rings) return ck::fail(CK_ERR_INVALID_ARGUMENT, "rings is NULL");
+    if (policy != CK_LDPC_FEED_OLDEST && policy != CK_LDPC_FEED_SHORTEST)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "unknown feed policy %d", policy);
+    if (idle_us < 1 || idle_us > 1000000)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "idle_us must be in [1, 1000000], got %u", idle_us);
+    MixedResolved R;
+    CK_TRY(resolve_mixed(queues, num_queues, &R, true));
+    for (int c = 0; c < num_queues; ++c) {
+        const ck_ldpc_feed_ring& q = rings[c];
+        if (!q.frames || !q.published)
+            return ck::fail(CK_ERR_INVALID_ARGUMENT, "queue %d: ring frames and published count are required", c);
+        if (q.capacity < 1 || q.capacity > (1u << 30) || (q.capacity & (q.capacity - 1)))
+            return ck::fail(CK_ERR_INVALID_ARGUMENT, "queue %d: ring capacity %u is not a power of two in [1, 2^30]",
+                            c, q.capacity);
+    }
+    if (!workspace) return ck::fail(CK_ERR_INVALID_ARGUMENT, "a feed needs its workspace (its counts persist)");
+    if (workspace_bytes < R.ws_bytes)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "workspace of %zu bytes, %zu needed", workspace_bytes, R.ws_bytes);
+    if (reinterpret_cast<uintptr_t>(workspace) % 256)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
+    unsigned char* wsb = static_cast<unsigned char*>(workspace);
+    for (int c = 0; c < num_queues; ++c) {
+        MixedCode& K = R.p.code[c];
+        K.counter = reinterpret_cast<uint32_t*>(wsb + 4 * c);
+        K.g_r = reinterpret_cast<uint32_t*>(wsb + kHeaderBytes);
+        K.ring = reinterpret_cast<const ck::ldpc::FeedFrame*>(rings[c].frames);
+        K.published = rings[c].published;
+        K.ring_mask = rings[c].capacity - 1u;
+        K.B = 0;
+        K.order = nullptr;
+    }
+    R.p.feed = 1;
+    R.p.feed_policy = policy;
+    R.p.stop = stop;
+    R.p.idle_ns = static_cast<uint64_t>(idle_us) * 1000ull;
+    R.p.idle_polls = idle_us;  // each poll sleeps up to 2 us: a second bound on the wait
+    void* args[] = {&R.p};
+    return ck::cuda_check(cudaLaunchKernel(R.kernel, dim3(static_cast<unsigned>(R.grid)),
+                                           dim3(static_cast<unsigned>(R.block_threads)), args, R.smem,
+                                           static_cast<cudaStream_t>(stream)),
+                          "feed decoder launch");
 }
 
 namespace {

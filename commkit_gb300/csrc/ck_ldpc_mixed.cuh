@@ -22,6 +22,20 @@ namespace ldpc {
 constexpr int kMaxMixed = 12;  // CK_LDPC_MAX_MIXED
 constexpr int kMixedThreads = 768;
 
+// One frame of a continuous feed (the C ABI's ck_ldpc_feed_frame): where
+// its symbols are, where its results go, and its place in the order of
+// publication across queues.
+struct FeedFrame {
+    const float2* sym;
+    float* llr_out;
+    int8_t* bits;
+    int32_t* iters;
+    uint8_t* valid;
+    float inv_s2;
+    uint32_t seq;
+};
+constexpr uint32_t kFeedNone = 0xffffffffu;
+
 struct MixedCode {
     const int32_t* layer;
     const int32_t* eptr;
@@ -65,6 +79,18 @@ struct MixedCode {
     const int32_t* ax_pos[2];
     int32_t ka;
     uint32_t axes_off;
+    // Continuous feed (ring != null; fused demapping only): the frames come
+    // from a ring of ring_mask + 1 descriptors that the host fills while the
+    // kernel runs.  Positions [0, *published) are valid (the host publishes
+    // with a release store), position q at ring[q & ring_mask]; counter
+    // counts the positions taken, across launches.
+    const FeedFrame* ring;
+    const uint32_t* published;
+    uint32_t ring_mask;
+    // A word in the block's table region: how many of the block's groups
+    // hold a frame of this code (a feed's groups keep looking for frames of
+    // their queue while others of the block still work).
+    uint32_t busy_off;
 };
 
 // The fused demapper's two axis tables, as laid out at MixedCode::axes_off.
@@ -89,14 +115,12 @@ __device__ __forceinline__ void mixed_load_axes(const MixedCode& K, unsigned cha
 // the demapper kernels, so the same bits.
 template <int KA>
 __device__ __forceinline__ void mixed_demap_frame(const MixedCode& K, const unsigned char* smem, float* a,
-                                                  uint32_t f, int tid) {
+                                                  const float2* x, float s2, int tid) {
     constexpr int KB = 2 * KA;
     constexpr int kAhead = 4;  // symbol loads in flight per thread
     const MixedAxes<KA>* t = reinterpret_cast<const MixedAxes<KA>*>(smem + K.axes_off);
     const uint32_t S = static_cast<uint32_t>(K.n_in) / KB;
     const uint32_t T = static_cast<uint32_t>(K.T);
-    const float2* x = K.sym + static_cast<size_t>(f) * S;
-    const float s2 = K.inv_s2[f];
     // The thread's symbols tid, tid + T, ... come through a ring of kAhead
     // registers: the loads of the next ones are in flight while one is
     // demapped (the symbols may sit in host memory, microseconds away).
@@ -128,7 +152,90 @@ struct MixedParams {
     MixedCode code[kMaxMixed];
     int32_t num_codes;
     int32_t start_block[kMaxMixed + 1];  // blocks [start_block[c], start_block[c+1]) begin on c
+    // Continuous feed (feed != 0): a block with no published frame to take
+    // polls for one, and returns once none has appeared for idle_ns (or
+    // after idle_polls polls, whichever comes first) or once *stop (host
+    // memory) is non-zero.
+    int32_t feed;
+    uint32_t idle_polls;
+    uint64_t idle_ns;
+    const uint32_t* stop;
+    // Which queue a feed block takes next: 0 the one whose oldest untaken
+    // frame was published first; 1 the one with the fewest edges per frame
+    // (the shortest frames), the oldest first among equals.
+    int32_t feed_policy;
 };
+
+// Takes the next published position of feed queue K for one frame group,
+// or returns kFeedNone when every published position is taken (a bounded
+// number of tries against other groups taking the same position).
+__device__ __forceinline__ uint32_t feed_claim(const MixedCode& K) {
+    // One read of the published count (host memory, a round trip over the
+    // link); a count that has grown since only makes this group look again
+    // later.  A failed compare-and-swap returns the count that won.
+    const uint32_t avail = ck::ld_acquire_sys(K.published);
+    uint32_t taken = *reinterpret_cast<volatile uint32_t*>(K.counter);
+    for (int tries = 0; tries < 64; ++tries) {
+        if (static_cast<int32_t>(avail - taken) <= 0) return kFeedNone;
+        const uint32_t won = atomicCAS(K.counter, taken, taken + 1u);
+        if (won == taken) return taken;
+        taken = won;
+    }
+    return kFeedNone;
+}
+
+// The feed queue whose oldest untaken frame was published first, or -1
+// when no queue has one.  Every queue's counts are read before any is
+// compared, so the host-memory loads overlap (two round trips in all).
+__device__ inline int feed_pick(const MixedParams& p) {
+    uint32_t taken[kMaxMixed], avail[kMaxMixed], seq[kMaxMixed];
+#pragma unroll
+    for (int c = 0; c < kMaxMixed; ++c) {
+        if (c < p.num_codes) {
+            taken[c] = *reinterpret_cast<volatile uint32_t*>(p.code[c].counter);
+            avail[c] = ck::ld_acquire_sys(p.code[c].published);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < kMaxMixed; ++c) {
+        seq[c] = 0u;
+        if (c < p.num_codes && static_cast<int32_t>(avail[c] - taken[c]) > 0)
+            seq[c] = ck::ld_relaxed_sys(&p.code[c].ring[taken[c] & p.code[c].ring_mask].seq);
+    }
+    int best = -1;
+    uint32_t first = 0;
+    float light = 0.0f;
+#pragma unroll
+    for (int c = 0; c < kMaxMixed; ++c) {
+        if (c >= p.num_codes || static_cast<int32_t>(avail[c] - taken[c]) <= 0) continue;
+        const float w = p.code[c].weight;
+        const bool older = static_cast<int32_t>(seq[c] - first) < 0;
+        const bool better = p.feed_policy == 1 ? (w < light || (w == light && older)) : older;
+        if (best < 0 || better) {
+            best = c;
+            first = seq[c];
+            light = w;
+        }
+    }
+    return best;
+}
+
+// feed_pick, polling while nothing is published (sleeping 1 us between
+// polls at first, doubling up to 32 us, so idle blocks do not flood the
+// link): -1 once the idle time or poll budget is spent, or the host has
+// set *stop.
+__device__ inline int feed_wait_pick(const MixedParams& p) {
+    const uint64_t t0 = ck::globaltimer_ns();
+    uint32_t nap = 1000;
+    for (uint32_t poll = 0;; ++poll) {
+        const int c = feed_pick(p);
+        if (c >= 0) return c;
+        if (p.stop && ck::ld_relaxed_sys(p.stop) != 0u) return -1;
+        if (poll >= p.idle_polls || ck::globaltimer_ns() - t0 >= p.idle_ns) return -1;
+        __nanosleep(nap);
+        nap = nap < 32000 ? 2 * nap : nap;
+    }
+}
 
 // The code this block should work on next: `prefer` while its queue has
 // frames, else the one with the most edges left; -1 when all are drained.
@@ -201,18 +308,75 @@ __device__ __forceinline__ void mixed_frames(const MixedCode& K, unsigned char* 
         return syndrome_table();
     };
 
+    // With a feed, thread 0 copies the descriptor of the group's frame into
+    // the group's control block, where the other threads read it.
+    FeedFrame* s_io = reinterpret_cast<FeedFrame*>(gbase + 16);
     for (;;) {
-        if (tid == 0) *s_frame = atomicAdd(K.counter, 1u);
+        if (tid == 0) {
+            uint32_t pos;
+            if (K.ring) {
+                pos = feed_claim(K);
+                // While other groups of the block still decode (the block
+                // changes queue only once all its groups are free), keep
+                // looking for this queue's frames instead of idling; bounded
+                // by their frames' decoding and by the wait limit.
+                volatile int32_t* busy = reinterpret_cast<volatile int32_t*>(smem + K.busy_off);
+                uint32_t nap = 1000;
+                for (uint32_t poll = 0; pos == kFeedNone && *busy > 0 && poll < ck::kWaitLimit; ++poll) {
+                    __nanosleep(nap);
+                    nap = nap < 8000 ? 2 * nap : nap;
+                    pos = feed_claim(K);
+                }
+                if (pos != kFeedNone) {
+                    atomicAdd(const_cast<int32_t*>(busy), 1);
+                    // Written by the host before it published the position
+                    // (feed_claim's acquire orders these loads after it).
+                    const FeedFrame* d = K.ring + (pos & K.ring_mask);
+                    s_io->sym = reinterpret_cast<const float2*>(ck::ld_relaxed_sys_u64(&d->sym));
+                    s_io->llr_out = reinterpret_cast<float*>(ck::ld_relaxed_sys_u64(&d->llr_out));
+                    s_io->bits = reinterpret_cast<int8_t*>(ck::ld_relaxed_sys_u64(&d->bits));
+                    s_io->iters = reinterpret_cast<int32_t*>(ck::ld_relaxed_sys_u64(&d->iters));
+                    s_io->valid = reinterpret_cast<uint8_t*>(ck::ld_relaxed_sys_u64(&d->valid));
+                    s_io->inv_s2 = __uint_as_float(ck::ld_relaxed_sys(reinterpret_cast<const uint32_t*>(&d->inv_s2)));
+                }
+            } else {
+                pos = atomicAdd(K.counter, 1u);
+            }
+            *s_frame = pos;
+        }
         group_sync(bar, K.T);
         const uint32_t pos = *s_frame;
-        if (pos >= K.B) break;
-        const uint32_t f = K.order ? static_cast<uint32_t>(__ldg(K.order + pos)) : pos;
+        if (K.ring ? pos == kFeedNone : pos >= K.B) break;
+        // This frame's symbols, noise scale and result locations.
+        const float2* f_sym;
+        float f_s2;
+        float* f_llr;
+        int8_t* f_bits;
+        int32_t* f_iters;
+        uint8_t* f_valid;
+        uint32_t f = 0;
+        if (K.ring) {
+            f_sym = s_io->sym;
+            f_s2 = s_io->inv_s2;
+            f_llr = s_io->llr_out;
+            f_bits = K.k_bits > 0 ? s_io->bits : nullptr;
+            f_iters = s_io->iters;
+            f_valid = s_io->valid;
+        } else {
+            f = K.order ? static_cast<uint32_t>(__ldg(K.order + pos)) : pos;
+            f_sym = K.sym ? K.sym + static_cast<size_t>(f) * static_cast<uint32_t>(K.n_in / (2 * K.ka)) : nullptr;
+            f_s2 = K.sym ? K.inv_s2[f] : 0.0f;
+            f_llr = K.llr_out + static_cast<size_t>(f) * K.n_in;
+            f_bits = K.bits ? K.bits + static_cast<size_t>(f) * K.k_bits : nullptr;
+            f_iters = K.iters + f;
+            f_valid = K.valid + f;
+        }
         if (K.sym) {
             switch (K.ka) {
-                case 1: mixed_demap_frame<1>(K, smem, a, f, tid); break;
-                case 2: mixed_demap_frame<2>(K, smem, a, f, tid); break;
-                case 3: mixed_demap_frame<3>(K, smem, a, f, tid); break;
-                default: mixed_demap_frame<4>(K, smem, a, f, tid); break;
+                case 1: mixed_demap_frame<1>(K, smem, a, f_sym, f_s2, tid); break;
+                case 2: mixed_demap_frame<2>(K, smem, a, f_sym, f_s2, tid); break;
+                case 3: mixed_demap_frame<3>(K, smem, a, f_sym, f_s2, tid); break;
+                default: mixed_demap_frame<4>(K, smem, a, f_sym, f_s2, tid); break;
             }
         } else {
             const float* src = K.llr_in + static_cast<size_t>(f) * K.n_in;
@@ -254,21 +418,19 @@ __device__ __forceinline__ void mixed_frames(const MixedCode& K, unsigned char* 
             }
             ++it;
         }
-        float* dst = K.llr_out + static_cast<size_t>(f) * K.n_in;
-        for (int i = tid; i < K.n_in; i += K.T) __stcs(dst + i, a[i]);
-        if (K.bits) {
-            int8_t* bdst = K.bits + static_cast<size_t>(f) * K.k_bits;
-            for (int i = tid; i < K.k_bits; i += K.T) bdst[i] = a[i] < 0.0f ? 1 : 0;
-        }
+        for (int i = tid; i < K.n_in; i += K.T) __stcs(f_llr + i, a[i]);
+        if (f_bits)
+            for (int i = tid; i < K.k_bits; i += K.T) f_bits[i] = a[i] < 0.0f ? 1 : 0;
         // The iteration count is written last, after a system-scope fence
         // that follows the group's writes: a host that reads it from mapped
         // memory (the request server polls frames as they finish) then also
         // sees the frame's LLRs, bits and flag.
         group_sync(bar, K.T);
         if (tid == 0) {
-            K.valid[f] = ok ? 1 : 0;
+            *f_valid = ok ? 1 : 0;
             __threadfence_system();
-            K.iters[f] = it;
+            *reinterpret_cast<volatile int32_t*>(f_iters) = it;
+            if (K.ring) atomicSub(reinterpret_cast<int32_t*>(smem + K.busy_off), 1);
         }
         group_sync(bar, K.T);
     }
@@ -300,9 +462,13 @@ __device__ __forceinline__ void mixed_body(const MixedParams& p) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int s_code;
     if (threadIdx.x == 0) {
-        int c = 0;
-        while (c + 1 < p.num_codes && static_cast<int32_t>(blockIdx.x) >= p.start_block[c + 1]) ++c;
-        s_code = mixed_pick(p, c);
+        if (p.feed) {
+            s_code = feed_wait_pick(p);
+        } else {
+            int c = 0;
+            while (c + 1 < p.num_codes && static_cast<int32_t>(blockIdx.x) >= p.start_block[c + 1]) ++c;
+            s_code = mixed_pick(p, c);
+        }
     }
     __syncthreads();
     for (;;) {
@@ -316,6 +482,7 @@ __device__ __forceinline__ void mixed_body(const MixedParams& p) {
         for (int i = threadIdx.x; i <= K.L; i += blockDim.x) s_layer[i] = K.layer[i];
         for (int i = threadIdx.x; i <= K.mb; i += blockDim.x) s_eptr[i] = K.eptr[i];
         for (int i = threadIdx.x; i < K.nnzb; i += blockDim.x) s_blk[i] = K.blk[i];
+        if (threadIdx.x == 0) *reinterpret_cast<int32_t*>(smem + K.busy_off) = 0;
         if (K.sym) {
             switch (K.ka) {
                 case 1: mixed_load_axes<1>(K, smem); break;
@@ -331,7 +498,7 @@ __device__ __forceinline__ void mixed_body(const MixedParams& p) {
             Dispatch::template run<DMAX>(c, K, smem, s_layer, s_eptr, s_blk, g, tid);
         }
         __syncthreads();
-        if (threadIdx.x == 0) s_code = mixed_pick(p, -1);
+        if (threadIdx.x == 0) s_code = p.feed ? feed_wait_pick(p) : mixed_pick(p, -1);
         __syncthreads();
     }
 }

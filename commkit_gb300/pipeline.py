@@ -38,7 +38,7 @@ from typing import Any
 import numpy as np
 
 from . import _device, _lib
-from .coding import DecodeResult, LDPCCode, MinSum, _require_leading_info, decode_mixed
+from .coding import DecodeResult, LDPCCode, MinSum, _require_leading_info, _rule_args, decode_mixed
 from .mapping import Constellation, _axis_struct, _table_kind, compute_llr_frames, device_tables, inv_s2_frames
 
 
@@ -118,7 +118,7 @@ class MixedReceiver:
             plan = s.code._plan(self.device.index)
             out = self.outputs[i]
             arr[i] = _lib.Batch(plan.handle, self.llr[i].data_ptr(), out[0].data_ptr(), s.frames, s.code.n,
-                                _lib.CK_LDPC_MIN_SUM, np.float32(s.method.scale), np.float32(s.method.offset),
+                                *_rule_args(s.method),
                                 int(s.method.max_iterations), 1 if s.method.early_stop else 0,
                                 out[2].data_ptr(), out[3].data_ptr(), out[1].data_ptr(), s.code.k,
                                 self.order[i].data_ptr())  # fmt: skip

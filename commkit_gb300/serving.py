@@ -43,7 +43,7 @@ from typing import Any
 import numpy as np
 
 from . import _lib
-from .coding import LDPCCode, MinSum, _require_leading_info
+from .coding import LDPCCode, MinSum, _require_leading_info, _rule_args
 from .mapping import Constellation
 
 # Largest piece of one request's symbols a gather block copies (so one big
@@ -272,13 +272,7 @@ class Server:
         return 4 * code.n + code.k + 4 + 1
 
     def _axis_structs(self, order: int):
-        from . import _device
-        from .mapping import _axis_struct, device_tables
-
-        like = _device.wrap(self.torch.empty(1, device=self.device))
-        tabs = device_tables(Constellation.qam(order), "maxlog", like)
-        half = len(tabs) // 2
-        return (_axis_struct(tabs[:half], "maxlog"), _axis_struct(tabs[half:], "maxlog"), tabs)
+        return _axis_structs(self.torch, self.device, order)
 
     def _batch_array(self, entries: list, slot: _Slot, out: dict):
         """The mixed decode's batch arguments, one per entry ``(name, order,
@@ -298,7 +292,7 @@ class Server:
                 it_o, ok_o = it_o + 4 * f_off, ok_o + f_off
             arr[i] = _lib.Batch(code._plan(self.device.index).handle,
                                 slot.llr[name].data_ptr() + 4 * f_off * code.n, llr_o, B, code.n,
-                                _lib.CK_LDPC_MIN_SUM, np.float32(m.scale), np.float32(m.offset),
+                                *_rule_args(m),
                                 int(m.max_iterations), 1 if m.early_stop else 0, it_o, ok_o, bits_o,
                                 code.k)  # fmt: skip
             if self.spread_long and name in self.long_codes:
@@ -542,6 +536,256 @@ class Server:
                         time.sleep(wait - 1e-4)
             self._poll(block=True)
         return self.completed
+
+
+# ---------------------------------------------------------------------------
+# Continuous feed
+# ---------------------------------------------------------------------------
+
+class FeedServer:
+    """Demap + decode server over a continuous feed (``ck_ldpc_feed_launch``).
+
+    Instead of a launch per admitted batch, one persistent decoder runs
+    while requests arrive: each (code, constellation) is a queue whose
+    frames the host publishes into a ring of descriptors in pinned host
+    memory (where the frame's symbols are, where its results go), and the
+    decoder's blocks take published frames as they free up, the queue whose
+    oldest untaken frame was published first before the others.  A request
+    is published whole the moment it arrives (``ck_ldpc_feed_publish``, one
+    native call); nothing is copied (the decoder reads each frame's symbols
+    from the request's pinned buffer and writes its results into a pinned
+    output ring).  Each queue's iteration counts sit in one pinned array, so
+    one vectorized test per queue finds the finished requests.  The decoder
+    returns after ``idle_us`` with nothing published; the next request
+    launches it again, and it continues where it stopped (the counts of
+    frames taken stay in its workspace).  Results are bit-identical to
+    :func:`commkit_gb300.decode` on the same LLRs.
+    """
+
+    def __init__(self, codes: dict[str, LDPCCode], method: MinSum, *, device: Any = None, orders=(4, 16, 64),
+                 ring_frames: int = 1 << 14, output_arena_bytes: int = 1 << 30, idle_us: int = 20000,
+                 policy: str = "oldest", max_inflight_frames: int = 8192):  # fmt: skip
+        import torch
+
+        self.torch = torch
+        self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        for code in codes.values():
+            _require_leading_info(code, "FeedServer")
+        if not isinstance(method, MinSum):
+            raise NotImplementedError("FeedServer decodes with MinSum")
+        if ring_frames < 1 or ring_frames & (ring_frames - 1):
+            raise ValueError(f"ring_frames must be a power of two, got {ring_frames}")
+        self.codes, self.method, self.orders = codes, method, tuple(orders)
+        self.queues = [(name, order) for name in codes for order in self.orders]
+        if len(self.queues) > _lib.CK_LDPC_MAX_MIXED:
+            raise ValueError(f"{len(self.queues)} (code, constellation) queues, at most {_lib.CK_LDPC_MAX_MIXED}")
+        self._qidx = {q: i for i, q in enumerate(self.queues)}
+        self.ring_frames = int(ring_frames)
+        self.idle_us = int(idle_us)
+        policies = {"oldest": _lib.CK_LDPC_FEED_OLDEST, "shortest": _lib.CK_LDPC_FEED_SHORTEST}
+        if policy not in policies:
+            raise ValueError(f"policy must be one of {sorted(policies)}, got {policy!r}")
+        self.policy = policy
+        self._policy = policies[policy]
+        # Frames published and not yet finished, at most (later arrivals wait
+        # on the host in arrival order): keeps the host's poll short under
+        # overload while the GPU still has every frame slot filled.
+        self.max_inflight_frames = int(max_inflight_frames)
+        nq = len(self.queues)
+        lib = _lib.lib()
+        with torch.cuda.device(self.device):
+            self._tables = {o: _axis_structs(torch, self.device, o) for o in self.orders}
+            if not all(t[0].k == t[1].k and 1 <= t[0].k <= 4 for t in self._tables.values()):
+                raise NotImplementedError("FeedServer demaps in the decoder: square QAM of 4 to 256 points")
+            self._arr = (_lib.Batch * nq)()
+            rule, scale, offset = _rule_args(method)
+            for i, (name, order) in enumerate(self.queues):
+                code = codes[name]
+                re, im, _ = self._tables[order]
+                b = self._arr[i]
+                b.plan = code._plan(self.device.index).handle
+                b.n_in, b.rule, b.scale, b.offset = code.n, rule, scale, offset
+                b.max_iterations, b.early_stop = int(method.max_iterations), 1 if method.early_stop else 0
+                b.k_bits = code.k
+                b.symbols = 1  # the frames' own symbols come from the ring
+                b.axis_re, b.axis_im = ctypes.pointer(re), ctypes.pointer(im)
+            # Pinned host memory: the descriptor rings, each queue's iteration
+            # counts by ring slot, the published counts and the stop word.
+            fb = ctypes.sizeof(_lib.FeedFrame)
+            self._ring_buf = torch.zeros(nq * self.ring_frames * fb, dtype=torch.uint8, pin_memory=True)
+            self._iters = torch.full((nq, self.ring_frames), -2, dtype=torch.int32, pin_memory=True)
+            self._iters_np = self._iters.numpy()
+            self._ctl = torch.zeros(64, dtype=torch.int32, pin_memory=True)
+            self._ctl_np = self._ctl.numpy().view(np.uint32)
+            base = self._ctl.data_ptr()
+            self._published_addr = [base + 4 * i for i in range(nq)]
+            self._stop_addr = base + 4 * 48
+            self._ring_addr = [self._ring_buf.data_ptr() + i * self.ring_frames * fb for i in range(nq)]
+            self._iters_addr = [self._iters.data_ptr() + 4 * i * self.ring_frames for i in range(nq)]
+            self._rings = (_lib.FeedRing * nq)()
+            for i in range(nq):
+                self._rings[i] = _lib.FeedRing(self._ring_addr[i], self._published_addr[i], self.ring_frames)
+            need = ctypes.c_size_t(0)
+            _lib.check(lib.ck_ldpc_feed_workspace_size(self._arr, nq, ctypes.byref(need)), "FeedServer")
+            self.ws = torch.empty(max(int(need.value), 256), dtype=torch.uint8, device=self.device)
+            self.stream = torch.cuda.Stream(self.device)
+            self.event = torch.cuda.Event()
+            _lib.check(lib.ck_ldpc_feed_reset(self.ws.data_ptr(), self.stream.cuda_stream), "FeedServer")
+        self.hbm_bytes = self.ws.numel()
+        self.arena = OutputArena(output_arena_bytes)
+        self._pos = [0] * nq  # positions published per queue
+        self._seq = 0
+        self._running = False
+        # Per queue, its requests in flight in publication order:
+        # (request, first position, arena region, (llrs, bits, valid) views).
+        self._inflight: list[list] = [[] for _ in range(nq)]
+        self._count = 0
+        self._frames = 0  # frames in flight
+        self.completed: list[Request] = []
+        self.launches = 0
+        self._t0 = 0.0
+
+    def _ensure_running(self) -> None:
+        """Launches the decoder when it is not running (it returns when idle)."""
+        if self._running and not self.event.query():
+            return
+        st = _lib.lib().ck_ldpc_feed_launch(self._arr, self._rings, len(self.queues), self._stop_addr, self.idle_us,
+                                            self._policy, self.ws.data_ptr(), self.ws.numel(),
+                                            self.stream.cuda_stream)  # fmt: skip
+        _lib.check(st, "FeedServer launch")
+        self.event.record(self.stream)
+        self._running = True
+        self.launches += 1
+
+    def _wait_region(self, lo: int, hi: int) -> None:
+        """Blocks until no request in flight has results in arena bytes [lo, hi)."""
+        while any(f[2][0] < hi and lo < f[2][1] for q in self._inflight for f in q):
+            self._ensure_running()
+            self._poll()
+
+    def _publish(self, r: Request, now: float) -> None:
+        q = self._qidx[(r.code, r.order)]
+        code = self.codes[r.code]
+        F, n, k = r.frames, code.n, code.k
+        if F > self.ring_frames:
+            raise ValueError(f"request {r.rid}: {F} frames, the ring holds {self.ring_frames}")
+        sizes = (4 * F * n, F * k, F)
+        total = sum((b + 255) // 256 * 256 for b in sizes)
+        off = self.arena.alloc(total, self._wait_region)
+        parts, o = [], off
+        for nbytes in sizes:
+            parts.append(o)
+            o += (nbytes + 255) // 256 * 256
+        a = self.arena.np
+        views = (a[parts[0] : parts[0] + sizes[0]].view(np.float32).reshape(F, n),
+                 a[parts[1] : parts[1] + sizes[1]].view(np.int8).reshape(F, k), a[parts[2] : parts[2] + F])  # fmt: skip
+        p0 = self._pos[q]
+        # A ring slot is rewritten only after the frame it held has finished.
+        while self._inflight[q] and p0 + F - self._inflight[q][0][1] > self.ring_frames:
+            self._ensure_running()
+            self._poll()
+        base = self.arena.base
+        st = _lib.lib().ck_ldpc_feed_publish(
+            self._ring_addr[q], self.ring_frames, self._iters_addr[q], self._published_addr[q], p0 & 0xFFFFFFFF, F,
+            r.symbols.data_ptr(), 8 * r.symbols.shape[1], base + parts[0], n, base + parts[1], k, base + parts[2],
+            float(np.float32(1.0 / max(r.noise_var, 1e-20))), self._seq)  # fmt: skip
+        _lib.check(st, "FeedServer publish")
+        self._seq = (self._seq + F) & 0xFFFFFFFF
+        self._pos[q] = p0 + F
+        r.admitted = now
+        self._inflight[q].append((r, p0, (off, off + total), views))
+        self._count += 1
+        self._frames += F
+
+    # Requests of a queue tested per poll, oldest first: the decoder takes a
+    # queue's frames in order, so later ones are rarely done before these.
+    _POLL_WINDOW = 64
+
+    def _poll(self) -> None:
+        """Delivers the requests whose frames have all finished: per queue,
+        one test of the iteration counts over the positions of its oldest
+        requests in flight."""
+        now = None
+        mask = self.ring_frames - 1
+        for q, every in enumerate(self._inflight):
+            if not every:
+                continue
+            items = every[: self._POLL_WINDOW]
+            lo = items[0][1]
+            hi = items[-1][1] + items[-1][0].frames
+            pos = np.arange(lo, hi) & mask
+            done = self._iters_np[q][pos] >= -1
+            starts = np.fromiter((it[1] - lo for it in items), dtype=np.int64, count=len(items))
+            whole = np.logical_and.reduceat(done, starts)
+            if not whole.any():
+                continue
+            _lib.lib().ck_host_acquire()
+            if now is None:
+                now = time.perf_counter() - self._t0
+            keep = []
+            for ok, item in zip(whole, items, strict=True):
+                if not ok:
+                    keep.append(item)
+                    continue
+                r, p, _, (llrs, bits, valid) = item
+                r.llrs, r.bits, r.valid = llrs, bits, valid.view(np.bool_)
+                r.iterations = self._iters_np[q][(p + np.arange(r.frames)) & mask].copy()
+                r.done = now
+                self.completed.append(r)
+                self._count -= 1
+                self._frames -= r.frames
+            self._inflight[q] = keep + every[self._POLL_WINDOW :]
+
+    def serve(self, requests: list[Request]) -> list[Request]:
+        """Run a request stream (arrival times in seconds from now) to completion."""
+        pending = deque(sorted(requests, key=lambda r: r.arrival))
+        for r in pending:
+            if r.order not in self.orders or r.code not in self.codes:
+                raise ValueError(f"request {r.rid}: no queue for code {r.code} on {r.order}-QAM")
+            if not r.symbols.is_contiguous():
+                r.symbols = r.symbols.contiguous()
+            if not r.symbols.is_cuda and not r.symbols.is_pinned():
+                r.symbols = r.symbols.pin_memory()  # read in place by the decoder
+        self.completed = []
+        gc_on = gc.isenabled()
+        gc.disable()
+        try:
+            self._t0 = time.perf_counter()
+            while pending or self._count:
+                now = time.perf_counter() - self._t0
+                while (pending and pending[0].arrival <= now
+                       and (self._frames == 0 or self._frames + pending[0].frames <= self.max_inflight_frames)):
+                    self._publish(pending.popleft(), now)
+                if self._count:
+                    self._ensure_running()
+                    self._poll()
+                elif pending:
+                    wait = pending[0].arrival - (time.perf_counter() - self._t0)
+                    if wait > 2e-4:
+                        time.sleep(wait - 1e-4)
+        finally:
+            if gc_on:
+                gc.enable()
+        return self.completed
+
+    def close(self) -> None:
+        """Asks the decoder to return now and waits for it."""
+        _lib.lib().ck_host_publish(self._stop_addr, 1)
+        self.event.synchronize()
+        _lib.lib().ck_host_publish(self._stop_addr, 0)
+        self._running = False
+
+
+def _axis_structs(torch, device, order: int):
+    """The max-log axis structs of square QAM ``order`` on ``device``, and
+    the device tables they point into (kept alive with them)."""
+    from . import _device
+    from .mapping import _axis_struct, device_tables
+
+    like = _device.wrap(torch.empty(1, device=device))
+    tabs = device_tables(Constellation.qam(order), "maxlog", like)
+    half = len(tabs) // 2
+    return (_axis_struct(tabs[:half], "maxlog"), _axis_struct(tabs[half:], "maxlog"), tabs)
 
 
 # ---------------------------------------------------------------------------

@@ -252,6 +252,14 @@ int ck_gather(const ck_segment* segments, int32_t n, void* stream);
  */
 void ck_host_acquire(void);
 
+/*
+ * Host release store: writes `value` to `*counter` (mapped host memory)
+ * after every earlier store of the calling thread, e.g. the descriptors of a
+ * continuous feed's ring before the count that publishes them
+ * (ck_ldpc_feed_launch).
+ */
+void ck_host_publish(uint32_t* counter, uint32_t value);
+
 /* ---------------------------------------------------------------------- */
 /* Layered LDPC decoding                                                   */
 /* ---------------------------------------------------------------------- */
@@ -463,6 +471,93 @@ int ck_ldpc_mixed_workspace_size(const ck_ldpc_batch* batches, int32_t num_batch
  */
 int ck_ldpc_decode_mixed(const ck_ldpc_batch* batches, int32_t num_batches, void* workspace,
                          size_t workspace_bytes, void* stream);
+
+/*
+ * Continuous feed: the mixed decoder kept running while the host adds
+ * frames (no counterpart in the reference, which decodes one call's batch
+ * at a time).  Each queue is one batch entry (a code with its demapping, as
+ * for ck_ldpc_decode_mixed, with fused demapping) whose frames come from a
+ * ring of descriptors in mapped host memory that the host fills while the
+ * kernel runs.
+ *
+ * One frame of a feed: its symbols (n_in / k complex64, 8-byte aligned),
+ * where its results go (device or mapped host memory; bits ignored when the
+ * queue's k_bits is 0), its 1/sigma^2, and its place in the order of
+ * publication across queues (seq, compared modulo 2^32).  iters is written
+ * last, after the other results and a system-scope fence: a host that reads
+ * it >= -1 then sees them all (after ck_host_acquire).
+ */
+typedef struct ck_ldpc_feed_frame {
+    const void* symbols;
+    float* llr_out;
+    int8_t* bits;
+    int32_t* iters;
+    uint8_t* valid;
+    float inv_s2;
+    uint32_t seq;
+} ck_ldpc_feed_frame;
+
+/*
+ * A queue's ring: `capacity` (a power of two, at most 2^30) descriptors and
+ * the count of positions published so far, both in mapped host memory.
+ * Position q is frames[q % capacity]; the host writes a position's
+ * descriptor, then raises *published past it with ck_host_publish.  A slot
+ * may be rewritten once the frame it held has finished (its iters written).
+ */
+typedef struct ck_ldpc_feed_ring {
+    const ck_ldpc_feed_frame* frames;
+    const uint32_t* published;
+    uint32_t capacity;
+} ck_ldpc_feed_ring;
+
+/*
+ * Device scratch bytes of a feed over these queues.  The queues are
+ * ck_ldpc_batch entries as for ck_ldpc_decode_mixed with fused demapping:
+ * plan, n_in, min-sum parameters, k_bits, the two axis structs,
+ * frames_per_block and threads_per_frame are read; `symbols` must be
+ * non-NULL (the frames' own come from the ring); B, llr_in, llr_out, iters,
+ * valid, bits, inv_s2 and order are not read.
+ */
+int ck_ldpc_feed_workspace_size(const ck_ldpc_batch* queues, int32_t num_queues, size_t* bytes);
+
+/*
+ * Zeroes a feed workspace's counts of positions taken (its first 256 bytes),
+ * on `stream`: once, before the first launch over the workspace.
+ */
+int ck_ldpc_feed_reset(void* workspace, void* stream);
+
+/*
+ * Launches the continuous decoder: persistent blocks take published frames
+ * (each queue's in order; queues as `policy` says: CK_LDPC_FEED_OLDEST or
+ * CK_LDPC_FEED_SHORTEST), demap and decode them, and write their results.  A
+ * block with nothing to take polls for new frames and returns once none has
+ * been published for idle_us microseconds (1 to 1,000,000), or at once when
+ * *stop (mapped host memory; may be NULL) is non-zero; the launch ends when
+ * every block has returned.  The counts of positions taken stay in the
+ * workspace, so a later launch over the same workspace and rings continues
+ * where this one stopped.  Results are bit-identical to ck_ldpc_decode's.
+ */
+int ck_ldpc_feed_launch(const ck_ldpc_batch* queues, const ck_ldpc_feed_ring* rings, int32_t num_queues,
+                        const uint32_t* stop, uint32_t idle_us, int32_t policy, void* workspace,
+                        size_t workspace_bytes, void* stream);
+
+/* ck_ldpc_feed_launch policies: which queue a block takes next. */
+#define CK_LDPC_FEED_OLDEST 0   /* the queue whose oldest untaken frame was published first */
+#define CK_LDPC_FEED_SHORTEST 1 /* the queue of the fewest edges per frame; the oldest among equals */
+
+/*
+ * Host side of a feed, one request at a time: writes the descriptors of
+ * `frames` consecutive frames at ring positions [first, first + frames)
+ * (modulo capacity), then raises *published to first + frames with a
+ * release store.  Frame f reads symbols + f * symbol_bytes and writes its
+ * LLRs to llr_out + f * n_in, its bits to bits + f * k_bits (bits may be
+ * NULL), its flag to valid[f] and its iteration count, last, to
+ * iters_ring[(first + f) % capacity], which this call sets to -2 first
+ * (the host polls a queue's counts in one array); its seq is seq0 + f.
+ */
+int ck_ldpc_feed_publish(ck_ldpc_feed_frame* ring, uint32_t capacity, int32_t* iters_ring, uint32_t* published,
+                         uint32_t first, int32_t frames, const void* symbols, int64_t symbol_bytes, float* llr_out,
+                         int32_t n_in, int8_t* bits, int32_t k_bits, uint8_t* valid, float inv_s2, uint32_t seq0);
 
 /* Capacity of the decoder's static scratch array (64 MiB per GPU). */
 #define CK_LDPC_STATIC_SCRATCH_BYTES (64u * 1024u * 1024u)

@@ -38,6 +38,53 @@ def test_library_exports_every_declared_symbol():
     assert lib.ck_status_string(5) == b"device-side wait timed out"
 
 
+def test_python_constants_equal_the_header():
+    """Every integer #define of the C header has the same value in _lib."""
+    text = (ROOT / "include" / "commkit_gb300.h").read_text()
+    found = re.findall(r"#define (CK_[A-Z0-9_]+) \(?([0-9u* ]+)\)?", text)
+    assert len(found) > 10
+    for name, value in found:
+        want = 1
+        for factor in value.replace("u", "").split("*"):
+            want *= int(factor)
+        assert getattr(_lib, name) == want, name
+
+
+def test_feed_frame_layout_and_host_publish():
+    """The continuous feed's descriptor as the C header declares it (five
+    pointers, a float, a word: 48 bytes), and the host side of a feed, which
+    needs no GPU: ck_ldpc_feed_publish writes a request's descriptors around
+    the end of the ring, sets its iteration slots to -2 and raises the
+    published count."""
+    F = _lib.FeedFrame
+    assert ctypes.sizeof(F) == 48
+    assert [getattr(F, n).offset for n, _ in F._fields_] == [0, 8, 16, 24, 32, 40, 44]
+    assert ctypes.sizeof(_lib.FeedRing) == 24
+    cap, n_in, k_bits = 8, 100, 40
+    ring = (F * cap)()
+    iters = (ctypes.c_int32 * cap)(*range(cap))
+    published = ctypes.c_uint32(6)
+    sym, llr, bits, valid = 1 << 20, 2 << 20, 3 << 20, 4 << 20
+    st = _lib.lib().ck_ldpc_feed_publish(ctypes.addressof(ring), cap, ctypes.addressof(iters),
+                                         ctypes.addressof(published), 6, 4, sym, 4096, llr, n_in, bits, k_bits,
+                                         valid, 0.25, 77)  # fmt: skip
+    assert st == 0
+    assert published.value == 10
+    for f, slot in enumerate([6, 7, 0, 1]):
+        d = ring[slot]
+        assert d.symbols == sym + 4096 * f and d.llr_out == llr + 4 * n_in * f
+        assert d.bits == bits + k_bits * f and d.valid == valid + f
+        assert d.iters == ctypes.addressof(iters) + 4 * slot and iters[slot] == -2
+        assert d.inv_s2 == 0.25 and d.seq == 77 + f
+    assert [iters[s] for s in (2, 3, 4, 5)] == [2, 3, 4, 5]
+    assert _lib.lib().ck_ldpc_feed_publish(ctypes.addressof(ring), 6, ctypes.addressof(iters),
+                                           ctypes.addressof(published), 0, 1, sym, 8, llr, n_in, None, 0, valid,
+                                           1.0, 0) != 0  # capacity not a power of two  # fmt: skip
+    word = (ctypes.c_uint32 * 2)(7, 9)
+    _lib.lib().ck_host_publish(ctypes.addressof(word), 12345)
+    assert list(word) == [12345, 9]
+
+
 @pytest.mark.parametrize("name", ["A", "B", "C"])
 def test_native_schedule_matches_oracle(name):
     spec = W.CODES[name]
