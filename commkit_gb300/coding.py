@@ -626,13 +626,12 @@ def _decode_torch(llrs: Any, x0: _device.DeviceArray, code: LDPCCode, method: Mi
     nb = last // n
     C = 1 if len(shape) == 1 else shape[0]
     rows = C * nb
+    dev = llrs.device
     lead = () if len(shape) == 1 else (C,)
-    # empty_like / new_empty: the input's device and layout without parsing
-    # a device argument (the allocations are most of this call's host time).
-    out_llrs = torch.empty_like(llrs)
-    bits = llrs.new_empty(lead + (nb * k,), dtype=torch.int8)
-    iters = llrs.new_empty(lead + (nb,), dtype=torch.int32)
-    valid = llrs.new_empty(lead + (nb,), dtype=torch.bool)
+    out_llrs = torch.empty(lead + (nb * n,), dtype=torch.float32, device=dev)
+    bits = torch.empty(lead + (nb * k,), dtype=torch.int8, device=dev)
+    iters = torch.empty(lead + (nb,), dtype=torch.int32, device=dev)
+    valid = torch.empty(lead + (nb,), dtype=torch.bool, device=dev)
     if rows:
         with _device.on_device(x0):
             plan = code._plan(x0.device)

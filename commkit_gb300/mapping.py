@@ -578,7 +578,8 @@ def _llr_separable_gpu(symbols: Any, x: _device.DeviceArray, c: Constellation, n
     # The output in its final shape, (..., N * k): the same memory as (n, k).
     shape = tuple(x.shape[:-1]) + (x.shape[-1] * k,) if x.ndim else (k,)
     if x.kind == "torch":
-        out = symbols.new_empty(shape, dtype=_device._torch().float32)
+        torch = _device._torch()
+        out = torch.empty(shape, dtype=torch.float32, device=symbols.device)
         out_ptr = out.data_ptr()
     else:
         out = _device.empty(x, shape, np.float32)
