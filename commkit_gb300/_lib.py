@@ -33,7 +33,7 @@ CK_LDPC_SPECIALISE_OFF = 1
 CK_LDPC_SPECIALISE_ON = 2
 CK_LDPC_MAX_MIXED = 12
 CK_LDPC_FEED_OLDEST = 0
-CK_LDPC_FEED_SHORTEST = 1
+CK_LDPC_FEED_SHORT_FIRST = 1
 CK_LDPC_STATIC_SCRATCH_BYTES = 64 * 1024 * 1024
 
 # Every symbol the header declares; tests check the library exports them.

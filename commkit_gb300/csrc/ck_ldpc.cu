@@ -939,7 +939,7 @@ extern "C" int ck_ldpc_feed_launch(const ck_ldpc_batch* queues, const ck_ldpc_fe
                                    void* workspace, size_t workspace_bytes, void* stream) {
     ck::clear_error();
     if (!rings) return ck::fail(CK_ERR_INVALID_ARGUMENT, "rings is NULL");
-    if (policy != CK_LDPC_FEED_OLDEST && policy != CK_LDPC_FEED_SHORTEST)
+    if (policy != CK_LDPC_FEED_OLDEST && policy != CK_LDPC_FEED_SHORT_FIRST)
         return ck::fail(CK_ERR_INVALID_ARGUMENT, "unknown feed policy %d", policy);
     if (idle_us < 1 || idle_us > 1000000)
         return ck::fail(CK_ERR_INVALID_ARGUMENT, "idle_us must be in [1, 1000000], got %u", idle_us);

@@ -161,8 +161,9 @@ struct MixedParams {
     uint64_t idle_ns;
     const uint32_t* stop;
     // Which queue a feed block takes next: 0 the one whose oldest untaken
-    // frame was published first; 1 the one with the fewest edges per frame
-    // (the shortest frames), the oldest first among equals.
+    // frame was published first; 1 the same among the short codes' queues
+    // (under a quarter of the longest code's edges per frame) while any has
+    // a frame, else among the others.
     int32_t feed_policy;
 };
 
@@ -202,19 +203,20 @@ __device__ inline int feed_pick(const MixedParams& p) {
         if (c < p.num_codes && static_cast<int32_t>(avail[c] - taken[c]) > 0)
             seq[c] = ck::ld_relaxed_sys(&p.code[c].ring[taken[c] & p.code[c].ring_mask].seq);
     }
+    float heaviest = 0.0f;
+    for (int c = 0; c < p.num_codes; ++c) heaviest = fmaxf(heaviest, p.code[c].weight);
     int best = -1;
     uint32_t first = 0;
-    float light = 0.0f;
+    bool best_short = false;
 #pragma unroll
     for (int c = 0; c < kMaxMixed; ++c) {
         if (c >= p.num_codes || static_cast<int32_t>(avail[c] - taken[c]) <= 0) continue;
-        const float w = p.code[c].weight;
+        const bool is_short = p.feed_policy == 1 && 4.0f * p.code[c].weight < heaviest;
         const bool older = static_cast<int32_t>(seq[c] - first) < 0;
-        const bool better = p.feed_policy == 1 ? (w < light || (w == light && older)) : older;
-        if (best < 0 || better) {
+        if (best < 0 || (is_short && !best_short) || (is_short == best_short && older)) {
             best = c;
             first = seq[c];
-            light = w;
+            best_short = is_short;
         }
     }
     return best;

@@ -582,7 +582,7 @@ class FeedServer:
         self._qidx = {q: i for i, q in enumerate(self.queues)}
         self.ring_frames = int(ring_frames)
         self.idle_us = int(idle_us)
-        policies = {"oldest": _lib.CK_LDPC_FEED_OLDEST, "shortest": _lib.CK_LDPC_FEED_SHORTEST}
+        policies = {"oldest": _lib.CK_LDPC_FEED_OLDEST, "short_first": _lib.CK_LDPC_FEED_SHORT_FIRST}
         if policy not in policies:
             raise ValueError(f"policy must be one of {sorted(policies)}, got {policy!r}")
         self.policy = policy

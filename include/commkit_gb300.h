@@ -529,7 +529,7 @@ int ck_ldpc_feed_reset(void* workspace, void* stream);
 /*
  * Launches the continuous decoder: persistent blocks take published frames
  * (each queue's in order; queues as `policy` says: CK_LDPC_FEED_OLDEST or
- * CK_LDPC_FEED_SHORTEST), demap and decode them, and write their results.  A
+ * CK_LDPC_FEED_SHORT_FIRST), demap and decode them, and write their results.  A
  * block with nothing to take polls for new frames and returns once none has
  * been published for idle_us microseconds (1 to 1,000,000), or at once when
  * *stop (mapped host memory; may be NULL) is non-zero; the launch ends when
@@ -543,7 +543,8 @@ int ck_ldpc_feed_launch(const ck_ldpc_batch* queues, const ck_ldpc_feed_ring* ri
 
 /* ck_ldpc_feed_launch policies: which queue a block takes next. */
 #define CK_LDPC_FEED_OLDEST 0   /* the queue whose oldest untaken frame was published first */
-#define CK_LDPC_FEED_SHORTEST 1 /* the queue of the fewest edges per frame; the oldest among equals */
+#define CK_LDPC_FEED_SHORT_FIRST 1 /* the same among the short codes' queues (under a quarter of the
+                                       longest code's edges per frame) while any has a frame */
 
 /*
  * Host side of a feed, one request at a time: writes the descriptors of

@@ -34,7 +34,7 @@ def _check_standalone(ck, codes, method, done, dev):
         np.testing.assert_array_equal(r.valid, alone.valid.cpu().numpy().reshape(-1))
 
 
-@pytest.mark.parametrize("policy", ["oldest", "shortest"])
+@pytest.mark.parametrize("policy", ["oldest", "short_first"])
 def test_feed_results_equal_standalone_decodes(policy):
     """A Poisson stream of every code and constellation through the feed,
     under either queue policy."""
