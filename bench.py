@@ -514,7 +514,7 @@ def measure_mixed(args, dist: Dist) -> dict:
         copy_step()
     copy_ms = timed_flushed(dist, copy_step, args.steps, flush)
 
-    parity_ok, fer, iters = True, {}, {}
+    parity_ok, fer, iters, fp64 = True, {}, {}, {}
     oracle.build()
     edge_updates = 0.0
     for i, n in enumerate(names):
@@ -535,6 +535,10 @@ def measure_mixed(args, dist: Dist) -> dict:
                       and np.array_equal(r.llrs.cpu().numpy()[idx], opost)
                       and np.array_equal(r.iterations.cpu().numpy()[idx], oi)
                       and np.array_equal(r.valid.cpu().numpy()[idx], ov))  # fmt: skip
+        fp64[n] = decode_error_vs_fp64(r.llrs.cpu().numpy()[idx], r.iterations.cpu().numpy()[idx],
+                                       r.valid.cpu().numpy()[idx], r.bits.cpu().numpy()[idx], codes[n].k, want,
+                                       codes[n]._schedule, codes[n].num_variables, method.scale, method.offset,
+                                       w["max_it"])  # fmt: skip
         it = r.iterations.cpu().numpy()
         edge_updates += float(it.sum()) * codes[n].checks.size
         iters[n] = [int(it.min()), round(float(it.mean()), 2), int(it.max())]
@@ -586,7 +590,8 @@ def measure_mixed(args, dist: Dist) -> dict:
                          traffic=MIXED_DRAM_BYTES_PER_FRAME * sum(int(work[n].symbols.shape[0]) for n in names),
                          traffic_source=MIXED_TRAFFIC_NOTE),
         "decode": {"fer": fer, "iterations_min_mean_max": iters},
-        "parity": {"frames_checked": 16 * len(names), "bit_exact": bool(parity_ok)},
+        "parity": {"frames_checked": 16 * len(names), "bit_exact": bool(parity_ok),
+                   "decoder_vs_fp64": {"input": "the same float32 channel LLRs", "codes": fp64}},
         "clocks": clocks,
     }  # fmt: skip
 
@@ -648,9 +653,12 @@ def measure_single(args, dist: Dist, wname: str) -> dict:
     row, col, _ = code._schedule
     ob, opost, ov, oi = oracle.decode(llr_np, (row, col, code.num_variables), k=code.k, max_iterations=w["max_it"])
     bits = res.bits.reshape(frames, -1).cpu().numpy()
-    ok = (llr_ok and np.array_equal(bits[idx], ob)
-          and np.array_equal(res.llrs.reshape(frames, -1).cpu().numpy()[idx], opost)
-          and np.array_equal(res.valid.reshape(-1).cpu().numpy()[idx], ov) and np.array_equal(iters[idx], oi))  # fmt: skip
+    post = res.llrs.reshape(frames, -1).cpu().numpy()
+    valid = res.valid.reshape(-1).cpu().numpy()
+    ok = (llr_ok and np.array_equal(bits[idx], ob) and np.array_equal(post[idx], opost)
+          and np.array_equal(valid[idx], ov) and np.array_equal(iters[idx], oi))  # fmt: skip
+    fp64 = decode_error_vs_fp64(post[idx], iters[idx], valid[idx], bits[idx], code.k, llr_np, code._schedule,
+                                code.num_variables, method.scale, method.offset, w["max_it"])  # fmt: skip
     pk = peaks()
     sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
     ksym = const.bits_per_symbol
@@ -671,7 +679,8 @@ def measure_single(args, dist: Dist, wname: str) -> dict:
                      "frac": demap_bytes / (demap_ms * 1e-3) / 1e9 / pk["hbm_gbs"]},
         "decode": {"iterations_mean": float(iters.mean()),
                    "fer": float(np.mean(np.any(bits != batch.info, axis=1)))},
-        "parity": {"frames_checked": int(len(idx)), "bit_exact": bool(ok)},
+        "parity": {"frames_checked": int(len(idx)), "bit_exact": bool(ok),
+                   "decoder_vs_fp64": dict(fp64, input="the same float32 channel LLRs")},
     }  # fmt: skip
 
 
@@ -709,6 +718,98 @@ def llr_error_vs_fp64(llr: np.ndarray, ref: np.ndarray) -> dict:
 
 
 FP64_SAMPLE = 1 << 16
+
+
+def decode_fp64(llr: np.ndarray, schedule, n_var: int, scale: float, offset: float, max_it: int,
+                dtype=np.float64):
+    """The layered min-sum decode evaluated in float64 from the decoder's
+    float32 input LLRs: per row Q = APP - R, min1/min2/first argmin and the
+    sign parity of Q, R' = sign * max(scale min - offset, 0) (min2 at the
+    argmin), APP = Q + R', rows in the schedule's layer order, a syndrome
+    test before the first iteration and after each one
+    (``commkit/coding/_numba_loops.py:43-68,97-147``).  The rows of a layer
+    share no variable, so a layer is one vectorised step over its rows and
+    the frames.  Returns (posteriors, iterations, valid).  A checker for the
+    error statement beside the decoder's results, not a decoding path;
+    ``dtype=np.float32`` evaluates the same steps in the decoder's own
+    precision (the CPU tests hold that to the oracle bit for bit)."""
+    row_ptr, cols, layer_ptr = (np.asarray(a, np.int64) for a in schedule)
+    F, n = llr.shape
+    E = int(row_ptr[-1])
+    layers = []  # per layer: edge ids and columns (rows x widest row), padded with a dummy edge E / column n_var
+    for l in range(layer_ptr.size - 1):
+        rows = np.arange(layer_ptr[l], layer_ptr[l + 1])
+        deg = row_ptr[rows + 1] - row_ptr[rows]
+        D = int(deg.max())
+        pos = np.arange(D)[None, :]
+        mask = pos < deg[:, None]
+        eid = np.where(mask, row_ptr[rows][:, None] + pos, E)
+        cid = np.where(mask, np.append(cols, n_var)[eid], n_var)
+        layers.append((eid, cid, mask))
+    app = np.zeros((F, n_var + 1), dtype)
+    app[:, :n] = llr.astype(dtype)
+    msg = np.zeros((F, E + 1), dtype)
+    scale, offset = dtype(scale), dtype(offset)
+    one = dtype(1.0)
+    check_rows = np.repeat(np.arange(row_ptr.size - 1), np.diff(row_ptr))
+
+    def satisfied(a):
+        neg = (a[:, cols] < 0).astype(np.int64)
+        par = np.zeros((a.shape[0], row_ptr.size - 1), np.int64)
+        np.add.at(par.T, check_rows, neg.T)
+        return ~np.any(par & 1, axis=1)
+
+    iters = np.zeros(F, np.int32)
+    live = ~satisfied(app)
+    for _ in range(max_it):
+        f = np.flatnonzero(live)
+        if f.size == 0:
+            break
+        a, r = app[f], msg[f]
+        for eid, cid, mask in layers:
+            q = a[:, cid] - r[:, eid]
+            mag = np.where(mask, np.abs(q), np.inf)
+            order = np.argsort(mag, axis=2, kind="stable")  # the first edge holding min1 comes first
+            min1 = np.take_along_axis(mag, order[..., :1], axis=2)
+            min2 = np.take_along_axis(mag, order[..., 1:2], axis=2) if mag.shape[2] > 1 else np.full_like(min1, np.inf)
+            neg = (q < 0) & mask
+            par = np.logical_xor.reduce(neg, axis=2, keepdims=True)
+            n1 = np.maximum(scale * min1 - offset, dtype(0.0))
+            n2 = np.maximum(scale * min2 - offset, dtype(0.0))
+            at = np.arange(mask.shape[1])[None, None, :] == order[..., :1]
+            rn = np.where(at, n2, n1) * np.where(par ^ neg, -one, one)
+            a[:, cid[mask]] = (q + rn)[:, mask]
+            r[:, eid[mask]] = rn[:, mask]
+        app[f], msg[f] = a, r
+        iters[f] += 1
+        live[f] = ~satisfied(a)
+    return app[:, :n], iters, ~live
+
+
+def decode_error_vs_fp64(post: np.ndarray, iters: np.ndarray, valid: np.ndarray, bits: np.ndarray, k: int,
+                         llr: np.ndarray, schedule, n_var: int, scale: float, offset: float, max_it: int) -> dict:
+    """The decoder's float32 results against ``decode_fp64`` of the same
+    input LLRs, split by outcome.  Frames that converged: how many take the
+    same iteration count, the same validity and the same hard decisions in
+    float64, and over those with the same count the largest absolute
+    posterior error and the largest relative to the frame's largest
+    |posterior|.  Frames that ran every iteration without converging: how
+    many keep the same hard decisions (min-sum on a frame it cannot decode
+    wanders, and float32 and float64 rounding send it along different
+    paths, so these are counted, not compared)."""
+    p64, i64, v64 = decode_fp64(llr, schedule, n_var, scale, offset, max_it)
+    valid = np.asarray(valid).astype(bool).reshape(-1)
+    same_bits = np.all(bits.astype(bool) == (p64[:, :k] < 0), axis=1)
+    ok = valid
+    same = ok & (iters == i64) & v64
+    conv = {"frames": int(ok.sum()), "same_iterations_and_valid": int(same.sum()),
+            "same_bits": int((same_bits & ok).sum())}  # fmt: skip
+    if same.any():
+        err = np.abs(post[same].astype(np.float64) - p64[same])
+        peak = np.maximum(np.abs(p64[same]).max(axis=1, keepdims=True), 1e-30)
+        conv.update(max_abs=float(err.max()), max_rel_to_frame_peak=float((err / peak).max()))
+    return {"converged": conv,
+            "unconverged": {"frames": int((~ok).sum()), "same_bits": int((same_bits & ~ok).sum())}}
 
 
 def measure_demapper(dist: Dist) -> dict:
