@@ -28,6 +28,7 @@ CK_LDPC_SUM_PRODUCT = 1
 CK_LDPC_PLACE_AUTO = 0
 CK_LDPC_PLACE_SHARED = 1
 CK_LDPC_PLACE_GLOBAL = 2
+CK_LDPC_PLACE_EDGES = 3
 CK_LDPC_SPECIALISE_AUTO = 0
 CK_LDPC_SPECIALISE_OFF = 1
 CK_LDPC_SPECIALISE_ON = 2
@@ -62,6 +63,7 @@ EXPORTS = (
     "ck_ldpc_plan_get_info",
     "ck_ldpc_plan_set_launch",
     "ck_ldpc_plan_get_launch",
+    "ck_ldpc_plan_resolved_launch",
     "ck_ldpc_plan_set_specialise",
     "ck_ldpc_plan_get_specialise",
     "ck_ldpc_specialised_source",
@@ -210,6 +212,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         "ck_ldpc_plan_get_info": ([p, ctypes.POINTER(PlanInfo)], ctypes.c_int),
         "ck_ldpc_plan_set_launch": ([p, ctypes.POINTER(Launch)], ctypes.c_int),
         "ck_ldpc_plan_get_launch": ([p, ctypes.POINTER(Launch)], ctypes.c_int),
+        "ck_ldpc_plan_resolved_launch": ([p, i32, ctypes.POINTER(Launch)], ctypes.c_int),
         "ck_ldpc_plan_set_specialise": ([p, i32], ctypes.c_int),
         "ck_ldpc_plan_get_specialise": ([p, ctypes.POINTER(i32), ctypes.POINTER(i32)], ctypes.c_int),
         "ck_ldpc_specialised_source": ([p, p, p, i32, i32, i32, i32, ctypes.c_char_p, ctypes.c_size_t,

@@ -428,6 +428,15 @@ class _Plan:
         _lib.check(_lib.lib().ck_ldpc_plan_get_launch(self.handle, ctypes.byref(cfg)), "get_launch")
         return cfg.threads_per_frame, cfg.frames_per_block, cfg.placement
 
+    def resolved_launch(self, rule: int = _lib.CK_LDPC_MIN_SUM) -> tuple[int, int, int]:
+        """(threads per frame, frames per block, placement) a decode by
+        ``rule`` runs with now: the setting resolved on the plan's device
+        (current), the placement the one actually used."""
+        cfg = _lib.Launch()
+        st = _lib.lib().ck_ldpc_plan_resolved_launch(self.handle, int(rule), ctypes.byref(cfg))
+        _lib.check(st, "resolved_launch")
+        return cfg.threads_per_frame, cfg.frames_per_block, cfg.placement
+
     def set_specialise(self, mode: int) -> None:
         """``_lib.CK_LDPC_SPECIALISE_{AUTO,OFF,ON}``: whether min-sum decodes
         of this circulant code run its code-specialised kernel."""

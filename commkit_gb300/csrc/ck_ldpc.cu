@@ -121,6 +121,7 @@ struct Resolved {
     int cluster;
     int plain_grid;  // the plain kernel's grid for the same frames
     int32_t sign_words;  // wide min-sum state: sign words per row (0: packed or sum-product)
+    bool edges;  // min-sum with one message per edge in shared memory (CK_LDPC_PLACE_EDGES)
 };
 
 constexpr int kMaxCluster = 8;  // the portable cluster size
@@ -244,21 +245,6 @@ int resolve_shape(const ck_ldpc_plan* plan, int32_t rule, Resolved* r, int* per_
                         "quasi-cyclic code of N = %d: its posterior (%u bytes) does not fit in shared "
                         "memory",
                         plan->N, app_bytes);
-    bool r_smem;
-    // A plan's frames per block and placement are min-sum shapes (tuned or
-    // set); sum-product, whose per-edge state is several times larger,
-    // always picks its own.
-    const int32_t place = sp ? CK_LDPC_PLACE_AUTO : plan->launch.placement;
-    if (!app_smem || place == CK_LDPC_PLACE_GLOBAL) {
-        r_smem = false;
-    } else if (place == CK_LDPC_PLACE_SHARED) {
-        r_smem = ctrl + gblk_bytes + app_bytes + r_bytes <= budget;
-    } else {
-        // Auto: beside the LLRs when two frames still fit per block budget.
-        r_smem = 2 * (ctrl + gblk_bytes + app_bytes + r_bytes) <= budget;
-    }
-    uint32_t group = ctrl + gblk_bytes + (app_smem ? app_bytes : 0) + (r_smem ? r_bytes : 0);
-
     int32_t T = plan->launch.threads_per_frame;
     const int32_t Zp = plan->qc ? (plan->Z + 31) / 32 * 32 : 0;
     if (T == 0) {
@@ -283,6 +269,45 @@ int resolve_shape(const ck_ldpc_plan* plan, int32_t rule, Resolved* r, int* per_
         return ck::fail(CK_ERR_INVALID_ARGUMENT,
                         "threads_per_frame %d above %d for row degree %d", T, max_threads,
                         plan->max_deg);
+
+    bool r_smem;
+    uint32_t r_used = r_bytes, r_stride_used = r_stride;
+    // A plan's frames per block and placement are min-sum shapes (tuned or
+    // set); sum-product, whose per-edge state is several times larger,
+    // always picks its own.
+    const int32_t place = sp ? CK_LDPC_PLACE_AUTO : plan->launch.placement;
+    // One message per edge in shared memory: the code-specialised kernel of a
+    // circulant code with rows up to 27 edges and one thread per row slot,
+    // when a frame fits (EDGES) or two frames fit per block budget (AUTO:
+    // measured faster than the records on codes A and B); otherwise (or when
+    // its kernel is unavailable) the records as SHARED (AUTO as before).
+    const void* edge_kernel = nullptr;
+    if ((place == CK_LDPC_PLACE_EDGES || place == CK_LDPC_PLACE_AUTO) && !sp && plan->qc && app_smem && T == Zp &&
+        plan->max_deg <= kPackedDegree) {
+        const uint32_t e_stride = align_up(static_cast<uint32_t>(plan->E), 32);
+        const uint32_t frames = place == CK_LDPC_PLACE_AUTO ? 2 : 1;
+        if (frames * (ctrl + gblk_bytes + app_bytes + e_stride * 4) <= budget) {
+            if (may_compile)
+                CK_TRY(specialised_kernel(plan, kernel_dmax(true, plan->max_deg), kPlaceEdges, &edge_kernel));
+            else
+                CK_TRY(specialised_kernel_ready(plan, kPlaceEdges, &edge_kernel));
+            if (edge_kernel) {
+                r_used = e_stride * 4;
+                r_stride_used = e_stride;
+            }
+        }
+    }
+    if (edge_kernel) {
+        r_smem = true;
+    } else if (!app_smem || place == CK_LDPC_PLACE_GLOBAL) {
+        r_smem = false;
+    } else if (place == CK_LDPC_PLACE_SHARED || place == CK_LDPC_PLACE_EDGES) {
+        r_smem = ctrl + gblk_bytes + app_bytes + r_bytes <= budget;
+    } else {
+        // Auto: beside the LLRs when two frames still fit per block budget.
+        r_smem = 2 * (ctrl + gblk_bytes + app_bytes + r_bytes) <= budget;
+    }
+    uint32_t group = ctrl + gblk_bytes + (app_smem ? app_bytes : 0) + (r_smem ? r_used : 0);
     int32_t G = sp ? 0 : plan->launch.frames_per_block;
     const int32_t gmax_threads = max_threads / T;
     const int32_t gmax_smem = static_cast<int32_t>(budget / group);
@@ -296,14 +321,17 @@ int resolve_shape(const ck_ldpc_plan* plan, int32_t rule, Resolved* r, int* per_
                               : min_sum_kernel(plan->qc, plan->max_deg, app_smem, r_smem, one_row);
     if (!table) return ck::fail(CK_ERR_UNSUPPORTED, "no decoder kernel for this code shape");
     const void* kernel = reinterpret_cast<const void*>(table);
-    if (!sp && plan->qc && T == Zp && app_smem && plan->max_deg <= kPackedDegree) {
+    if (edge_kernel) {
+        kernel = edge_kernel;
+    } else if (!sp && plan->qc && T == Zp && app_smem && plan->max_deg <= kPackedDegree) {
         // The code-specialised kernel, where the plan has one (codes with
         // rows above 27 edges have none: they run the any-degree kernels).
         const void* special = nullptr;
+        const int kind = r_smem ? kPlaceRecords : kPlaceDevice;
         if (may_compile)
-            CK_TRY(specialised_kernel(plan, kernel_dmax(true, plan->max_deg), r_smem, &special));
+            CK_TRY(specialised_kernel(plan, kernel_dmax(true, plan->max_deg), kind, &special));
         else
-            CK_TRY(specialised_kernel_ready(plan, r_smem, &special));
+            CK_TRY(specialised_kernel_ready(plan, kind, &special));
         if (special) kernel = special;
     }
     CK_TRY(ck::allow_max_smem(kernel, plan->device, optin));
@@ -337,7 +365,8 @@ int resolve_shape(const ck_ldpc_plan* plan, int32_t rule, Resolved* r, int* per_
     r->gblk_off = ctrl;
     r->app_off = ctrl + gblk_bytes;
     r->r_off = ctrl + gblk_bytes + (app_smem ? app_bytes : 0);
-    r->r_stride = r_stride;
+    r->r_stride = r_stride_used;
+    r->edges = edge_kernel != nullptr;
     r->smem = tables + static_cast<uint32_t>(G) * group;
     r->app_stride = static_cast<int32_t>(app_bytes / 4);
     r->sign_words = sign_words;
@@ -627,6 +656,7 @@ struct MixedResolved {
     uint32_t block_words;  // device-memory message state per block, shared by the codes
     bool wide;  // some code has rows above degree 16
     bool any_degree;  // some code has rows above degree 27: the any-degree kernel, wide state for all
+    bool edges;  // some code keeps one message per edge (r_smem == 2; its specialised program only)
 };
 
 // Occupancy per (kernel, device, block shape), remembered: the request
@@ -650,8 +680,9 @@ int mixed_occupancy(const void* kernel, int dev, int threads, uint32_t smem, int
 
 // feed: the queues of a continuous feed (ck_ldpc_feed_launch): every queue
 // may run (its frames come later), the grid is every resident block, and
-// the per-frame arrays come from the rings instead.
-int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R, bool feed = false) {
+// the per-frame arrays come from the rings instead.  allow_edges: codes set
+// to CK_LDPC_PLACE_EDGES may keep one message per edge.
+int resolve_mixed_shape(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R, bool feed, bool allow_edges) {
     if (!batches || n < 1 || n > kMaxMixed)
         return ck::fail(CK_ERR_INVALID_ARGUMENT, "1 to %d batches per mixed launch, got %d", kMaxMixed, n);
     int dev = -1;
@@ -664,6 +695,7 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R, boo
     R->smem = 0;
     R->wide = false;
     R->any_degree = false;
+    R->edges = false;
     for (int c = 0; c < n; ++c)
         if (batches[c].plan && batches[c].plan->max_deg > kPackedDegree) R->any_degree = true;
     for (int c = 0; c < n; ++c) {
@@ -738,11 +770,17 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R, boo
         const uint32_t budget = static_cast<uint32_t>(optin) > tables + 1024 ? optin - tables - 1024 : 0;
         const int32_t max_threads = R->wide ? 512 : kMixedThreads;
         int32_t gmax = std::min(max_threads / T, T > 32 ? ck::kMaxNamedGroups : 32);
-        // Message state in shared memory when two frames still fit with it.
-        const bool r_smem = plan->launch.placement == CK_LDPC_PLACE_GLOBAL
-                                ? false
-                                : 2 * (ctrl + gblk + app + rsm) <= budget;
-        const uint32_t group = ctrl + gblk + app + (r_smem ? rsm : 0);
+        // Message state in shared memory when two frames still fit with it:
+        // one message per edge (CK_LDPC_PLACE_EDGES, a code run by its
+        // program with one thread per row slot), else the records.
+        const uint32_t e_stride = align_up(static_cast<uint32_t>(plan->E), 32);
+        const bool edges = allow_edges &&
+                           (plan->launch.placement == CK_LDPC_PLACE_EDGES ||
+                            plan->launch.placement == CK_LDPC_PLACE_AUTO) &&
+                           !R->any_degree && T == Zp && 2 * (ctrl + gblk + app + 4 * e_stride) <= budget;
+        const bool r_smem = edges || (plan->launch.placement != CK_LDPC_PLACE_GLOBAL &&
+                                      2 * (ctrl + gblk + app + rsm) <= budget);
+        const uint32_t group = ctrl + gblk + app + (edges ? 4 * e_stride : (r_smem ? rsm : 0));
         gmax = std::min<int32_t>(gmax, static_cast<int32_t>(budget / group));
         // As many groups as the block's threads and shared memory hold: a
         // plain launch's tuned frames per block (one block of G groups among
@@ -777,13 +815,14 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R, boo
         K.T = T;
         K.G = G;
         K.q_bstep = T >= Zp ? T / Zp : 1;
-        K.r_smem = r_smem ? 1 : 0;
+        K.r_smem = edges ? 2 : (r_smem ? 1 : 0);
+        R->edges |= edges;
         K.tables_bytes = tables;
         K.group_bytes = group;
         K.gblk_off = ctrl;
         K.app_off = ctrl + gblk;
         K.r_off = ctrl + gblk + app;
-        K.r_stride = r_stride;
+        K.r_stride = edges ? e_stride : r_stride;
         K.weight = static_cast<float>(plan->E);
         K.sign_words = sign_words;
         K.ka = ka;
@@ -813,15 +852,21 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R, boo
         // The code-specialised mixed kernel, where the plans have one.
         const ck_ldpc_plan* plans[kMaxMixed];
         int32_t threads[kMaxMixed];
+        int edges[kMaxMixed];
         for (int c = 0; c < n; ++c) {
             plans[c] = batches[c].plan;
             threads[c] = R->p.code[c].T;
+            edges[c] = R->p.code[c].r_smem == 2 ? 1 : 0;
         }
         const void* special = nullptr;
-        CK_TRY(ck::ldpc::mixed_specialised_kernel(plans, threads, n, R->wide ? 27 : 16, &special));
+        CK_TRY(ck::ldpc::mixed_specialised_kernel(plans, threads, edges, n, R->wide ? 27 : 16, &special));
         if (special) kernel = special;
     }
+    // The per-edge state runs in the specialised programs only: without
+    // them the codes keep the records (the caller sizes the launch again).
     R->kernel = kernel;
+    if (R->edges && kernel == reinterpret_cast<const void*>(R->wide ? ldpc_mixed_kernel<27> : ldpc_mixed_kernel<16>))
+        return CK_OK;
     CK_TRY(ck::allow_max_smem(kernel, dev, optin));
     int per_sm = 0;
     CK_TRY(mixed_occupancy(kernel, dev, R->block_threads, R->smem, &per_sm));
@@ -862,7 +907,30 @@ int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R, boo
     return CK_OK;
 }
 
+int resolve_mixed(const ck_ldpc_batch* batches, int32_t n, MixedResolved* R, bool feed = false) {
+    CK_TRY(resolve_mixed_shape(batches, n, R, feed, true));
+    const void* table = reinterpret_cast<const void*>(R->wide ? ldpc_mixed_kernel<27> : ldpc_mixed_kernel<16>);
+    if (R->edges && R->kernel == table) CK_TRY(resolve_mixed_shape(batches, n, R, feed, false));
+    return CK_OK;
+}
+
 }  // namespace
+
+extern "C" int ck_ldpc_plan_resolved_launch(const ck_ldpc_plan* plan, int32_t rule, ck_ldpc_launch* out) {
+    ck::clear_error();
+    if (!plan || !out) return ck::fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
+    int device = -1;
+    CK_CUDA(cudaGetDevice(&device));
+    if (device != plan->device)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "plan is for device %d, current device is %d", plan->device,
+                        device);
+    Resolved r;
+    CK_TRY(resolve(plan, rule, 1, &r));
+    out->threads_per_frame = r.T;
+    out->frames_per_block = r.G;
+    out->placement = !r.r_smem ? CK_LDPC_PLACE_GLOBAL : (r.edges ? CK_LDPC_PLACE_EDGES : CK_LDPC_PLACE_SHARED);
+    return CK_OK;
+}
 
 extern "C" int ck_ldpc_mixed_workspace_size(const ck_ldpc_batch* batches, int32_t num_batches,
                                             size_t* bytes) {

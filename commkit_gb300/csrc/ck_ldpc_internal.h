@@ -69,7 +69,7 @@ struct ck_ldpc_plan {
         bool tried = false;
         int dmax = 0;
         cudaLibrary_t lib = nullptr;
-        const void* kernel[2] = {nullptr, nullptr};
+        const void* kernel[3] = {nullptr, nullptr, nullptr};  // by placement: device, records, edges
         std::string why;  // why there are none
     };
     uint64_t id = 0;  // unique in the process, never reused
@@ -88,27 +88,34 @@ int allow_max_smem(const void* kernel, int device, int optin);
 // (a kernel loaded later may get the same handle).
 void forget_kernel(const void* kernel);
 namespace ldpc {
+// Message-state placements of the specialised kernels (kernel index).
+constexpr int kPlaceDevice = 0;  // packed records in device memory
+constexpr int kPlaceRecords = 1;  // packed records in shared memory
+constexpr int kPlaceEdges = 2;  // one message per edge in shared memory
 // The plan's code-specialised min-sum kernel for a row-degree bound and a
 // message-state placement (compiled on first use), or nullptr in *out when
 // the plan has none (specialisation off, NVRTC missing or the compilation
 // failed); an error only when the plan requires specialisation.
-int specialised_kernel(const ck_ldpc_plan* plan, int dmax, bool r_smem, const void** out);
+int specialised_kernel(const ck_ldpc_plan* plan, int dmax, int place, const void** out);
 // The same kernel only if an earlier call already compiled it (nullptr in
 // *out otherwise): never compiles or loads code, for the allocation-free
 // entry point.  An error only when the plan requires specialisation and has
 // no compiled kernel.
-int specialised_kernel_ready(const ck_ldpc_plan* plan, bool r_smem, const void** out);
+int specialised_kernel_ready(const ck_ldpc_plan* plan, int place, const void** out);
 // The NVRTC source of a circulant plan's specialised kernels.
 std::string specialised_source(const ck_ldpc_plan& plan, int dmax);
 // The NVRTC source of the specialised mixed kernel of n plans, batch c with
-// parts[c] threads per row slot (0: the table loop).
-std::string mixed_source(const ck_ldpc_plan* const* plans, const int* parts, int n, int dmax);
+// parts[c] threads per row slot (0: the table loop) and edges[c] its
+// per-edge state.
+std::string mixed_source(const ck_ldpc_plan* const* plans, const int* parts, const int* edges, int n, int dmax);
 // The code-specialised mixed kernel for these plans with threads per frame
 // T[c] (batches with T[c] == Zp or 2 Zp, Zp = Z rounded up to whole warps,
-// run their code's program, the others the table loop), compiled on first
-// use; nullptr in *out when there is none.
-int mixed_specialised_kernel(const ck_ldpc_plan* const* plans, const int32_t* T, int n, int dmax,
-                             const void** out);
+// run their code's program, the others the table loop) and edges[c] (a
+// batch run by its program with one thread per row slot keeps one message
+// per edge in shared memory), compiled on first use; nullptr in *out when
+// there is none.
+int mixed_specialised_kernel(const ck_ldpc_plan* const* plans, const int32_t* T, const int* edges, int n,
+                             int dmax, const void** out);
 // Unloads the specialised kernels that use `plan` (before it is freed).
 void forget_plan_kernels(const ck_ldpc_plan* plan);
 }  // namespace ldpc

@@ -210,9 +210,12 @@ std::string program_struct(const ck_ldpc_plan& plan, const char* name, int H = 1
                     4ll * first);
             }
         }
+        // The row's state: its record at b Z + qr0, or (per-edge state) the
+        // messages of its circulants e0.. at byte 4 (e0 Z + qr0) + 4 Z e.
         s += ind;
-        add(s, "    st.template row_cols<%lld>(c, cur, %lldu + qr0, scale, offset);\n", deg,
-            static_cast<long long>(b) * Z);
+        add(s, "    st.template row_cols<%lld, %lldu>(c, cur, ", deg, 4ll * Z);
+        add(s, "%lldu + qr0, %lldu + 4u * qr0, scale, offset);\n", static_cast<long long>(b) * Z,
+            4ll * e0 * Z);
         if (pad) {
             s += ind;
             s += "    }\n";
@@ -304,17 +307,19 @@ std::string program_struct(const ck_ldpc_plan& plan, const char* name, int H = 1
 }
 
 // The plain decoder of one code: one kernel per message-state placement
-// (device memory, shared memory).
+// (r0 records in device memory, r1 records in shared memory, r2 one
+// message per edge in shared memory).
 std::string program_source(const ck_ldpc_plan& plan, int dmax) {
     std::string s = "#include \"ck_ldpc_minsum.cuh\"\nusing namespace ck::ldpc;\nnamespace {\n";
     s += program_struct(plan, "CodeProgram");
     s += "}  // namespace\n";
-    for (int r = 0; r < 2; ++r) {
+    for (int r = 0; r < 3; ++r) {
         // A minimum of one block per SM, stated: without it ptxas held some of
         // these kernels to 40 registers and spilled.
         add(s, "extern \"C\" __global__ void __launch_bounds__(%lld, 1) ck_ldpc_code_r%lld(const __grid_constant__ Params p) {\n",
             max_block_threads(true, dmax), r);
-        add(s, "    decode_body<MinSumState, true, %lld, true, ", dmax);
+        s += r == 2 ? "    decode_body<EdgeMinSumState" : "    decode_body<MinSumState";
+        add(s, ", true, %lld, true, ", dmax);
         s += r ? "true" : "false";
         s += ", true, CodeProgram>(p);\n}\n";
     }
@@ -322,8 +327,11 @@ std::string program_source(const ck_ldpc_plan& plan, int dmax) {
 }
 
 // The mixed decoder of n batches; batch c runs its code's program with
-// parts[c] threads per row slot when parts[c] > 0, else the table loop.
-std::string mixed_program_source(const ck_ldpc_plan* const* plans, const int* parts, int n, int dmax) {
+// parts[c] threads per row slot when parts[c] > 0, else the table loop;
+// edges[c]: its program keeps one message per edge in shared memory
+// (MixedCode::r_smem == 2).
+std::string mixed_program_source(const ck_ldpc_plan* const* plans, const int* parts, const int* edges, int n,
+                                 int dmax) {
     std::string s = "#include \"ck_ldpc_mixed.cuh\"\nusing namespace ck::ldpc;\nnamespace {\n";
     // A code may fill several batches (one per constellation): one program
     // and one call site per distinct (plan, parts), its batches as cases of
@@ -334,7 +342,7 @@ std::string mixed_program_source(const ck_ldpc_plan* const* plans, const int* pa
         special[c] = parts[c] > 0;
         first[c] = c;
         for (int u = 0; u < c; ++u)
-            if (plans[u] == plans[c] && parts[u] == parts[c]) {
+            if (plans[u] == plans[c] && parts[u] == parts[c] && edges[u] == edges[c]) {
                 first[c] = u;
                 break;
             }
@@ -351,7 +359,10 @@ std::string mixed_program_source(const ck_ldpc_plan* const* plans, const int* pa
         if (first[c] != c) continue;
         for (int d = c; d < n; ++d)
             if (first[d] == c) add(s, "            case %lld:\n", d);
-        if (special[c]) {
+        if (special[c] && edges[c]) {
+            const std::string prog = "CodeProgram" + std::to_string(c);
+            s += "                mixed_frames<DMAX, true, true, " + prog + ", true>(K, smem, s_layer, s_eptr, s_blk, g, tid);\n";
+        } else if (special[c]) {
             const std::string prog = "CodeProgram" + std::to_string(c);
             s += "                if (K.r_smem)\n";
             s += "                    mixed_frames<DMAX, true, true, " + prog + ">(K, smem, s_layer, s_eptr, s_blk, g, tid);\n";
@@ -440,11 +451,11 @@ std::map<std::vector<uint64_t>, MixedJit> g_mixed;
 
 std::string specialised_source(const ck_ldpc_plan& plan, int dmax) { return program_source(plan, dmax); }
 
-std::string mixed_source(const ck_ldpc_plan* const* plans, const int* parts, int n, int dmax) {
-    return mixed_program_source(plans, parts, n, dmax);
+std::string mixed_source(const ck_ldpc_plan* const* plans, const int* parts, const int* edges, int n, int dmax) {
+    return mixed_program_source(plans, parts, edges, n, dmax);
 }
 
-int specialised_kernel(const ck_ldpc_plan* plan, int dmax, bool r_smem, const void** out) {
+int specialised_kernel(const ck_ldpc_plan* plan, int dmax, int place, const void** out) {
     *out = nullptr;
     const int mode = effective_mode(plan->jit_mode);
     if (mode == CK_LDPC_SPECIALISE_OFF) return CK_OK;
@@ -453,8 +464,8 @@ int specialised_kernel(const ck_ldpc_plan* plan, int dmax, bool r_smem, const vo
     if (!j.tried) {  // a plan's degree bound never changes, so one compilation serves it
         j.tried = true;
         j.dmax = dmax;
-        static const char* const names[] = {"ck_ldpc_code_r0", "ck_ldpc_code_r1"};
-        if (!compile_load(program_source(*plan, dmax), plan->device, names, 2, &j.lib, j.kernel, &j.why))
+        static const char* const names[] = {"ck_ldpc_code_r0", "ck_ldpc_code_r1", "ck_ldpc_code_r2"};
+        if (!compile_load(program_source(*plan, dmax), plan->device, names, 3, &j.lib, j.kernel, &j.why))
             j.lib = nullptr;
     }
     if (!j.lib) {
@@ -462,18 +473,18 @@ int specialised_kernel(const ck_ldpc_plan* plan, int dmax, bool r_smem, const vo
             return ck::fail(CK_ERR_UNSUPPORTED, "code-specialised decoder unavailable: %s", j.why.c_str());
         return CK_OK;
     }
-    *out = j.kernel[r_smem ? 1 : 0];
+    *out = j.kernel[place];
     return CK_OK;
 }
 
-int specialised_kernel_ready(const ck_ldpc_plan* plan, bool r_smem, const void** out) {
+int specialised_kernel_ready(const ck_ldpc_plan* plan, int place, const void** out) {
     *out = nullptr;
     const int mode = effective_mode(plan->jit_mode);
     if (mode == CK_LDPC_SPECIALISE_OFF) return CK_OK;
     std::lock_guard<std::mutex> lock(plan->jit_mu);
     const ck_ldpc_plan::Jit& j = plan->jit;
     if (j.tried && j.lib) {
-        *out = j.kernel[r_smem ? 1 : 0];
+        *out = j.kernel[place];
         return CK_OK;
     }
     if (mode == CK_LDPC_SPECIALISE_ON)
@@ -485,10 +496,11 @@ int specialised_kernel_ready(const ck_ldpc_plan* plan, bool r_smem, const void**
     return CK_OK;
 }
 
-int mixed_specialised_kernel(const ck_ldpc_plan* const* plans, const int32_t* T, int n, int dmax,
-                             const void** out) {
+int mixed_specialised_kernel(const ck_ldpc_plan* const* plans, const int32_t* T, const int* edges, int n,
+                             int dmax, const void** out) {
     *out = nullptr;
     int parts[CK_LDPC_MAX_MIXED] = {};
+    int edge[CK_LDPC_MAX_MIXED] = {};
     if (n < 1 || n > CK_LDPC_MAX_MIXED) return CK_OK;
     bool any = false, required = false;
     std::vector<uint64_t> key{static_cast<uint64_t>(dmax)};
@@ -500,9 +512,10 @@ int mixed_specialised_kernel(const ck_ldpc_plan* const* plans, const int32_t* T,
         // the code's program; other shapes run the table loop.
         const int32_t Zp = (plans[c]->Z + 31) / 32 * 32;
         parts[c] = T[c] == Zp ? 1 : (T[c] == 2 * Zp ? 2 : 0);
+        edge[c] = parts[c] == 1 && edges[c] ? 1 : 0;  // per-edge state with one thread per row slot only
         any |= parts[c] > 0;
         key.push_back(plans[c]->id);
-        key.push_back(static_cast<uint64_t>(parts[c]));
+        key.push_back(static_cast<uint64_t>(parts[c]) | (static_cast<uint64_t>(edge[c]) << 8));
     }
     if (!any) return CK_OK;
     std::lock_guard<std::mutex> lock(g_mixed_mu);
@@ -512,7 +525,7 @@ int mixed_specialised_kernel(const ck_ldpc_plan* const* plans, const int32_t* T,
         static const char* const names[] = {"ck_ldpc_mixed_code"};
         const void* k = nullptr;
         const int dev = plans[0]->device;
-        if (compile_load(mixed_program_source(plans, parts, n, dmax), dev, names, 1, &mj.lib, &k, &mj.why))
+        if (compile_load(mixed_program_source(plans, parts, edge, n, dmax), dev, names, 1, &mj.lib, &k, &mj.why))
             mj.kernel = k;
         it = g_mixed.emplace(key, std::move(mj)).first;
     }
@@ -542,8 +555,7 @@ void forget_plan_kernels(const ck_ldpc_plan* plan) {
         it = g_mixed.erase(it);
     }
     if (plan->jit.lib) {
-        ck::forget_kernel(plan->jit.kernel[0]);
-        ck::forget_kernel(plan->jit.kernel[1]);
+        for (const void* k : plan->jit.kernel) ck::forget_kernel(k);
         (void)cudaLibraryUnload(plan->jit.lib);
     }
 }

@@ -255,12 +255,12 @@ struct MinSumState {
     }
     template <int DMAX>
     __device__ __forceinline__ void qc_row(const Params& p, const int2* gblk, int deg, uint32_t row,
-                                           int32_t, int32_t, uint32_t r4, uint32_t Z4) const {
-        qc_row_k<DMAX>(gblk, deg, row, r4, Z4, p.scale, p.offset);
+                                           int32_t e0, int32_t, uint32_t r4, uint32_t Z4) const {
+        qc_row_k<DMAX>(gblk, deg, row, e0, r4, Z4, p.scale, p.offset);
     }
     template <int DMAX>
-    __device__ __forceinline__ void qc_row_k(const int2* gblk, int deg, uint32_t row, uint32_t r4, uint32_t Z4,
-                                             float scale, float offset) const {
+    __device__ __forceinline__ void qc_row_k(const int2* gblk, int deg, uint32_t row, int32_t, uint32_t r4,
+                                             uint32_t Z4, float scale, float offset) const {
         const uint4 s = load(row);
         float m1 = __uint_as_float(s.x), m2 = __uint_as_float(s.y);
         uint32_t w = s.z;
@@ -278,9 +278,10 @@ struct MinSumState {
         return R_SMEM ? load(row) : early;
     }
     // One circulant row with its columns computed by the caller (the
-    // code-specialised programs), its state `s` from take().
-    template <int D>
-    __device__ __forceinline__ void row_cols(const uint32_t (&c)[D], const uint4 s, uint32_t row,
+    // code-specialised programs), its state `s` from take(); the edge-state
+    // form's message offset and lifting are unused here.
+    template <int D, uint32_t Z4>
+    __device__ __forceinline__ void row_cols(const uint32_t (&c)[D], const uint4 s, uint32_t row, uint32_t,
                                              float scale, float offset) const {
         float m1 = __uint_as_float(s.x), m2 = __uint_as_float(s.y);
         uint32_t w = s.z;
@@ -414,8 +415,8 @@ struct WideMinSumState {
         any_row(QcSmemPost{gblk, r4, Z4}, deg, row, p.scale, p.offset);
     }
     template <int DMAX>
-    __device__ __forceinline__ void qc_row_k(const int2* gblk, int deg, uint32_t row, uint32_t r4, uint32_t Z4,
-                                             float scale, float offset) const {
+    __device__ __forceinline__ void qc_row_k(const int2* gblk, int deg, uint32_t row, int32_t, uint32_t r4,
+                                             uint32_t Z4, float scale, float offset) const {
         any_row(QcSmemPost{gblk, r4, Z4}, deg, row, scale, offset);
     }
     template <int DMAX, class ColOf>
@@ -423,6 +424,160 @@ struct WideMinSumState {
                                             const ColOf& col_of) const {
         any_row(CsrPost<ColOf>{a, col_of}, deg, row, p.scale, p.offset);
     }
+};
+
+// One circulant row of exactly D edges with one message per edge (the
+// edge state below): c[e] the shared addresses of its posteriors, mo[e] of
+// its messages.  The reference's two passes (commkit/_cuda/src/ldpc.cu:45-72)
+// with the record form's reductions (qc_row_cols: min1/min2 over pairs of
+// edges, min2' for every edge whose |Q| equals min1), so the same floats:
+//  * Q = APP - R_old, the old message a plain load;
+//  * the row's sign parity is bit 31 of the XOR of its Q words (no -0
+//    reaches Q and its NaNs are positive, so the sign bit is "Q < 0");
+//  * the parity goes onto min1' and min2' once per row, and each edge's new
+//    message is the chosen magnitude with its own Q sign XORed in.
+template <int D>
+__device__ __forceinline__ void qc_row_edges(const uint32_t (&c)[D], const uint32_t (&mo)[D], const float scale,
+                                             const float offset) {
+    float q[D];
+    float min1 = ck::inf_f(), min2 = ck::inf_f();
+    uint32_t par = 0u;
+#pragma unroll
+    for (int e = 0; e < D; ++e) {
+        const float qe = __fsub_rn(ld_shared_f32(c[e]), ld_shared_f32(mo[e]));
+        q[e] = qe;
+        par ^= __float_as_uint(qe);
+        if (e & 1) {
+            const float x = fabsf(q[e - 1]), y = fabsf(qe);
+            const float hi = fmax_nan(x, y);
+            if (e == 1) {
+                min1 = fmin3(x, y, ck::inf_f());
+                min2 = fminf(hi, ck::inf_f());
+            } else {
+                const float lo = fminf(x, y);
+                min2 = fmin3(min2, hi, fmax_nan(min1, lo));
+                min1 = fminf(min1, lo);
+            }
+        } else if (e == D - 1) {
+            const float mag = fabsf(qe);
+            min2 = fminf(min2, fmax_nan(min1, mag));
+            min1 = fminf(min1, mag);
+        }
+    }
+    const float n1 = fmaxf(__fsub_rn(__fmul_rn(scale, min1), offset), 0.0f);
+    const float n2 = fmaxf(__fsub_rn(__fmul_rn(scale, min2), offset), 0.0f);
+    const uint32_t ps = par & 0x80000000u;
+    const uint32_t p1 = __float_as_uint(n1) ^ ps, p2 = __float_as_uint(n2) ^ ps;
+#pragma unroll
+    for (int e = 0; e < D; ++e) {
+        const uint32_t pm = fabsf(q[e]) == min1 ? p2 : p1;
+        const float rn = __uint_as_float(pm ^ (__float_as_uint(q[e]) & 0x80000000u));
+        st_shared_f32(mo[e], rn);
+        st_shared_f32(c[e], __fadd_rn(q[e], rn));
+    }
+}
+
+// The table-driven form: row r of a circulant base row, gblk[e] and r4/Z4
+// as in qc_row_fixed, m_r the shared address of circulant 0's message of
+// row r (circulant e's is Z4 bytes further per e).
+template <int D>
+__device__ __forceinline__ void qc_row_edges_fixed(const int2* __restrict__ gblk, const uint32_t r4,
+                                                   const uint32_t Z4, const uint32_t m_r, const float scale,
+                                                   const float offset) {
+    uint32_t c[D], mo[D];
+#pragma unroll
+    for (int e = 0; e < D; ++e) {
+        const int2 b = gblk[e];
+        const uint32_t ce = r4 + static_cast<uint32_t>(b.x);
+        c[e] = ce >= static_cast<uint32_t>(b.y) ? ce - Z4 : ce;
+        mo[e] = m_r + static_cast<uint32_t>(e) * Z4;
+    }
+    qc_row_edges<D>(c, mo, scale, offset);
+}
+
+// Min-sum check-message state of one message per edge, in the group's
+// shared memory (R_SMEM only): circulant i of a circulant code keeps row
+// r's message at i Z + r, as sum-product does, so a warp's lanes
+// (consecutive r) touch consecutive words; r_stride messages (E rounded up
+// to 32) per frame.  Uncompressed, it is the reference's own message array:
+// the old message is a load rather than a select and a sign flip out of a
+// packed record, and no signs or argmin are packed back, which leaves about
+// half the ALU work per edge of the record form.  It takes E words against
+// the record's four per row, so it serves codes of a few thousand edges
+// (the plan offers it as CK_LDPC_PLACE_EDGES, for code-specialised
+// circulant decoders of rows up to 27 edges); the results are the same bits
+// as every other placement's.
+template <bool R_SMEM>
+struct EdgeMinSumState {
+    static_assert(R_SMEM, "the per-edge min-sum state lives in shared memory");
+    uint32_t m0;     // shared address of the frame slot's first message
+    uint32_t count;  // messages per frame slot
+
+    __device__ __forceinline__ EdgeMinSumState(const Params& p, unsigned char* gbase, uint32_t)
+        : m0(ck::smem_addr(gbase + p.r_off)), count(static_cast<uint32_t>(p.r_stride)) {}
+    // The mixed kernel's form: rsm the group's state region, r_stride its
+    // message count.
+    __device__ __forceinline__ EdgeMinSumState(unsigned char* rsm, uint32_t*, uint32_t, uint32_t r_stride,
+                                               int32_t)
+        : m0(ck::smem_addr(rsm)), count(r_stride) {}
+
+    __device__ __forceinline__ void zero(const Params&, int first, int stride) const {
+        zero_rows(0, first, stride);
+    }
+    __device__ __forceinline__ void zero_rows(int32_t, int first, int stride) const {
+        for (uint32_t i = static_cast<uint32_t>(first); i < count; i += static_cast<uint32_t>(stride))
+            st_shared_f32(m0 + 4u * i, 0.0f);
+    }
+    // Row r of the base row whose circulants are e0 .. e0 + deg of the table.
+    template <int DMAX>
+    __device__ __forceinline__ void qc_row(const Params& p, const int2* gblk, int deg, uint32_t row,
+                                           int32_t e0, int32_t, uint32_t r4, uint32_t Z4) const {
+        qc_row_k<DMAX>(gblk, deg, row, e0, r4, Z4, p.scale, p.offset);
+    }
+    template <int DMAX>
+    __device__ __forceinline__ void qc_row_k(const int2* gblk, int deg, uint32_t, int32_t e0, uint32_t r4,
+                                             uint32_t Z4, float scale, float offset) const {
+        static_assert(DMAX == 16 || DMAX == 27, "per-edge messages serve rows of up to 27 edges");
+        const uint32_t m_r = m0 + r4 + static_cast<uint32_t>(e0) * Z4;
+#define CK_EDGE_CASE(D) \
+    case D:             \
+        qc_row_edges_fixed<D>(gblk, r4, Z4, m_r, scale, offset); \
+        break;
+        switch (deg) {
+            CK_EDGE_CASE(2) CK_EDGE_CASE(3) CK_EDGE_CASE(4) CK_EDGE_CASE(5) CK_EDGE_CASE(6)
+            CK_EDGE_CASE(7) CK_EDGE_CASE(8) CK_EDGE_CASE(9) CK_EDGE_CASE(10) CK_EDGE_CASE(11)
+            CK_EDGE_CASE(12) CK_EDGE_CASE(13) CK_EDGE_CASE(14) CK_EDGE_CASE(15) CK_EDGE_CASE(16)
+            default:
+                break;
+        }
+        if constexpr (DMAX > 16) {
+            switch (deg) {
+                CK_EDGE_CASE(17) CK_EDGE_CASE(18) CK_EDGE_CASE(19) CK_EDGE_CASE(20) CK_EDGE_CASE(21)
+                CK_EDGE_CASE(22) CK_EDGE_CASE(23) CK_EDGE_CASE(24) CK_EDGE_CASE(25) CK_EDGE_CASE(26)
+                CK_EDGE_CASE(27)
+                default:
+                    break;
+            }
+        }
+#undef CK_EDGE_CASE
+    }
+    // The code-specialised programs' form: nothing to load ahead per row.
+    __device__ __forceinline__ uint4 pre(uint32_t) const { return make_uint4(0u, 0u, 0u, 0u); }
+    __device__ __forceinline__ uint4 take(const uint4, uint32_t) const { return make_uint4(0u, 0u, 0u, 0u); }
+    // One circulant row with its columns computed by the caller: mo4 = 4 (e0
+    // Z + r) for its first circulant e0 and row r, Z4 = 4 Z a constant.
+    template <int D, uint32_t Z4>
+    __device__ __forceinline__ void row_cols(const uint32_t (&c)[D], const uint4, uint32_t, uint32_t mo4,
+                                             float scale, float offset) const {
+        uint32_t mo[D];
+#pragma unroll
+        for (int e = 0; e < D; ++e) mo[e] = m0 + mo4 + static_cast<uint32_t>(e) * Z4;
+        qc_row_edges<D>(c, mo, scale, offset);
+    }
+    // Circulant codes only: the frame loop's CSR branch is compiled for every
+    // state but never runs with this one.
+    template <int DMAX, class ColOf>
+    __device__ __forceinline__ void csr_row(const Params&, float*, uint32_t, int, int32_t, const ColOf&) const {}
 };
 
 // The min-sum state of the kernels with row-degree bound DMAX: the packed
@@ -434,6 +589,15 @@ struct MinSumFor {
 template <bool R_SMEM>
 struct MinSumFor<0, R_SMEM> {
     using type = WideMinSumState<R_SMEM>;
+};
+// The same, or the per-edge state (EDGES).
+template <int DMAX, bool R_SMEM, bool EDGES>
+struct MinSumStateOf {
+    using type = typename MinSumFor<DMAX, R_SMEM>::type;
+};
+template <int DMAX, bool R_SMEM>
+struct MinSumStateOf<DMAX, R_SMEM, true> {
+    using type = EdgeMinSumState<true>;
 };
 
 

@@ -52,6 +52,9 @@ struct MixedCode {
     const int32_t* order;  // queue position -> frame, or null
     float scale, offset;
     int32_t max_iterations, early_stop;
+    // r_smem: where the message state lives: 0 device memory, 1 packed
+    // records in shared memory, 2 one message per edge in shared memory
+    // (set only for a code that runs its specialised program here).
     int32_t T, G, q_bstep, r_smem;
     uint32_t tables_bytes, group_bytes, gblk_off, app_off, r_off, r_stride;
     // Device-memory message state: block b's groups use the words
@@ -262,8 +265,9 @@ __device__ inline int mixed_pick(const MixedParams& p, int prefer) {
 
 // Decodes frames of code K with group g until K's queue is empty (ONE_ROW:
 // K.T >= K.Zp, one row per visited base row, as in decode_body; Prog: the
-// table-driven layer loop or the code's specialised program).
-template <int DMAX, bool R_SMEM, bool ONE_ROW, class Prog>
+// table-driven layer loop or the code's specialised program; EDGES: one
+// message per edge in shared memory, K.r_smem == 2).
+template <int DMAX, bool R_SMEM, bool ONE_ROW, class Prog, bool EDGES = false>
 __device__ __forceinline__ void mixed_frames(const MixedCode& K, unsigned char* smem, const int32_t* s_layer,
                              const int32_t* s_eptr, const int2* s_blk, const int g,
                              const int tid) {
@@ -273,7 +277,7 @@ __device__ __forceinline__ void mixed_frames(const MixedCode& K, unsigned char* 
     unsigned char* gbase = smem + K.tables_bytes + static_cast<uint32_t>(g) * K.group_bytes;
     volatile uint32_t* s_frame = reinterpret_cast<volatile uint32_t*>(gbase + 8);
     float* a = reinterpret_cast<float*>(gbase + K.app_off);
-    using State = typename MinSumFor<DMAX, R_SMEM>::type;
+    using State = typename MinSumStateOf<DMAX, R_SMEM, EDGES>::type;
     const State st(gbase + K.r_off, K.g_r + static_cast<size_t>(blockIdx.x) * K.block_words,
                    static_cast<uint32_t>(g), K.r_stride, K.sign_words);
     int2* gblk = reinterpret_cast<int2*>(gbase + K.gblk_off);
@@ -396,7 +400,7 @@ __device__ __forceinline__ void mixed_frames(const MixedCode& K, unsigned char* 
             auto do_row = [&](int32_t b, int32_t e0, int deg, int32_t r) {
                 const uint32_t row = static_cast<uint32_t>(b) * static_cast<uint32_t>(K.Z) +
                                      static_cast<uint32_t>(r);
-                st.template qc_row_k<DMAX>(gblk + e0, deg, row, r4 + 4u * static_cast<uint32_t>(r - qr0), Z4,
+                st.template qc_row_k<DMAX>(gblk + e0, deg, row, e0, r4 + 4u * static_cast<uint32_t>(r - qr0), Z4,
                                            K.scale, K.offset);
             };
             if constexpr (Prog::kSpecialised)

@@ -274,7 +274,7 @@ extern "C" int ck_ldpc_specialised_source(const int32_t* row_ptr, const int32_t*
                                           int32_t form, char* out, size_t capacity, size_t* length) {
     ck::clear_error();
     if (!length) return ck::fail(CK_ERR_INVALID_ARGUMENT, "length is NULL");
-    if (form < 0 || form > 2) return ck::fail(CK_ERR_INVALID_ARGUMENT, "form must be 0, 1 or 2");
+    if (form < 0 || form > 3) return ck::fail(CK_ERR_INVALID_ARGUMENT, "form must be 0, 1, 2 or 3");
     ck_ldpc_plan plan;
     CK_TRY(plan_host(row_ptr, cols, layer_ptr, m, N, L, &plan));
     if (!plan.qc) return ck::fail(CK_ERR_UNSUPPORTED, "the schedule has no circulant structure");
@@ -284,9 +284,10 @@ extern "C" int ck_ldpc_specialised_source(const int32_t* row_ptr, const int32_t*
                         "which have no code-specialised form", plan.max_deg, ck::ldpc::kPackedDegree);
     const int dmax = ck::ldpc::kernel_dmax(true, plan.max_deg);
     const ck_ldpc_plan* plans[1] = {&plan};
-    const int parts[1] = {form};  // form 1: one thread per row slot, 2: two
-    const std::string src =
-        form == 0 ? ck::ldpc::specialised_source(plan, dmax) : ck::ldpc::mixed_source(plans, parts, 1, dmax);
+    const int parts[1] = {form == 2 ? 2 : 1};  // form 2: two threads per row slot, else one
+    const int edges[1] = {form == 3 ? 1 : 0};  // form 3: one message per edge in shared memory
+    const std::string src = form == 0 ? ck::ldpc::specialised_source(plan, dmax)
+                                      : ck::ldpc::mixed_source(plans, parts, edges, 1, dmax);
     *length = src.size();
     if (out && capacity > 0) {
         const size_t n = std::min(capacity - 1, src.size());
@@ -340,6 +341,8 @@ extern "C" int ck_ldpc_plan_set_launch(ck_ldpc_plan* plan, const ck_ldpc_launch*
         return ck::fail(CK_ERR_INVALID_ARGUMENT,
                         "at most %d multi-warp frames per block (named barriers)",
                         ck::kMaxNamedGroups);
+    if (launch->placement < CK_LDPC_PLACE_AUTO || launch->placement > CK_LDPC_PLACE_EDGES)
+        return ck::fail(CK_ERR_INVALID_ARGUMENT, "unknown placement %d", launch->placement);
     plan->launch = *launch;
     return CK_OK;
 }

@@ -106,6 +106,10 @@ def candidates(plan_info: dict) -> list[tuple[int, int, int]]:
         for g in (0, 1, 2, 4, 8, 12):
             for place in (_lib.CK_LDPC_PLACE_SHARED, _lib.CK_LDPC_PLACE_GLOBAL):
                 shapes.add((t, g, place))
+            # One message per edge: the code-specialised kernel with one
+            # thread per row slot (other shapes would run the records).
+            if plan_info["quasi_cyclic"] and t == zp:
+                shapes.add((t, g, _lib.CK_LDPC_PLACE_EDGES))
     return sorted(shapes)
 
 

@@ -323,11 +323,25 @@ typedef struct ck_ldpc_launch {
     int32_t placement; /* CK_LDPC_PLACE_*: where the check-message state lives */
 } ck_ldpc_launch;
 
-#define CK_LDPC_PLACE_AUTO 0   /* the plan chooses */
+#define CK_LDPC_PLACE_AUTO 0   /* the plan chooses: EDGES where two frames fit, else SHARED where two fit,
+                                  else GLOBAL */
 #define CK_LDPC_PLACE_SHARED 1 /* shared memory, beside the frame's LLRs */
 #define CK_LDPC_PLACE_GLOBAL 2 /* device memory (L2-resident working set) */
+/* One uncompressed message per edge in shared memory (min-sum decoders
+ * of circulant codes with rows up to 27 edges, code-specialised, with one
+ * thread per row slot, whose frames' messages fit; other decodes with it
+ * keep the records as SHARED). */
+#define CK_LDPC_PLACE_EDGES 3
 int ck_ldpc_plan_set_launch(ck_ldpc_plan* plan, const ck_ldpc_launch* launch);
 int ck_ldpc_plan_get_launch(const ck_ldpc_plan* plan, ck_ldpc_launch* launch);
+/*
+ * The shape a plain decode by `rule` (CK_LDPC_MIN_SUM / CK_LDPC_SUM_PRODUCT)
+ * runs with under the current setting, resolved (and its code-specialised
+ * kernel compiled, when it has one): threads per frame, frames per block
+ * and the placement actually used (SHARED, GLOBAL or EDGES, never AUTO).
+ * The plan's device must be current.  No reference counterpart.
+ */
+int ck_ldpc_plan_resolved_launch(const ck_ldpc_plan* plan, int32_t rule, ck_ldpc_launch* launch);
 
 /*
  * Code-specialised min-sum decoding of a circulant code (no reference
@@ -351,8 +365,10 @@ int ck_ldpc_plan_get_specialise(const ck_ldpc_plan* plan, int32_t* mode, int32_t
 /*
  * The CUDA source a plan of this schedule would compile for its
  * code-specialised kernels (host only, no device needed): form 0 the plain
- * decoder, form 1 a mixed decoder of this code alone, form 2 the same with
- * two threads per row slot (threads per frame 2 Zp).  *length gets its
+ * decoder (one kernel per placement), form 1 a mixed decoder of this code
+ * alone, form 2 the same with two threads per row slot (threads per frame
+ * 2 Zp), form 3 form 1 with one message per edge in shared memory
+ * (CK_LDPC_PLACE_EDGES).  *length gets its
  * size, and up to capacity - 1 bytes of it go to `out` (NUL-terminated).
  * CK_ERR_UNSUPPORTED when the schedule is not circulant.
  */

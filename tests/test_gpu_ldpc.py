@@ -95,12 +95,14 @@ def test_nonfinite_llrs(golden_ldpc, torch_dev, ck, which, early_stop):
 
 
 @pytest.mark.parametrize("name,frames,order", [("A", 600, 4), ("B", 400, 16), ("C", 160, 16)])
-@pytest.mark.parametrize("placement", [1, 2])
+@pytest.mark.parametrize("placement", [1, 2, 3])
 def test_specialised_kernel_equals_table_kernel(torch_dev, ck, name, frames, order, placement):
     """The code-specialised kernel (compiled at run time) against the
     table-driven kernel on the same frames, message state in shared (1;
     code C's does not fit there and stays in device memory) or device (2)
-    memory: every output bit for bit; and against the oracle."""
+    memory, or one message per edge in shared memory (3: codes A and B; the
+    table kernel and code C keep the records): every output bit for bit;
+    and against the oracle."""
     from commkit_gb300 import _lib
 
     torch, dev = torch_dev
@@ -118,6 +120,9 @@ def test_specialised_kernel_equals_table_kernel(torch_dev, ck, name, frames, ord
     got = [_to_np(ck.decode(llr, code=c, method=method), frames) for c in codes]
     assert codes[0]._plan(0).specialisation()[1] == 1, codes[0]._plan(0).specialisation()
     assert codes[1]._plan(0).specialisation()[1] == 0
+    if placement == _lib.CK_LDPC_PLACE_EDGES:
+        used = codes[0]._plan(0).resolved_launch()[2], codes[1]._plan(0).resolved_launch()[2]
+        assert used == ((3, 1) if name != "C" else (2, 2)), used
     _assert_same(got[0], got[1])
     assert 0 < np.mean(got[0][3]) < 30  # frames stop at different iterations
     _assert_same(got[0], _oracle(codes[0], llr.cpu().numpy(), max_iterations=30))
@@ -267,7 +272,7 @@ def test_launch_shapes_do_not_change_results(torch_dev, ck, name):
     plan = code._plan(0)
     base = _to_np(ck.decode(llr, code=code, method=method), frames)
     _assert_same(base, _oracle(code, llr.cpu().numpy(), max_iterations=12))
-    shapes = [(32, 1, 0), (32, 3, 0), (64, 2, 1), (128, 1, 2), (256, 2, 0), (512, 1, 2)]
+    shapes = [(32, 1, 0), (32, 3, 0), (64, 2, 1), (128, 1, 2), (256, 2, 0), (512, 1, 2), (64, 0, 3), (384, 1, 3)]
     try:
         for T, G, place in shapes:
             try:

@@ -22,7 +22,7 @@ def _batch(ck, dev, name, frames, order, ebn0, seed):
     return code, llr
 
 
-@pytest.mark.parametrize("placement", [0, 2])
+@pytest.mark.parametrize("placement", [0, 2, 3])
 @pytest.mark.parametrize("specialise,parts", [("table_plain", 1), ("both_auto", 1), ("both_auto", 2)])
 def test_mixed_launch_matches_plain_calls(placement, specialise, parts):
     """table_plain: plain calls on the table-driven kernel, the mixed launch

@@ -80,7 +80,8 @@ def test_specialised_source_compiles(name):
     bodies = src.count("st.template row_cols<")
     assert bodies > 0 and m % bodies == 0
     assert src.count("ck::group_sync(bar, T);") == sched[2].size - 1
-    assert "ck_ldpc_code_r0" in src and "ck_ldpc_code_r1" in src
+    assert "ck_ldpc_code_r0" in src and "ck_ldpc_code_r1" in src and "ck_ldpc_code_r2" in src
+    assert "decode_body<EdgeMinSumState" in src
     st, log = compile_nvrtc(src)
     assert st == 0, log[:3000]
     mixed = source(*sched, m, n, form=1)
@@ -91,6 +92,11 @@ def test_specialised_source_compiles(name):
     split = source(*sched, m, n, form=2)
     assert "kParts = 2" in split and split.count("st.template row_cols<") == bodies
     st, log = compile_nvrtc(split)
+    assert st == 0, log[:3000]
+    # One message per edge in shared memory (CK_LDPC_PLACE_EDGES).
+    edges = source(*sched, m, n, form=3)
+    assert ", true>(K, smem" in edges and "if (K.r_smem)" not in edges
+    st, log = compile_nvrtc(edges)
     assert st == 0, log[:3000]
 
 

@@ -18,6 +18,11 @@ def test_candidates_respect_the_lifting():
     shapes = tuning.candidates({"quasi_cyclic": 1, "lifting": 54})  # padded to 64
     assert {t for t, _, _ in shapes} == {32, 64, 128}
     assert {t for t, _, _ in tuning.candidates({"quasi_cyclic": 0, "lifting": 0})} == {32, 64, 128, 256, 512}
+    # One message per edge only with one thread per row slot (the specialised kernel), circulant codes only.
+    from commkit_gb300 import _lib
+
+    assert {t for t, _, p in shapes if p == _lib.CK_LDPC_PLACE_EDGES} == {64}
+    assert not any(p == _lib.CK_LDPC_PLACE_EDGES for _, _, p in tuning.candidates({"quasi_cyclic": 0, "lifting": 0}))
 
 
 def test_cache_roundtrip_and_key(tmp_path, monkeypatch):
