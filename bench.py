@@ -76,7 +76,8 @@ WORKLOADS = {
     "served": dict(max_it=50,
                    desc="served stream: Poisson arrivals of 1-256 frames (log-uniform), codes A/B/C 50/35/15 "
                         "on QPSK/16-QAM/64-QAM, Es/N0 near each waterfall, MinSum 50 it, 4 GiB admission "
-                        "budget over 12 batch slots, load 10-100% of measured saturation"),
+                        "budget over 12 batch slots, load 10-100% of measured saturation, each level three "
+                        "independent 1 s streams (the median of their percentiles)"),
 }  # fmt: skip
 
 
@@ -1096,28 +1097,18 @@ def measure_served(args, dist: Dist) -> dict:
     sat_s = time.perf_counter() - t0
     sat_rate = len(over) / sat_s
     backlog = over
-    duration = float(os.environ.get("CK_SERVE_SECONDS", "1.5"))
+    duration = float(os.environ.get("CK_SERVE_SECONDS", "1.0"))
+    reps = int(os.environ.get("CK_SERVE_REPS", "3"))
     sweep = {}
     with Clocks(dev.index) as clk:
         for load in (0.1, 0.3, 0.5, 0.7, 0.9, 1.0):
-            reqs = poisson_requests(load * sat_rate, duration, pool, seed=int(load * 100))
-            t0 = time.perf_counter()
-            done = server.serve(reqs)
-            wall = time.perf_counter() - t0
-            lat = np.array([r.latency for r in done]) * 1e3
-            sweep[f"{int(round(load * 100))}%"] = {
-                "requests": len(done), "frames": int(sum(r.frames for r in done)),
-                "gbps": info_bits(done) / wall / 1e9, "p50_ms": float(np.percentile(lat, 50)),
-                "p99_ms": float(np.percentile(lat, 99)), "p999_ms": float(np.percentile(lat, 99.9)),
-                "max_ms": float(lat.max()),
-                "p99_ms_by_code": {c: float(np.percentile([r.latency * 1e3 for r in done if r.code == c], 99))
-                                   for c in "ABC" if any(r.code == c for r in done)},
-                # Time from arrival to admission into a batch slot: the queueing part of the latency.
-                "p99_wait_ms": float(np.percentile([(r.admitted - r.arrival) * 1e3 for r in done], 99)),
-                "p99_wait_ms_by_code": {c: float(np.percentile([(r.admitted - r.arrival) * 1e3 for r in done
-                                                                if r.code == c], 99))
-                                        for c in "ABC" if any(r.code == c for r in done)},
-            }  # fmt: skip
+            runs = []
+            for rep in range(reps):
+                reqs = poisson_requests(load * sat_rate, duration, pool, seed=int(load * 100) + 1000 * rep)
+                t0 = time.perf_counter()
+                done = server.serve(reqs)
+                runs.append((done, time.perf_counter() - t0))
+            sweep[f"{int(round(load * 100))}%"] = _load_level(runs, info_bits, waits=True)
     feed = {policy: measure_feed(codes, pool, sat_rate, duration, info_bits, dev, policy)
             for policy in ("oldest", "short_first")}
     return {
@@ -1133,13 +1124,40 @@ def measure_served(args, dist: Dist) -> dict:
     }  # fmt: skip
 
 
-def _latency_summary(done, wall: float, info_bits) -> dict:
+def _latency_summary(done, wall: float, info_bits, waits: bool = False) -> dict:
     lat = np.array([r.latency for r in done]) * 1e3
-    return {"requests": len(done), "frames": int(sum(r.frames for r in done)),
-            "gbps": info_bits(done) / wall / 1e9, "p50_ms": float(np.percentile(lat, 50)),
-            "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()),
-            "p99_ms_by_code": {c: float(np.percentile([r.latency * 1e3 for r in done if r.code == c], 99))
-                               for c in "ABC" if any(r.code == c for r in done)}}  # fmt: skip
+    out = {"requests": len(done), "frames": int(sum(r.frames for r in done)),
+           "gbps": info_bits(done) / wall / 1e9, "p50_ms": float(np.percentile(lat, 50)),
+           "p99_ms": float(np.percentile(lat, 99)), "p999_ms": float(np.percentile(lat, 99.9)),
+           "max_ms": float(lat.max()),
+           "p99_ms_by_code": {c: float(np.percentile([r.latency * 1e3 for r in done if r.code == c], 99))
+                              for c in "ABC" if any(r.code == c for r in done)}}  # fmt: skip
+    if waits:
+        # Time from arrival to admission into a batch slot: the queueing part of the latency.
+        out["p99_wait_ms"] = float(np.percentile([(r.admitted - r.arrival) * 1e3 for r in done], 99))
+        out["p99_wait_ms_by_code"] = {c: float(np.percentile([(r.admitted - r.arrival) * 1e3 for r in done
+                                                              if r.code == c], 99))
+                                      for c in "ABC" if any(r.code == c for r in done)}  # fmt: skip
+    return out
+
+
+def _load_level(runs, info_bits, waits: bool = False) -> dict:
+    """One load level measured as independent request streams (different
+    seeds) served one after another: each stream's percentiles, and their
+    median as the level's figure, so a single host stall of a few
+    milliseconds in one stream (seen now and then on the GPU machine, cause
+    unknown) shows in that stream's entry instead of deciding the level."""
+    per = [_latency_summary(done, wall, info_bits, waits) for done, wall in runs]
+    med = {k: float(np.median([p[k] for p in per])) for k in per[0] if isinstance(per[0][k], float)}
+    med.update(requests=int(sum(p["requests"] for p in per)), frames=int(sum(p["frames"] for p in per)),
+               gbps=float(sum(info_bits(d) for d, _ in runs) / sum(w for _, w in runs) / 1e9))  # fmt: skip
+    for key in ("p99_ms_by_code", "p99_wait_ms_by_code"):
+        if key in per[0]:
+            med[key] = {c: float(np.median([p[key][c] for p in per if c in p[key]])) for c in per[0][key]}
+    med["streams"] = len(per)
+    med["p99_ms_each"] = [p["p99_ms"] for p in per]
+    med["max_ms_each"] = [p["max_ms"] for p in per]
+    return med
 
 
 def measure_feed(codes, pool, sat_rate: float, duration: float, info_bits, dev, policy: str) -> dict:
@@ -1158,12 +1176,16 @@ def measure_feed(codes, pool, sat_rate: float, duration: float, info_bits, dev, 
     done = server.serve(over)
     sat_s = time.perf_counter() - t0
     sweep = {}
+    reps = int(os.environ.get("CK_SERVE_REPS", "3"))
     with Clocks(dev.index) as clk:
         for load in (0.1, 0.3, 0.5, 0.7, 0.9):
-            reqs = poisson_requests(load * sat_rate, duration, pool, seed=int(load * 100))
-            t0 = time.perf_counter()
-            got = server.serve(reqs)
-            sweep[f"{int(round(load * 100))}%"] = _latency_summary(got, time.perf_counter() - t0, info_bits)
+            runs = []
+            for rep in range(reps):
+                reqs = poisson_requests(load * sat_rate, duration, pool, seed=int(load * 100) + 1000 * rep)
+                t0 = time.perf_counter()
+                got = server.serve(reqs)
+                runs.append((got, time.perf_counter() - t0))
+            sweep[f"{int(round(load * 100))}%"] = _load_level(runs, info_bits)
     launches = server.launches
     server.close()
     return {"what": "one persistent decoder fed from pinned descriptor rings (ck_ldpc_feed_launch); loads are "
