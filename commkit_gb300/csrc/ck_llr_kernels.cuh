@@ -83,6 +83,7 @@ struct LevelAxis {
     // then the halves of every bit are known at compile time.
     alignas(16) float2 lp[L];
     int32_t gray;
+    alignas(8) float nz[2];  // (-0, -0): the addend of the two-lane products (mul2z)
 };
 
 __device__ __forceinline__ float2 lds2(uint32_t addr) {
@@ -288,8 +289,14 @@ __device__ __forceinline__ void axis_exact(float x, const LevelAxis<KA>& t, floa
 
 // Packed pairs of floats for the FMA pipe's two-lane forms (add, sub, mul,
 // fma .rn.f32x2, sm_100 and later): each lane rounds as the scalar _rn
-// operation does, so results are bit for bit those of two scalar ops, at
-// half the instruction count.
+// operation does, at half the instruction count.  One catch, measured on
+// GB300: a two-lane product that feeds a two-lane addition is contracted
+// into one fused multiply-add by the assembler (mul.rn.f32x2 then
+// add.rn.f32x2 differed from the scalar _rn chain in 27 % of random cases,
+// every operation alone matched), and an fma with a constant -0 addend is
+// treated the same way.  mul2z is the product that stays rounded: an fma
+// whose -0 addend comes from memory (nz, loaded from shared memory), which
+// the assembler cannot fold away; use it wherever a product is added to.
 __device__ __forceinline__ uint64_t pk2(float lo, float hi) {
     uint64_t r;
     asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
@@ -317,6 +324,16 @@ __device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
     uint64_t r;
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
     return r;
+}
+// a * b rounded once, as mul.rn would give it, for a product that is then
+// added to: nz is the pair (-0, -0) loaded from memory (see above).
+__device__ __forceinline__ uint64_t mul2z(uint64_t a, uint64_t b, uint64_t nz) { return fma2(a, b, nz); }
+// The pair (-0, -0) at a shared address, loaded so that the compiler does
+// not know its value.
+__device__ __forceinline__ uint64_t lds_nz(uint32_t addr) {
+    uint64_t v;
+    asm volatile("ld.shared.b64 %0, [%1];" : "=l"(v) : "r"(addr));
+    return v;
 }
 
 // exp_split of two arguments, its multiply-adds in the two-lane forms: the
@@ -358,11 +375,12 @@ __device__ __forceinline__ void axis_exact_gray(float x, const LevelAxis<KA>& t,
     // rounded as the scalar steps (-(d*d) times s2 is d*d times -s2).
     float m[L];
     const uint64_t x2 = pk2(x, x), ns2 = pk2(-inv_s2, -inv_s2);
+    const uint64_t nz = lds_nz(ck::smem_addr(&t.nz[0]));
 #pragma unroll
     for (int j = 0; j < L; j += 2) {
         const float4 v = lds4(base + 8u * static_cast<uint32_t>(j));  // (lev j, logp j, lev j+1, logp j+1)
         const uint64_t d = sub2(x2, pk2(v.x, v.z));
-        upk2(add2(mul2(mul2(d, d), ns2), pk2(v.y, v.w)), m[j], m[j + 1]);
+        upk2(add2(mul2z(mul2(d, d), ns2, nz), pk2(v.y, v.w)), m[j], m[j + 1]);
     }
     float peak = m[0];
 #pragma unroll
@@ -439,6 +457,7 @@ __device__ __forceinline__ void load_level_axis(LevelAxis<KA>& t, const ck_axis_
         int32_t g = 1;
         for (int j = 0; j < L; ++j) g &= a.labels[j] == (j ^ (j >> 1)) ? 1 : 0;
         t.gray = g;
+        t.nz[0] = t.nz[1] = -0.0f;
     }
     for (int i = threadIdx.x; i < KA; i += blockDim.x) {
         t.pos[i] = a.pos[i];

@@ -15,7 +15,7 @@ int launch_points(const float2* x, uint32_t n, const Table& t, const NoiseScale&
         kernel = exact ? llr_points_kernel<K, true, true> : llr_points_kernel<K, false, true>;
     else
         kernel = exact ? llr_points_kernel<K, true, false> : llr_points_kernel<K, false, false>;
-    const int bytes = kSmem ? static_cast<int>(smem_bytes(K)) : 0;
+    const int bytes = kSmem ? static_cast<int>(smem_bytes(K, exact)) : 0;
     // Shared-memory opt-in and occupancy, once per device and method (the
     // writes are idempotent, so concurrent first calls are harmless).
     static int per_sm_cache[2][kMaxDevices] = {};
@@ -31,7 +31,9 @@ int launch_points(const float2* x, uint32_t n, const Table& t, const NoiseScale&
         if (per_sm < 1) return ck::fail(CK_ERR_UNSUPPORTED, "M-point LLR block does not fit an SM");
         if (dev < kMaxDevices) per_sm_cache[exact][dev] = per_sm;
     }
-    const uint32_t want = (n + kThreads - 1) / kThreads;
+    // Staged tables run two symbols per thread and step for the exact method.
+    const uint32_t units = kSmem && exact ? n / 2 + (n & 1u) : n;
+    const uint32_t want = (units + kThreads - 1) / kThreads;
     const uint32_t cap = static_cast<uint32_t>(num_sms()) * static_cast<uint32_t>(per_sm);
     const uint32_t blocks = want < cap ? (want > 0 ? want : 1) : cap;
     const bool vec = reinterpret_cast<uintptr_t>(out) % 16 == 0;
