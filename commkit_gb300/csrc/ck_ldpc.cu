@@ -167,7 +167,7 @@ int resolve(const ck_ldpc_plan* plan, int32_t rule, int64_t B, Resolved* r, bool
             c.valid = true;
         }
     }
-    const int32_t G = r->G;
+    int32_t G = r->G;
     r->cluster = 1;
     size_t slots;
     if (r->cluster_kernel && B * 2 <= int64_t(sms) * r->cluster_per_sm) {
@@ -195,6 +195,19 @@ int resolve(const ck_ldpc_plan* plan, int32_t rule, int64_t B, Resolved* r, bool
                 r->cluster = c;
                 break;
             }
+        }
+    }
+    if (r->cluster <= 1 && B > 0 && B < int64_t(sms) * per_sm * G) {
+        // Less than one resident wave: spread the frames over every resident
+        // block (fewer frame groups per block, the same kernel) instead of
+        // filling the first blocks and leaving SMs idle.  Any shape gives the
+        // same bits.
+        const int64_t blocks = int64_t(sms) * per_sm;
+        const int32_t g2 = static_cast<int32_t>((B + blocks - 1) / blocks);
+        if (g2 >= 1 && g2 < G) {
+            G = g2;
+            r->G = g2;
+            r->smem = r->tables_bytes + static_cast<uint32_t>(g2) * r->group_bytes;
         }
     }
     const int64_t need = (B + G - 1) / G;
@@ -925,7 +938,7 @@ extern "C" int ck_ldpc_plan_resolved_launch(const ck_ldpc_plan* plan, int32_t ru
         return ck::fail(CK_ERR_INVALID_ARGUMENT, "plan is for device %d, current device is %d", plan->device,
                         device);
     Resolved r;
-    CK_TRY(resolve(plan, rule, 1, &r));
+    CK_TRY(resolve(plan, rule, int64_t(1) << 40, &r));  // a full batch: the shape before any spreading of a short one
     out->threads_per_frame = r.T;
     out->frames_per_block = r.G;
     out->placement = !r.r_smem ? CK_LDPC_PLACE_GLOBAL : (r.edges ? CK_LDPC_PLACE_EDGES : CK_LDPC_PLACE_SHARED);

@@ -263,9 +263,10 @@ __device__ __noinline__ float half_log_sum(const float4* __restrict__ ri, const 
 // reference's factories build), so label order is the reference's point
 // order (commkit/mapping/_numba_llr.py:35-81): each symbol's peak metric
 // first, then each half-sum adds e = exp(m - peak) point by point in that
-// order, as the reference does.  Within a chunk of up to 16 labels their low
-// four bits are compile-time, so each addition goes straight to its half
-// (no test of the label's bits); the higher bits are one branch per chunk.
+// order, as the reference does.  Within a chunk (all labels up to 16, else 8
+// at a time, which holds fewer registers) the labels' low bits are
+// compile-time, so each addition goes straight to its half (no test of the
+// label's bits); the higher bits are one branch per chunk.
 // The metrics, the exponent arguments, the exponential's multiply-adds and
 // the additions run in the FMA pipe's two-lane forms, each lane rounding as
 // the scalar operation.  e is exp_split (a few ulp, as in the separable
@@ -278,7 +279,7 @@ __device__ __noinline__ float half_log_sum(const float4* __restrict__ ri, const 
 template <int K>
 __device__ __forceinline__ void exact_sorted2(const float4* __restrict__ ri, const float2* __restrict__ lp, uint64_t NZ,
                                               float2 xa, float2 xb, float sa, float sb, float* oa, float* ob) {
-    constexpr int R = K < 4 ? K : 4;
+    constexpr int R = K <= 4 ? K : 3;  // one chunk up to 16 labels, else chunks of 8 (fewer registers)
     constexpr int C = 1 << R;
     constexpr int L = 1 << K;
     const uint64_t X = pk2(xa.x, xb.x), Y = pk2(xa.y, xb.y), NS2 = pk2(-sa, -sb);
