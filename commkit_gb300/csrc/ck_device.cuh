@@ -180,6 +180,26 @@ __device__ __forceinline__ uint64_t ld_relaxed_sys_u64(const void* p) {
 }
 
 // The global nanosecond timer (for waits bounded in wall time).
+// Stores of data a kernel keeps re-reading from L2 (the decoder's
+// device-memory message state: written and read back once per iteration)
+// with the L2 eviction priority "evict last", so that streams passing
+// through L2 (frames loaded, posteriors written) are evicted before it and
+// it is not written back to DRAM between iterations.  L1 is bypassed (.cg),
+// as with __stcg.  Volatile and clobbering memory: kept in order with the
+// barriers and with the other accesses.
+__device__ __forceinline__ uint64_t l2_keep_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ void st_l2keep(uint2* p, uint2 v, uint64_t pol) {
+    asm volatile("st.global.cg.L2::cache_hint.v2.u32 [%0], {%1, %2}, %3;" ::"l"(p), "r"(v.x), "r"(v.y), "l"(pol)
+                 : "memory");
+}
+__device__ __forceinline__ void st_l2keep(uint32_t* p, uint32_t v, uint64_t pol) {
+    asm volatile("st.global.cg.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
+}
+
 __device__ __forceinline__ uint64_t globaltimer_ns() {
     uint64_t t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
