@@ -14,6 +14,7 @@ raises ``TypeError``.
 from __future__ import annotations
 
 import ctypes
+import logging
 import warnings
 from dataclasses import dataclass
 from functools import cached_property
@@ -23,6 +24,8 @@ import numpy as np
 
 from . import _device, _lib
 from .mapping import PrecisionWarning
+
+_log = logging.getLogger(__name__)
 
 __all__ = ["DecodeResult", "LDPCCode", "MinSum", "SumProduct", "decode", "decode_mixed", "encode"]
 
@@ -132,22 +135,44 @@ class LDPCCode:
             raise ValueError("base must be a non-empty 2-D integer matrix.")
         if b.min() < -1:
             raise ValueError("base entries must be shifts >= 0 or -1.")
-        bi, bj = np.nonzero(b >= 0)
-        r = np.arange(z)
-        rows = (bi[:, None] * z + r).ravel()
-        cols = (bj[:, None] * z + (r + b[bi, bj][:, None]) % z).ravel()
-        return cls(rows, cols, b.shape[0] * z, b.shape[1] * z, punctured)
+        # One edge per (nonzero block, row within it): block (i, j) of shift s
+        # links check i z + t to variable j z + (t + s) mod z, t = 0 .. z - 1.
+        blocks = np.argwhere(b >= 0)
+        t = np.tile(np.arange(z), len(blocks))
+        shift = np.repeat(b[blocks[:, 0], blocks[:, 1]], z)
+        checks = np.repeat(blocks[:, 0] * z, z) + t
+        variables = np.repeat(blocks[:, 1] * z, z) + (t + shift) % z
+        code = cls(checks, variables, b.shape[0] * z, b.shape[1] * z, punctured)
+        _warn_if_4_cycles(code)
+        return code
 
     @classmethod
     def from_parity_check(cls, h: Any, *, punctured: int = 0) -> LDPCCode:
-        """The code of a dense 0/1 parity-check matrix ``(m, N)``."""
-        h = np.asarray(h)
-        if h.ndim != 2:
-            raise ValueError(f"parity_check must be 2-D, got {h.ndim}-D.")
-        if np.any((h != 0) & (h != 1)):
-            raise ValueError("parity_check must contain only 0 and 1.")
-        rows, cols = np.nonzero(h)
-        return cls(rows, cols, h.shape[0], h.shape[1], punctured)
+        """The code of a 0/1 parity-check matrix ``(m, N)``, dense or SciPy
+        sparse (``ldpc.py:146-181``); logs a warning when two checks share
+        two bits (a 4-cycle)."""
+        import scipy.sparse
+
+        if scipy.sparse.issparse(h):
+            if h.ndim != 2:
+                raise ValueError(f"parity_check must be 2-D, got {h.ndim}-D.")
+            coo = scipy.sparse.coo_array(h)
+            coo.sum_duplicates()
+            coo.eliminate_zeros()
+            if np.any(coo.data != 1):
+                raise ValueError("parity_check must contain only 0 and 1.")
+            rows, cols, shape = coo.row, coo.col, coo.shape
+        else:
+            h = np.asarray(h)
+            if h.ndim != 2:
+                raise ValueError(f"parity_check must be 2-D, got {h.ndim}-D.")
+            if np.any((h != 0) & (h != 1)):
+                raise ValueError("parity_check must contain only 0 and 1.")
+            rows, cols = np.nonzero(h)
+            shape = h.shape
+        code = cls(rows, cols, shape[0], shape[1], punctured)
+        _warn_if_4_cycles(code)
+        return code
 
     @property
     def n(self) -> int:
@@ -655,6 +680,20 @@ def _decode_torch(llrs: Any, x0: _device.DeviceArray, code: LDPCCode, method: Mi
                 )  # fmt: skip
             _lib.check(st, "decode()")
     return DecodeResult(bits=bits, llrs=out_llrs, valid=valid, iterations=iters, checked=True)
+
+
+def _warn_if_4_cycles(code: LDPCCode) -> None:
+    """Logs a warning when two checks share two or more bits, a 4-cycle of
+    the Tanner graph on which belief propagation degrades, as the reference
+    does when it builds a code (``ldpc.py:415-419``): the off-diagonal
+    entries of H H^T count the bits each pair of checks shares."""
+    import scipy.sparse
+
+    h = scipy.sparse.csr_array((np.ones(code.checks.size, np.int32), (code.checks, code.variables)),
+                               shape=(code.num_checks, code.num_variables))  # fmt: skip
+    shared = (h @ h.T).tocoo()
+    if np.any(shared.data[shared.row != shared.col] > 1):
+        _log.warning("%r has 4-cycles; belief propagation degrades on them.", code)
 
 
 def _encoder_tables(code: LDPCCode, like: _device.DeviceArray) -> tuple:

@@ -215,3 +215,28 @@ def test_fastdiv_exhaustive_on_host():
         hi = (n * np.uint64(mul)) >> np.uint64(32)
         q = (hi + n) >> np.uint64(sh)
         np.testing.assert_array_equal(q, n // np.uint64(d))
+
+
+def test_four_cycle_warning_and_sparse_parity_check(caplog):
+    """``LDPCCode.from_parity_check`` takes dense or SciPy sparse 0/1
+    matrices and, like ``quasi_cyclic``, logs a warning when two checks
+    share two bits (``commkit/coding/ldpc.py:146-181, 415-419``)."""
+    import logging
+
+    import scipy.sparse
+
+    from commkit_gb300.coding import LDPCCode
+
+    cyc = np.array([[1, 1, 1, 0], [1, 1, 0, 1], [0, 0, 1, 1]])  # checks 0 and 1 share bits 0 and 1
+    tree = np.array([[1, 1, 0, 0], [0, 1, 1, 0], [0, 0, 1, 1]])
+    with caplog.at_level(logging.WARNING, logger="commkit_gb300.coding"):
+        a = LDPCCode.from_parity_check(cyc)
+        assert any("4-cycles" in r.getMessage() for r in caplog.records)
+        caplog.clear()
+        b = LDPCCode.from_parity_check(scipy.sparse.csr_array(tree))
+        assert not any("4-cycles" in r.getMessage() for r in caplog.records)
+    assert (a.num_checks, a.num_variables) == (3, 4)
+    c = LDPCCode.from_parity_check(tree)
+    assert np.array_equal(b._schedule[1], c._schedule[1]) and b.k == c.k
+    with pytest.raises(ValueError, match="only 0 and 1"):
+        LDPCCode.from_parity_check(scipy.sparse.csr_array(2 * tree))
