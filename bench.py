@@ -81,13 +81,13 @@ WORKLOADS = {
 }  # fmt: skip
 
 
-# DRAM traffic of the mixed decoder (the code-specialised kernel), dram__bytes_read.sum +
-# dram__bytes_write.sum from one ncu capture (--set full) of a 2048-frame batch of the same mix on
-# GB300: 33.62 + 34.59 MB.  It grows with the frames, so a launch's traffic is scaled by its frame
-# count.
-MIXED_DRAM_BYTES_PER_FRAME = (20.135936e6 + 26.017792e6) / 2048
+# DRAM traffic of the mixed decoder (the code-specialised kernel, codes A and B with one message
+# per edge), dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture (--set full) of a
+# 2048-frame batch of the same mix on GB300: 20.16 + 24.91 MB.  It grows with the frames, so a
+# launch's traffic is scaled by its frame count.
+MIXED_DRAM_BYTES_PER_FRAME = (20.157184e6 + 24.912128e6) / 2048
 MIXED_TRAFFIC_NOTE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of a 2048-frame launch of the same mix "
-                      "(fused demapping), scaled by frames (46.2 MB / 2048 frames)")
+                      "(fused demapping), scaled by frames (45.1 MB / 2048 frames)")
 
 
 def parse() -> argparse.Namespace:
