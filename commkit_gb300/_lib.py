@@ -8,11 +8,16 @@ device function of the package fails with it.
 from __future__ import annotations
 
 import ctypes
+import os
+import sysconfig
 import threading
+import warnings
 from pathlib import Path
 
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "_lib" / "libck_gb300.so"
+# The per-call extension (csrc/python/ck_calls.cpp), built beside the library.
+CALLS_PATH = _PKG / "_lib" / ("ck_calls" + (sysconfig.get_config_var("EXT_SUFFIX") or ".so"))
 
 CK_OK = 0
 CK_ERR_INVALID_ARGUMENT = 1
@@ -259,6 +264,50 @@ def lib() -> ctypes.CDLL:
                 _declare(handle)
                 _lib = handle
     return _lib
+
+
+_calls = None  # the loaded extension; False once found missing or turned off
+
+
+def calls():
+    """The per-call extension over the library, initialised; None where it was
+    not built or ``COMMKIT_GB300_CALLS=0``.  It serves ``compute_llr`` and
+    ``decode`` of torch CUDA tensors without a ctypes call or a Python-level
+    allocation; both functions run the same kernels through ctypes without it.
+    """
+    global _calls
+    if _calls is None:
+        handle = lib()  # imports torch first, whose types the extension uses
+        with _lock:
+            if _calls is None:
+                _calls = _load_calls(handle) or False
+    return _calls or None
+
+
+def _load_calls(handle: ctypes.CDLL):
+    if os.environ.get("COMMKIT_GB300_CALLS", "1") == "0" or not CALLS_PATH.exists():
+        return None
+    import importlib.machinery
+    import importlib.util
+
+    try:
+        loader = importlib.machinery.ExtensionFileLoader("commkit_gb300.ck_calls", str(CALLS_PATH))
+        spec = importlib.util.spec_from_file_location("commkit_gb300.ck_calls", CALLS_PATH, loader=loader)
+        mod = importlib.util.module_from_spec(spec)
+        loader.exec_module(mod)
+    except ImportError as e:  # built against another torch: the ctypes calls serve
+        warnings.warn(f"{CALLS_PATH.name} does not load ({e}); rebuild with `python -m commkit_gb300.build`",
+                      RuntimeWarning, stacklevel=3)  # fmt: skip
+        return None
+    from .coding import DecodeResult
+
+    def addr(f):
+        return ctypes.cast(f, ctypes.c_void_p).value
+
+    mod.init(addr(handle.ck_ldpc_decode), addr(handle.ck_ldpc_workspace_size),
+             addr(handle.ck_llr_separable_maxlog), addr(handle.ck_llr_separable), addr(handle.ck_llr_points),
+             DecodeResult)  # fmt: skip
+    return mod
 
 
 def last_error() -> str:

@@ -4,6 +4,8 @@
 for sm_103a only (``-gencode arch=compute_103a,code=sm_103a``), in parallel,
 and links them against the shared CUDA runtime into
 ``commkit_gb300/_lib/libck_gb300.so``.  Objects go to ``commkit_gb300/_build``.
+Beside it, ``csrc/python/ck_calls.cpp`` becomes the per-call CPython
+extension over the installed torch (``_lib/ck_calls*.so``).
 Rebuilds only what changed (sources or headers newer than the object).
 """
 
@@ -13,6 +15,8 @@ import os
 import shutil
 import subprocess
 import sys
+import sysconfig
+import warnings
 from concurrent.futures import ThreadPoolExecutor
 from pathlib import Path
 
@@ -96,13 +100,52 @@ def _compile(src: Path, verbose: bool) -> Path:
     return obj
 
 
+CALLS_SRC = SRC / "python" / "ck_calls.cpp"
+CALLS = LIB_DIR / ("ck_calls" + (sysconfig.get_config_var("EXT_SUFFIX") or ".so"))
+
+
+def build_calls() -> Path | None:
+    """The per-call extension (``compute_llr``/``decode`` of torch tensors
+    without ctypes), compiled against the installed torch's headers and
+    libraries; None, with a warning, where those or Python's headers are
+    missing or the compiler fails (the package then calls through ctypes)."""
+    try:
+        import torch
+    except ImportError:
+        return None
+    tdir = Path(torch.__file__).resolve().parent
+    py_inc = Path(sysconfig.get_paths()["include"])
+    deps = [CALLS_SRC, INCLUDE / "commkit_gb300.h", tdir / "version.py"]
+    if not _stale(CALLS, deps):
+        return CALLS
+    if not (py_inc / "Python.h").exists() or not (tdir / "include" / "ATen").is_dir():
+        warnings.warn("Python or torch headers missing: the per-call extension is not built", stacklevel=2)
+        return None
+    cuda_inc = Path(nvcc()).resolve().parent.parent / "include"
+    tmp = CALLS.with_suffix(f".{os.getpid()}.tmp")
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall",
+           f"-D_GLIBCXX_USE_CXX11_ABI={int(torch.compiled_with_cxx11_abi())}",
+           "-I", str(py_inc), "-I", str(tdir / "include"), "-I", str(tdir / "include" / "torch" / "csrc" / "api" / "include"),
+           "-I", str(cuda_inc), "-I", str(INCLUDE), str(CALLS_SRC), "-o", str(tmp),
+           "-L", str(tdir / "lib"), "-lc10", "-lc10_cuda", "-ltorch_cpu", "-ltorch_python",
+           f"-Wl,-rpath,{tdir / 'lib'}"]  # fmt: skip
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        warnings.warn(f"the per-call extension did not compile:\n{res.stderr[-4000:]}", stacklevel=2)
+        return None
+    os.replace(tmp, CALLS)
+    return CALLS
+
+
 def build(verbose: bool = False) -> Path:
     """Compile and link the library if anything changed; returns its path."""
     BUILD.mkdir(exist_ok=True)
     LIB_DIR.mkdir(exist_ok=True)
     srcs = _sources()
-    with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as pool:
+    with ThreadPoolExecutor(max_workers=min(8, len(srcs) + 1)) as pool:
+        calls = pool.submit(build_calls)
         objs = list(pool.map(lambda s: _compile(s, verbose), srcs))
+        calls.result()
     if _stale(LIB, objs):
         tmp = LIB.with_suffix(f".{os.getpid()}.tmp")
         # The shared CUDA runtime (soname libcudart.so.13): a process that has

@@ -121,6 +121,8 @@ class LDPCCode:
         self.checks, self.variables = rows, cols
         self.num_checks, self.num_variables, self.punctured = m, n, p
         self._plans: dict[int, _Plan] = {}
+        # Per device, what the per-call extension needs to decode this code.
+        self._calls_entries: list | None = None
 
     @classmethod
     def quasi_cyclic(cls, base: Any, *, lifting: int, punctured: int = 0) -> LDPCCode:
@@ -513,7 +515,7 @@ class _Plan:
 
 def _resolve_method(method: Any) -> MinSum | SumProduct:
     if method is None:
-        return MinSum()
+        return _DEFAULT_METHOD
     if not isinstance(method, (MinSum, SumProduct)):
         raise TypeError(
             f"decode(): method {type(method).__name__} does not decode LDPCCode; use MinSum or SumProduct."
@@ -534,7 +536,31 @@ def _rule_args(method: MinSum | SumProduct) -> tuple[int, float, float]:
         else:
             args = (_lib.CK_LDPC_MIN_SUM, float(np.float32(method.scale)), float(np.float32(method.offset)))
         method.__dict__["_c_args"] = args
+        # The whole call as the per-call extension takes it.
+        method.__dict__["_c_call"] = args + (int(method.max_iterations), 1 if method.early_stop else 0)
     return args
+
+
+_DEFAULT_METHOD = MinSum()
+_METHODS = (MinSum, SumProduct)
+_calls_decode = None  # the per-call extension's decode, once a code has registered
+
+
+def _register_calls(code: LDPCCode, device: int, plan: _Plan) -> None:
+    """Lets later ``decode`` calls of ``code`` on ``device`` (contiguous
+    float32 torch LLRs, no workspace given) go straight to the per-call
+    extension: the entry is the plan's handle and the code's sizes, kept in
+    a list indexed by device."""
+    global _calls_decode
+    mod = _lib.calls()
+    if mod is None:
+        return
+    entries = code._calls_entries
+    if entries is None or len(entries) <= device:
+        entries = list(entries or ()) + [None] * (device + 1 - len(entries or ()))
+    entries[device] = (plan.handle.value, code.n, code.k)
+    code._calls_entries = entries
+    _calls_decode = mod.decode
 
 
 def _as_llrs(llrs: Any, x: _device.DeviceArray):
@@ -575,6 +601,18 @@ def decode(llrs: Any, *, code: LDPCCode, method: MinSum | SumProduct | None = No
     """
     if not isinstance(code, LDPCCode):
         raise TypeError(f"decode(): code must be an LDPCCode, got {type(code).__name__}.")
+    entries = code._calls_entries
+    if entries is not None and workspace is None:
+        # A form an earlier call registered: the extension takes it whole, or
+        # returns None and the general path below runs.
+        m = _DEFAULT_METHOD if method is None else method
+        call = m.__dict__.get("_c_call") if isinstance(m, _METHODS) else None
+        if call is not None:
+            r = _calls_decode(llrs, entries, call)
+            if r is not None:
+                if r.__class__ is int:
+                    _lib.check(r, "decode()")
+                return r
     method = _resolve_method(method)
     x0 = _device.wrap(llrs, "llrs")
     if workspace is None and x0.kind == "torch" and x0.dtype == np.float32 and x0.contiguous and code._leading_info:
@@ -679,6 +717,7 @@ def _decode_torch(llrs: Any, x0: _device.DeviceArray, code: LDPCCode, method: Mi
                     valid.data_ptr(), bits.data_ptr(), k, ws.data_ptr(), ws.numel(), stream,
                 )  # fmt: skip
             _lib.check(st, "decode()")
+            _register_calls(code, x0.device, plan)
     return DecodeResult(bits=bits, llrs=out_llrs, valid=valid, iterations=iters, checked=True)
 
 

@@ -329,6 +329,9 @@ class Constellation:
         on the symbols' device (``commkit/mapping/constellation.py:309-332``):
         separable lattices per axis, every other constellation over all its
         points."""
+        out = _calls_llr(symbols, noise_var, self, method)
+        if out is not None:
+            return out
         nv = _finite(noise_var, "Constellation.llr(): noise_var", low=0.0)
         return self._llr(symbols, _device.wrap(symbols, "symbols"), nv, method)
 
@@ -405,6 +408,37 @@ def _noise_variance(noise_var, esn0_db, constellation: Constellation, real: bool
     snr = _finite(esn0_db, f"{fn}: esn0_db")
     n0 = constellation.power() / 10 ** (snr / 10)
     return n0 / 2 if real else n0
+
+
+def _calls_llr(symbols: Any, noise_var: Any, c: Any, method: Any) -> Any:
+    """The per-call extension's demap of a form an earlier call registered
+    (complex64 torch symbols, contiguous, a float noise variance); None when
+    it does not take the call and the general path has to."""
+    per = getattr(c, "_calls_llr", None)
+    if per is None or not isinstance(method, str):
+        return None
+    entries = per.get(method)
+    if entries is None:
+        return None
+    out = _lib.calls().llr(symbols, noise_var, entries)
+    if out.__class__ is int:
+        _lib.check(out, "compute_llr()")
+    return out
+
+
+def _register_calls(c: Constellation, method: str, device: int, entry: tuple) -> None:
+    """Lets later calls of ``c`` and ``method`` on ``device`` go straight to
+    the per-call extension: ``entry`` = (kind, exact, three table addresses,
+    M, k), kind 0 the closed-form max-log, 1 the per-axis levels, 2 every
+    point; kept per method in a list indexed by device."""
+    if _lib.calls() is None:
+        return
+    per = c.__dict__.setdefault("_calls_llr", {})
+    entries = per.get(method) or []
+    if len(entries) <= device:
+        entries = entries + [None] * (device + 1 - len(entries))
+    entries[device] = entry
+    per[method] = entries
 
 
 def inv_s2(noise_var: float) -> float:
@@ -595,6 +629,10 @@ def _llr_separable_gpu(symbols: Any, x: _device.DeviceArray, c: Constellation, n
             st = lib.ck_llr_separable(ptr, n, re_ref, im_ref, inv_s2(nv), 1 if method == "exact" else 0,
                                       out_ptr, stream)  # fmt: skip
         _lib.check(st, "compute_llr()")
+    if x.kind == "torch" and x.contiguous and x.dtype == np.complex64:
+        re, im = _axis_args(c, kind, x)[:2]
+        _register_calls(c, method, x.device, (0 if kind == "maxlog" else 1, 1 if method == "exact" else 0,
+                                              ctypes.addressof(re), ctypes.addressof(im), 0, 0, k))  # fmt: skip
     return out
 
 
@@ -620,6 +658,9 @@ def _llr_points_gpu(symbols: Any, x: _device.DeviceArray, c: Constellation, nv: 
                                       c.order, k, inv_s2(nv), 1 if method == "exact" else 0, od.ptr,
                                       _device.stream_of(x))  # fmt: skip
         _lib.check(st, "compute_llr()")
+    if x.kind == "torch" and x.contiguous and x.dtype == np.complex64:
+        _register_calls(c, method, x.device, (2, 1 if method == "exact" else 0, pts.data_ptr(), logp.data_ptr(),
+                                              lab.data_ptr(), c.order, k))  # fmt: skip
     shape = tuple(x.shape[:-1]) + (x.shape[-1] * k,) if x.ndim else (k,)
     return out.reshape(shape)
 
@@ -633,6 +674,10 @@ def compute_llr(symbols: Any, *, noise_var: float | None = None, esn0_db: float 
     ``method`` ``"maxlog"`` or ``"exact"``.  Returns float32 ``(..., N * k)``
     on the symbols' device, the k bits of a symbol adjacent, MSB first.
     """
+    if esn0_db is None:
+        out = _calls_llr(symbols, noise_var, constellation, method)
+        if out is not None:
+            return out
     if constellation is None:
         raise ValueError("compute_llr(): constellation is required for array input.")
     x = _device.wrap(symbols, "symbols")
