@@ -889,20 +889,23 @@ int resolve_mixed_shape(const ck_ldpc_batch* batches, int32_t n, MixedResolved* 
         need += (R->p.code[c].B + R->p.code[c].G - 1) / R->p.code[c].G;
     R->grid = feed ? sms * per_sm
                    : static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(need, int64_t(sms) * per_sm)));
-    // Starting split of the blocks in proportion to each code's work
-    // (frames x edges x iteration budget), at least one block per code with frames.
-    double total = 0.0, work[kMaxMixed] = {};
-    for (int c = 0; c < n; ++c) {
-        const MixedCode& K = R->p.code[c];
-        work[c] = static_cast<double>(K.B) * K.weight * std::max(1, K.max_iterations) / K.G;
-        total += work[c];
-    }
+    // Starting split, longest frames first (mixed_pick's order): the codes
+    // by edges per frame times iteration budget, heaviest first (stable), each
+    // taking as many blocks as it has frame groups to fill, until the grid is
+    // used up.  Codes without frames, or beyond the grid, start no block.
+    int rank_code[kMaxMixed];
+    for (int c = 0; c < n; ++c) rank_code[c] = c;
+    const auto budget = [&](int c) {
+        return static_cast<double>(R->p.code[c].weight) * std::max(1, R->p.code[c].max_iterations);
+    };
+    std::stable_sort(rank_code, rank_code + n, [&](int a, int b) { return budget(a) > budget(b); });
     int start = 0;
-    for (int c = 0; c < n; ++c) {
-        R->p.start_block[c] = start;
-        int share = total > 0 ? static_cast<int>(R->grid * work[c] / total + 0.5) : 0;
-        if (R->p.code[c].B > 0) share = std::max(share, 1);
-        start = std::min(R->grid, start + share);
+    for (int r = 0; r < n; ++r) {
+        const MixedCode& K = R->p.code[rank_code[r]];
+        R->p.start_code[r] = rank_code[r];
+        R->p.start_block[r] = start;
+        const int64_t blocks = (static_cast<int64_t>(K.B) + K.G - 1) / K.G;
+        start = static_cast<int>(std::min<int64_t>(R->grid, start + blocks));
     }
     R->p.start_block[n] = R->grid;
     // Workspace: counters, then the device-memory message slots.  A block
