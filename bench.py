@@ -53,6 +53,9 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 SEED = 1
+# Input/output sets a demapper leg cycles through, so that no timed launch
+# finds its inputs in L2.
+ROTATE = 4
 METRIC = "decoded info Gb/s at bit-identical FER"
 UNIT = "Gb/s"
 # The measured configurations.
@@ -272,6 +275,27 @@ def timed_flushed(dist: Dist, fn, steps: int, flush) -> float:
         e1.record(stream)
     dist.barrier()
     return dist.max(sum(e0.elapsed_time(e1) for e0, e1 in ev))
+
+
+def timed_rotating(dist: Dist, fns: list, launches: int = 20) -> float:
+    """ms per launch of ``launches`` calls back to back, cycling through
+    ``fns`` (the same call over distinct input and output buffers, together
+    larger than L2, so that no launch finds its inputs in L2).  A device-side
+    pause first lets the host queue every call, so the events time the
+    kernels rather than the host; barrier and sync on both sides."""
+    torch = dist.torch
+    stream = torch.cuda.current_stream(dist.dev)
+    for i in range(2 * len(fns)):
+        fns[i % len(fns)]()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist.barrier()
+    torch.cuda._sleep(4_000_000)
+    e0.record(stream)
+    for i in range(launches):
+        fns[i % len(fns)]()
+    e1.record(stream)
+    dist.barrier()
+    return dist.max(e0.elapsed_time(e1)) / launches
 
 
 def roofline(pk: dict, alg_bytes: float, edge_updates: float, launch_ms: float, sm_count: int,
@@ -622,15 +646,18 @@ def measure_single(args, dist: Dist, wname: str) -> dict:
         return ck.decode(ck.compute_llr(x, noise_var=nv, constellation=const, method=w["method"]),
                          code=code, method=method, workspace=ws)  # fmt: skip
 
+    # Code A's batch (5.3 MB of symbols) fits the L2: every timed step starts
+    # from a flushed L2, as the headline's.
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     for _ in range(args.warmup):
         step(sym)
-    ms = timed(dist, lambda: step(sym), args.steps)
+    ms = timed_flushed(dist, lambda: step(sym), args.steps, flush)
     res = step(sym)
     llr = ck.compute_llr(sym, noise_var=nv, constellation=const, method=w["method"])
     reps = max(3, min(args.steps, 10))
-    demap_ms = timed(dist, lambda: ck.compute_llr(sym, noise_var=nv, constellation=const, method=w["method"]),
-                     reps) / reps  # fmt: skip
-    decode_ms = timed(dist, lambda: ck.decode(llr, code=code, method=method, workspace=ws), reps) / reps
+    demap_ms = timed_flushed(dist, lambda: ck.compute_llr(sym, noise_var=nv, constellation=const, method=w["method"]),
+                             reps, flush) / reps  # fmt: skip
+    decode_ms = timed_flushed(dist, lambda: ck.decode(llr, code=code, method=method, workspace=ws), reps, flush) / reps
     out = [torch.empty((frames, code.k), dtype=torch.int8, pin_memory=True),
            torch.empty((frames, code.n), dtype=torch.float32, pin_memory=True),
            torch.empty((frames, 1), dtype=torch.bool, pin_memory=True),
@@ -643,7 +670,8 @@ def measure_single(args, dist: Dist, wname: str) -> dict:
 
     for _ in range(max(1, args.warmup)):
         e2e_step()
-    e2e_ms = timed(dist, e2e_step, args.steps)
+    e2e_ms = timed_flushed(dist, e2e_step, args.steps, flush)
+    del flush
     iters = res.iterations.reshape(-1).cpu().numpy()
     oracle.build()
     idx = np.linspace(0, frames - 1, min(32, frames)).astype(int)
@@ -667,6 +695,7 @@ def measure_single(args, dist: Dist, wname: str) -> dict:
     return {
         "workload": w["desc"], "value": dist.rate(frames * code.k * args.steps, ms) / 1e9,
         "unit": UNIT, "ms_per_step": ms / args.steps,
+        "l2": "flushed before every timed step (256 MB written outside the timed spans)",
         "e2e": {"value": dist.rate(frames * code.k * args.steps, e2e_ms) / 1e9,
                 "h2d_bytes_per_step": int(sym_host.numel() * 8),
                 "d2h_bytes_per_step": int(sum(t.numel() * t.element_size() for t in out))},
@@ -815,7 +844,9 @@ def decode_error_vs_fp64(post: np.ndarray, iters: np.ndarray, valid: np.ndarray,
 
 def measure_demapper(dist: Dist) -> dict:
     """Config 2: 2^22 symbols in 1024 frames of 4096, per-frame Es/N0 in
-    [8, 20] dB, 16- and 64-QAM, max-log and exact, one batched launch."""
+    [8, 20] dB, 16- and 64-QAM, max-log and exact, one batched launch;
+    timed 20 launches back to back over four sets of symbols and outputs,
+    so that no launch finds its inputs in L2."""
     import commkit_gb300 as ck
     from commkit_gb300 import workloads as W
     from commkit_gb300.mapping import inv_s2_frames
@@ -828,30 +859,21 @@ def measure_demapper(dist: Dist) -> dict:
         x = torch.from_numpy(rx).to(dev)
         s2 = torch.from_numpy(inv_s2_frames(nv)).to(dev)
         c = ck.Constellation.qam(order)
-        res = torch.empty((1024, 4096 * c.bits_per_symbol), dtype=torch.float32, device=dev)
+        # Four sets of symbols and outputs (403 / 537 MB in all, against a
+        # 129 MB L2: 16-QAM's 101 MB of one launch alone would fit it).
+        xs = [x] + [x.clone() for _ in range(ROTATE - 1)]
+        res = [torch.empty((1024, 4096 * c.bits_per_symbol), dtype=torch.float32, device=dev) for _ in xs]
         for method in ("maxlog", "exact"):
-            def fn(method=method):
-                ck.compute_llr_frames(x, constellation=c, method=method, inv_s2=s2, out=res)
-
-            for _ in range(20):  # also brings the clocks up when this leg runs first
-                fn()
-            # 20 launches back to back: a device-side pause first lets the host
-            # queue them all (its per-call work, tens of microseconds, would
-            # otherwise pace a kernel of about that length), so the events
-            # time the kernels.
-            stream = torch.cuda.current_stream(dev)
-            torch.cuda.synchronize(dev)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            torch.cuda._sleep(4_000_000)
-            e0.record(stream)
-            for _ in range(20):
-                fn()
-            e1.record(stream)
-            torch.cuda.synchronize(dev)
-            ms = dist.max(e0.elapsed_time(e1)) / 20
+            fns = [lambda method=method, xi=xi, ri=ri: ck.compute_llr_frames(xi, constellation=c, method=method,
+                                                                             inv_s2=s2, out=ri)
+                   for xi, ri in zip(xs, res, strict=True)]  # fmt: skip
+            for _ in range(5):  # also brings the clocks up when this leg runs first
+                for fn in fns:
+                    fn()
+            ms = timed_rotating(dist, fns)
             nbytes = rx.size * (8 + 4 * c.bits_per_symbol) + 1024 * 4
             k = c.bits_per_symbol
-            got = res.reshape(-1, k)[:FP64_SAMPLE].cpu().numpy()
+            got = res[0].reshape(-1, k)[:FP64_SAMPLE].cpu().numpy()
             ref = llr_fp64(rx.reshape(-1)[:FP64_SAMPLE], c, np.repeat(inv_s2_frames(nv), 4096)[:FP64_SAMPLE],
                            method == "exact")  # fmt: skip
             out[f"qam{order}_{method}"] = {"us": ms * 1e3, "gbs": nbytes / (ms * 1e-3) / 1e9,
@@ -859,55 +881,48 @@ def measure_demapper(dist: Dist) -> dict:
                                            "err_vs_fp64": llr_error_vs_fp64(got, ref)}  # fmt: skip
     # Same-traffic calibration: device-to-device copies (torch copy_ of
     # contiguous buffers, cudaMemcpyAsync) with the demapper's reads and
-    # writes: the 8-byte symbols (reused by every launch, as the kernel's)
-    # copied k / 2 times into an output of 4k bytes per symbol, timed the
-    # same way: what this GPU sustains for that stream with no arithmetic at
-    # all, against the copy peak measured on 2 GB.
+    # writes: the 8-byte symbols copied k / 2 times into an output of 4k
+    # bytes per symbol, timed the same way (L2 flushed first): what this GPU
+    # sustains for that stream with no arithmetic at all, against the copy
+    # peak measured on 2 GB.
     calib = {}
-    src = torch.view_as_real(x).reshape(-1)
+    srcs = [torch.view_as_real(xi).reshape(-1) for xi in xs]
+    del res
     for order in (16, 64):
         reps = int(np.log2(order)) // 2
-        dst = torch.empty((reps, src.numel()), dtype=torch.float32, device=dev)
+        dsts = [torch.empty((reps, srcs[0].numel()), dtype=torch.float32, device=dev) for _ in srcs]
 
-        def copies(dst=dst, reps=reps):
+        def copies(src, dst, reps=reps):
             for r in range(reps):
                 dst[r].copy_(src)
 
-        for _ in range(20):
-            copies()
-        torch.cuda.synchronize(dev)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda._sleep(4_000_000)
-        e0.record()
-        for _ in range(20):
-            copies()
-        e1.record()
-        torch.cuda.synchronize(dev)
-        us = dist.max(e0.elapsed_time(e1)) / 20 * 1e3
-        nbytes = src.numel() * 4 + reps * src.numel() * 4
+        us = timed_rotating(dist, [lambda a=a, b=b: copies(a, b) for a, b in zip(srcs, dsts, strict=True)]) * 1e3
+        nbytes = srcs[0].numel() * 4 + reps * srcs[0].numel() * 4
         calib[f"qam{order}"] = {"copies": reps, "us": us, "gbs": nbytes / (us * 1e-6) / 1e9,
                                 "maxlog_kernel_over_copies": out[f"qam{order}_maxlog"]["us"] / us}  # fmt: skip
-        del dst
-    return {"workload": "2^22 symbols, 1024 frames x 4096, per-frame Es/N0 U[8,20] dB, one launch",
+        del dsts
+    return {"workload": f"2^22 symbols, 1024 frames x 4096, per-frame Es/N0 U[8,20] dB, one launch, 20 launches "
+                        f"back to back over {ROTATE} sets of inputs and outputs (larger than L2 together)",
             "fp64_sample_symbols": FP64_SAMPLE, "results": out,
             "same_traffic_calibration": {"what": "k/2 device-to-device copies of the symbols into a 4k-byte-per-symbol "
-                                                 "output (the demapper's reads and writes, no arithmetic), 20 repeats "
-                                                 "back to back", "results": calib}}  # fmt: skip
+                                                 "output (the demapper's reads and writes, no arithmetic), timed as the "
+                                                 "kernels: 20 back to back over the same rotating buffers",
+                                         "results": calib}}  # fmt: skip
 
 
 def measure_mpoint(dist: Dist) -> dict:
     """The M-point demapper (constellations without per-axis factors) at
     2^22 symbols: 16-PSK and 128-cross-QAM, the reference's non-separable
     benchmark constellations (``benchmarks/bench_llr.py:38-51``, there at
-    2^18 symbols), and 8-QAM; max-log and exact; the L2 is flushed before
-    every launch (its inputs are smaller than L2); device time of the
-    kernel, the call's host work hidden behind a device-side pause."""
+    2^18 symbols), and 8-QAM; max-log and exact; 20 launches back to back
+    over four copies of the symbols (and four outputs), so that no launch
+    finds its inputs in L2; the calls' host work is queued ahead behind a
+    device-side pause, so the events time the kernels."""
     import commkit_gb300 as ck
     from commkit_gb300.mapping import inv_s2
 
     torch, dev = dist.torch, dist.dev
     pk = peaks()
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     out = {}
     for name, c in (("psk16", ck.Constellation.psk(16)), ("qam128_cross", ck.Constellation.qam(128)),
                     ("qam8", ck.Constellation.qam(8))):  # fmt: skip
@@ -915,23 +930,17 @@ def measure_mpoint(dist: Dist) -> dict:
         rng = np.random.default_rng(5)
         x = c.points[rng.integers(0, c.order, n)] + 0.1 * (rng.standard_normal(n) + 1j * rng.standard_normal(n))
         xd = torch.from_numpy(x.astype(np.complex64)).to(dev)
+        xs = [xd] + [xd.clone() for _ in range(ROTATE - 1)]
         for method in ("maxlog", "exact"):
-            for _ in range(3):
-                ck.compute_llr(xd, noise_var=0.05, constellation=c, method=method)
-            times = []
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            for _ in range(10):
-                flush.zero_()
-                # A 0.1 ms device-side pause after the flush: the call's host
-                # work (about 35 us of Python) finishes under it, so the
-                # events time the kernel, not the host.
-                torch.cuda._sleep(200_000)
-                e0.record()
-                ck.compute_llr(xd, noise_var=0.05, constellation=c, method=method)
-                e1.record()
-                e1.synchronize()
-                times.append(e0.elapsed_time(e1))
-            ms = float(dist.max(float(np.median(times))))
+            # Each call allocates its output; the last ROTATE outputs stay
+            # alive, so the outputs rotate over distinct buffers as well.
+            kept = [None] * ROTATE
+
+            def call(i, method=method):
+                kept[i] = ck.compute_llr(xs[i], noise_var=0.05, constellation=c, method=method)
+
+            ms = timed_rotating(dist, [lambda i=i: call(i) for i in range(ROTATE)])
+            del kept
             nbytes = n * (8 + 4 * c.bits_per_symbol)
             got = ck.compute_llr(xd[:FP64_SAMPLE], noise_var=0.05, constellation=c, method=method)
             got = got.cpu().numpy().reshape(FP64_SAMPLE, -1)
@@ -941,7 +950,8 @@ def measure_mpoint(dist: Dist) -> dict:
                                        "gbs": nbytes / (ms * 1e-3) / 1e9,
                                        "frac": nbytes / (ms * 1e-3) / 1e9 / pk["hbm_gbs"],
                                        "err_vs_fp64": llr_error_vs_fp64(got, ref)}  # fmt: skip
-    return {"workload": "M-point demapping, 2^22 symbols per call (public compute_llr, L2 flushed)",
+    return {"workload": "M-point demapping, 2^22 symbols per call (public compute_llr), 20 calls back to back "
+                        f"over {ROTATE} sets of symbols and outputs (larger than L2 together)",
             "fp64_sample_symbols": FP64_SAMPLE, "results": out}
 
 
