@@ -88,9 +88,9 @@ WORKLOADS = {
 # per edge), dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture (--set full) of a
 # 2048-frame batch of the same mix on GB300: 20.16 + 24.91 MB.  It grows with the frames, so a
 # launch's traffic is scaled by its frame count.
-MIXED_DRAM_BYTES_PER_FRAME = (20.157184e6 + 24.912128e6) / 2048
+MIXED_DRAM_BYTES_PER_FRAME = (20.283648e6 + 23.402752e6) / 2048
 MIXED_TRAFFIC_NOTE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of a 2048-frame launch of the same mix "
-                      "(fused demapping), scaled by frames (45.1 MB / 2048 frames)")
+                      "(fused demapping, codes longest first), scaled by frames (43.7 MB / 2048 frames)")
 
 
 def parse() -> argparse.Namespace:
